@@ -1,0 +1,360 @@
+"""Benchmark of the osinco3d hot path on GB300: Mpt-steps/s of whole time
+steps (predictor, projection with the pressure Poisson solve, correction and
+the per-step diagnostics) on the Taylor-Green vortex at 256^3, Re = 1600,
+AB3, CFL 0.2, Poisson eps = 1e-8.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+One JSON line on stdout (rank 0).  `value` is the mixed-precision method
+(FP32 stencils and V-cycles inside the FP64 defect-correction loop); the
+plain-FP64 multigrid and red-black SOR steps are in `variants`.  With
+--impl reference the FP64 CPU restatement of the reference (the oracle; the
+Fortran reference has no compiler here) is timed on the host cores instead.
+
+With N > 1 (torchrun) every rank runs an independent replica of the same
+workload on its own GPU (the path has no data exchange): value = all points
+x steps over the max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N = 256
+EPS = 1e-8
+METRIC = "Mpt-steps/s at 256^3; Poisson s/step learned+mixed vs plain FP64 at same eps"
+WORKLOAD = ("Taylor-Green vortex 256^3 periodic [0,2pi)^3 (xlx = 2pi*255/256), Re=1600, AB3, "
+            "CFL=0.2 (dt=0.2*2pi/256), Poisson eps=1e-8, no LES, no scalar")
+
+# algorithmic bytes per grid point of one launch (float32 storage)
+PRED_BYTES_PER_PT = 15 * 4   # read u,v,w + 6 history, write 3 u* + 3 fluxes
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (replicas only)
+# ---------------------------------------------------------------------------
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        rows = []
+        if self.path and os.path.exists(self.path):
+            for ln in open(self.path):
+                parts = [p.strip() for p in ln.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+            os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = sorted(float(r[1]) for r in rows if r[1].replace(".", "").isdigit())
+        mx = max((float(r[2]) for r in rows if r[2].replace(".", "").isdigit()), default=None)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+_PINNED: list = []
+
+
+def pinned_field(shape):
+    """Fortran-ordered float64 array in page-locked host memory."""
+    import numpy as np
+    import torch
+
+    n = shape[0] * shape[1] * shape[2]
+    t = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    _PINNED.append(t)  # the numpy view does not own the page-locked memory
+    return t.numpy().reshape(shape, order="F")
+
+
+def run_variant(o3d, name: str, steps: int, warmup: int, world: int, **kw) -> dict:
+    import numpy as np
+
+    p = o3d.tgv_params(N, eps=EPS, **kw)
+    ctx = o3d.Context(p)
+    ux, uy, uz, pp = o3d.tgv_fields(p)
+    for nm, f in zip(("ux", "uy", "uz", "pp"), (ux, uy, uz, pp)):
+        ctx.upload(nm, f)
+    it = 0
+    for _ in range(warmup):
+        it += 1
+        ctx.step(it)
+    barrier(world)
+    l0 = ctx.launches
+    ms, pms, iters, cyc, res = [], [], [], [], []
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        it += 1
+        info = ctx.step(it)
+        ms.append(info.step_ms)
+        pms.append(info.poisson_ms)
+        iters.append(info.poisson_iters)
+        cyc.append(info.poisson_cycles)
+        res.append(info.poisson_res_inf)
+    wall = time.perf_counter() - t0
+    launches = ctx.launches - l0
+    dev_s = max_over_ranks(sum(ms) / 1e3, world)
+    out = {
+        "name": name,
+        "ms_per_step": 1e3 * dev_s / steps,
+        "mpts_per_s": world * (N ** 3) * steps / dev_s / 1e6,
+        "wall_ms_per_step": 1e3 * wall / steps,
+        "poisson_s_per_step": sum(pms) / 1e3 / steps,
+        "poisson_iters_per_step": sum(iters) / steps,
+        "vcycles_per_step": sum(cyc) / steps,
+        "poisson_res_inf_last": res[-1],
+        "gpu_launches": launches,
+        "omega": ctx.omega,
+    }
+    return out, ctx, it
+
+
+def measure_e2e(o3d, steps: int, warmup: int, world: int, **kw) -> dict:
+    """Same steps through o3d_step_host: the driver's host arrays (page-locked)
+    are copied in before and out after every step."""
+    p = o3d.tgv_params(N, eps=EPS, **kw)
+    ux0, uy0, uz0, pp0 = o3d.tgv_fields(p)
+    bufs = [pinned_field(ux0.shape) for _ in range(4)]
+    for b, f in zip(bufs, (ux0, uy0, uz0, pp0)):
+        b[...] = f
+    with o3d.Context(p) as ctx:
+        it = 0
+        for _ in range(warmup):
+            it += 1
+            ctx.step_host(it, *bufs)
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            it += 1
+            ctx.step_host(it, *bufs)
+        wall = max_over_ranks(time.perf_counter() - t0, world)
+    nbytes = 4 * (N ** 3) * 8
+    return {"value": world * (N ** 3) * steps / wall / 1e6, "unit": "Mpt-steps/s",
+            "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+            "ms_per_step": 1e3 * wall / steps}
+
+
+def predictor_roofline(o3d, ctx, peaks: dict) -> dict:
+    """Device time of the fused predictor kernel on the live state, CUDA events
+    on the context's stream, averaged over repeated launches."""
+    t = ctx.time_kernel("predict", 20)
+    achieved = PRED_BYTES_PER_PT * N ** 3 / (t * 1e-3) / 1e9
+    peak = peaks.get("hbm_gbs")
+    return {"kernel": "k_predict<float>", "ms": t, "achieved": achieved, "peak": peak,
+            "frac": achieved / peak if peak else None}
+
+
+def cpu_baseline_oracle(seconds_budget: float = 20.0, omp: bool = False, sweeps: int = 30) -> dict:
+    """FP64 oracle (serial restatement of the reference) on one bounded
+    sample of the workload: one time step at 256^3 with the lexicographic SOR
+    capped at `sweeps` sweeps (the GPU needs more, so this overstates the CPU
+    rate)."""
+    from oracle import oracle as orc
+
+    orc.build()
+    L = 2 * math.pi * (N - 1) / N
+    case = orc.Case(N, N, N, L, L, L, dt=0.2 * 2 * math.pi / N, omega=2.0 / (1.0 + math.sin(math.pi * 2 * math.pi / N)),
+                    eps=EPS, kmax=sweeps)
+    st = orc.State.zeros(case)
+    orc.init_tgv(case, st, omp=omp)
+    r = orc.Runner(case, st, omp=omp)
+    t0 = time.perf_counter()
+    r.step(1)
+    dt = time.perf_counter() - t0
+    cores = (os.cpu_count() or 1) if omp else 1
+    return {"value": N ** 3 / dt / 1e6, "unit": "Mpt-steps/s", "cores": cores, "kind": "port",
+            "sample": f"1 time step of the 256^3 workload in FP64 on the oracle (C restatement), "
+                      f"lexicographic SOR capped at {sweeps} sweeps; {dt:.1f} s",
+            "seconds": dt}
+
+
+def load_peaks() -> dict:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        d["source"] = "measured"
+        return d
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
+
+
+def gpu_arm(args, rank, world, local):
+    from osinco3d_gb300 import o3d
+
+    o3d.lib()
+    peaks = load_peaks()
+    variants = {}
+    with ClockSampler(local) as clk:
+        head, ctx, _ = run_variant(o3d, "mixed_mg", args.steps, args.warmup, world,
+                                   precision=o3d.PREC_MIXED, solver=o3d.SOLVER_MG, kmax=100)
+    clocks = clk.summary()
+    roof = predictor_roofline(o3d, ctx, peaks)
+    ctx.close()
+    variants["mixed_mg"] = head
+    if not args.quick:
+        v, c2, _ = run_variant(o3d, "fp64_mg", args.steps, args.warmup, world,
+                               precision=o3d.PREC_FP64, solver=o3d.SOLVER_MG, kmax=100)
+        c2.close()
+        variants["fp64_mg"] = v
+        sor_steps = max(2, args.steps // 4)
+        v, c3, _ = run_variant(o3d, "fp64_rbsor", sor_steps, min(args.warmup, 3), world,
+                               precision=o3d.PREC_FP64, solver=o3d.SOLVER_SOR, kmax=20000)
+        c3.close()
+        variants["fp64_rbsor"] = v
+    e2e = measure_e2e(o3d, max(3, args.steps // 2), 3, world, precision=o3d.PREC_MIXED,
+                      solver=o3d.SOLVER_MG, kmax=100)
+    line = {
+        "metric": METRIC,
+        "value": head["mpts_per_s"],
+        "unit": "Mpt-steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": head["ms_per_step"],
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "fp32 stencils/V-cycles + fp64 defect correction",
+        "data": "synthetic (analytic Taylor-Green initial state)",
+        "config": {"workload": WORKLOAD, "grid": [N, N, N], "poisson": "multigrid V(2,2) in FP64 defect correction",
+                   "parallelism": f"replicas x{world}", "l2": "no flush: every step streams > 1 GB, far above the 129 MB L2"},
+        "e2e": e2e,
+        "gpu_launches": head["gpu_launches"],
+        "clocks": clocks,
+        "variants": variants,
+    }
+    line["roofline"] = {"bound": "hbm", "achieved": roof["achieved"], "peak": roof["peak"], "unit": "GB/s",
+                        "frac": roof["frac"], "traffic": None, "kernel": roof["kernel"],
+                        "bytes_per_point": PRED_BYTES_PER_PT, "ms": roof["ms"],
+                        "peak_source": peaks.get("source")}
+    if "fp64_mg" in variants:
+        line["speedup_mixed_vs_fp64_mg"] = variants["fp64_mg"]["ms_per_step"] / head["ms_per_step"]
+        line["speedup_mixed_vs_fp64_rbsor"] = variants["fp64_rbsor"]["ms_per_step"] / head["ms_per_step"]
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline_oracle()
+    return line
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return None
+    samples = []
+    for k in range(args.warmup + args.steps):
+        r = cpu_baseline_oracle(omp=True, sweeps=10)
+        if k >= args.warmup:
+            samples.append(r)
+    sec = sum(s["seconds"] for s in samples)
+    val = N ** 3 * len(samples) / sec / 1e6
+    cb = {"value": val, "unit": "Mpt-steps/s", "cores": samples[0]["cores"], "kind": "port",
+          "sample": "per step: 1 time step of the 256^3 workload in FP64 on the oracle (C restatement, "
+                    "OpenMP on the stencil passes, lexicographic SOR serial as in the reference) with the "
+                    "SOR capped at 10 sweeps"}
+    return {"metric": METRIC, "value": val, "unit": "Mpt-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * sec / len(samples), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "grid": [N, N, N]}, "impl": "reference",
+            "cpu_baseline": cb, "e2e": {"value": val, "unit": "Mpt-steps/s", "h2d_bytes_per_step": 0,
+                                        "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--quick", action="store_true", help="headline variant only")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, world, local = dist_setup()
+    if args.impl == "reference":
+        line = reference_arm(args, rank, world)
+    else:
+        line = gpu_arm(args, rank, world, local)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,214 @@
+/*
+ * o3d.h -- C ABI of libo3d.so, the GB300 (sm_103a) implementation of
+ * osinco3d's per-step hot path: the 6th/4th-order stencils, the Smagorinsky
+ * eddy viscosity, the AB1/AB2/AB3 predictor, the projection and the pressure
+ * Poisson solve.
+ *
+ * Conventions
+ *  - Fields are column-major (nx, ny, nz) with x fastest, exactly as the
+ *    Fortran driver's real(8) arrays; a Fortran caller passes c_loc(ux) etc.
+ *  - Every function returns an int status: O3D_OK (0), a positive warning or
+ *    a negative error.  Nothing here calls exit() or abort().
+ *  - A context owns its device memory and one CUDA stream; fields stay
+ *    device-resident between calls.  A context is not thread-safe.
+ *  - Host-pointer entry points copy in and out; *_dev entry points take
+ *    device pointers and run on the context's stream.
+ *
+ * Each entry point names the reference routine it replaces (file:line in the
+ * osinco3d source tree).
+ */
+#ifndef O3D_H
+#define O3D_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define O3D_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define O3D_API __attribute__((visibility("default")))
+#else
+#define O3D_API
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  O3D_OK = 0,
+  O3D_WARN_POISSON_MAXIT = 1,   /* solver stopped at kmax (src/poisson.f90:53) */
+  O3D_WARN_STAGNATION = 2,      /* |dmax_old - dmax| < eps/1000 (src/poisson.f90:111-114) */
+  O3D_ERR_BADARG = -1,          /* unsupported size/BC/option (src/initialization.f90:238-242) */
+  O3D_ERR_CUDA = -2,            /* a CUDA call failed; see o3d_last_error() */
+  O3D_ERR_NONFINITE = -3,       /* NaN or max(u) > 1000 after correction (src/integration.f90:309-325) */
+  O3D_ERR_NOMEM = -4,           /* device allocation failed */
+  O3D_ERR_NOT_BUILT = -5        /* feature compiled out or network weights missing */
+};
+
+/* boundary codes, src/initialization.f90:74-75 */
+enum { O3D_BC_PERIODIC = 0, O3D_BC_FREE_SLIP = 1 };
+
+/* arithmetic of the step */
+enum {
+  O3D_PREC_FP64 = 0,   /* every kernel in FP64 (the plain method) */
+  O3D_PREC_MIXED = 1   /* FP32 stencils and V-cycles inside an FP64 defect-correction loop */
+};
+
+/* pressure solver */
+enum {
+  O3D_SOLVER_SOR = 0,  /* red-black SOR, same operator, stop test and dynamic omega as src/poisson.f90 */
+  O3D_SOLVER_MG = 1    /* geometric multigrid V(pre,post) cycles, FP64 outer correction loop */
+};
+
+/* initial guess of each pressure solve */
+enum {
+  O3D_GUESS_PREVIOUS = 0, /* previous step's pressure (the reference: pp persists) */
+  O3D_GUESS_ZERO = 1,
+  O3D_GUESS_LEARNED = 2   /* 3D U-Net prediction from (div u*, previous p) */
+};
+
+/* field identifiers for o3d_upload / o3d_download */
+enum {
+  O3D_FIELD_UX = 0, O3D_FIELD_UY = 1, O3D_FIELD_UZ = 2, O3D_FIELD_PP = 3,
+  O3D_FIELD_UX_PRED = 4, O3D_FIELD_UY_PRED = 5, O3D_FIELD_UZ_PRED = 6,
+  O3D_FIELD_PHI = 7, O3D_FIELD_SRC = 8, O3D_FIELD_NU_T = 9,
+  O3D_FIELD_RHS = 10,     /* last Poisson right-hand side, div(u*)/dt */
+  /* flux history: component c (0..2), age h (0 = newest, 1 = one step older) */
+  O3D_FIELD_FU0 = 16,     /* + 2*c + h */
+  O3D_FIELD_FPHI0 = 24    /* + h */
+};
+
+/* Mirrors the namelists of parameters.o3d (src/initialization.f90:117-125)
+ * plus the options this implementation adds. */
+typedef struct o3d_params {
+  /* &Domain */
+  int nx, ny, nz;
+  double xlx, yly, zlz;   /* node-inclusive: dx = xlx/(nx-1), src/initialization.f90:182 */
+  double x0, y0, z0;
+  /* &BoundaryConditions */
+  int nbcx1, nbcxn, nbcy1, nbcyn, nbcz1, nbczn, sim2d;
+  /* &AdvanceTime */
+  int itscheme;           /* 1 Euler, 2 AB2, 3 AB3 */
+  double dt;
+  /* &FlowParam */
+  double re;
+  /* &PoissonEq */
+  double omega, eps;
+  int kmax, idyn;
+  /* &Scalar */
+  int nscr;
+  double sc;
+  /* &LES */
+  int iles;
+  double cs;
+  /* additions */
+  int precision;          /* O3D_PREC_* */
+  int solver;             /* O3D_SOLVER_* */
+  int mg_levels;          /* 0 = as many as the grid allows */
+  int mg_pre, mg_post;    /* smoothing sweeps; 0 -> 2 */
+  int guess;              /* O3D_GUESS_* */
+  int diagnostics;        /* 1: per-step div/CFL/min-max reductions as the driver prints them */
+} o3d_params;
+
+/* Fills *p with the defaults of the reference's namelists (periodic 64^3). */
+O3D_API void o3d_default_params(o3d_params *p);
+
+/* What one time step reports (the values the reference prints each step). */
+typedef struct o3d_step_info {
+  int poisson_status;       /* O3D_OK / O3D_WARN_* */
+  int poisson_iters;        /* SOR sweeps or MG outer iterations */
+  int poisson_cycles;       /* V-cycles (MG) */
+  double poisson_dmax;      /* last max |p_gs - p| (SOR) or max |correction| (MG) */
+  double poisson_res_inf;   /* max |rhs - A p| after the solve, FP64 */
+  double omega;             /* SOR relaxation after the dynamic update */
+  int diverged;             /* 1 if NaN or max(u) > 1000 */
+  double divu_pred_stats[6];/* min, max, mean, imax, jmax, kmax of div(u*) */
+  double divu_stats[6];     /* same for div(u) after the correction */
+  double cfl[3];            /* src/utils.f90:202-204 */
+  double umin[3], umax[3];  /* velocity extrema per component */
+  double poisson_ms;        /* device time of the pressure solve */
+  double step_ms;           /* device time of the whole step */
+} o3d_step_info;
+
+typedef struct o3d_ctx o3d_ctx;
+
+/* Creates a context: validates the parameters like schemes()
+ * (src/initialization.f90:226-304), allocates device fields, zeroes them
+ * (src/initialization.f90:170-178) and sets dx, AB coefficients and the LES
+ * width (src/initialization.f90:182-209). */
+O3D_API int o3d_create(const o3d_params *p, o3d_ctx **out);
+O3D_API int o3d_destroy(o3d_ctx *ctx);
+O3D_API const char *o3d_last_error(void);
+/* Number of kernel launches this context has issued. */
+O3D_API long long o3d_launch_count(const o3d_ctx *ctx);
+/* The context's CUDA stream (a cudaStream_t) for callers that enqueue work. */
+O3D_API void *o3d_stream(o3d_ctx *ctx);
+
+/* Field transfer, host buffers of nx*ny*nz doubles. */
+O3D_API int o3d_upload(o3d_ctx *ctx, int field, const double *host);
+O3D_API int o3d_download(o3d_ctx *ctx, int field, double *host);
+
+/* der_type(df, f, d), src/initialization.f90:86-91: one derivative of f along
+ * axis (0 x, 1 y, 2 z), order 1 (6th-order, src/derivation.f90:6-479) or 2
+ * (4th-order, src/derivation.f90:497-932), parity 0 = even ("p" routines),
+ * 1 = odd ("i" routines), using the context's boundary types and spacing.
+ * FP64, host buffers. */
+O3D_API int o3d_der(o3d_ctx *ctx, int axis, int order, int odd, const double *f, double *df);
+O3D_API int o3d_der_dev(o3d_ctx *ctx, int axis, int order, int odd, const double *d_f, double *d_df);
+
+/* divergence(divf, fx, fy, fz, ..., odd), src/differential_operators.f90:7-38. FP64, host. */
+O3D_API int o3d_divergence(o3d_ctx *ctx, const double *fx, const double *fy,
+                   const double *fz, int odd, double *divf);
+/* calculate_nu_t from the context's velocity into O3D_FIELD_NU_T,
+ * src/les_turbulence.f90:10-97. */
+O3D_API int o3d_calculate_nu_t(o3d_ctx *ctx);
+
+/* predict_velocity(...), src/integration.f90:14-197: context fields
+ * ux,uy,uz and the flux history -> ux_pred.., new flux, history rotated. */
+O3D_API int o3d_predict_velocity(o3d_ctx *ctx, int itime);
+/* correct_pression(...), src/integration.f90:199-255: rhs = div(u*)/dt and
+ * the pressure solve; omega is read and written back like the Fortran
+ * intent(inout) argument. */
+O3D_API int o3d_correct_pression(o3d_ctx *ctx, double *omega, o3d_step_info *info);
+/* correct_velocity(...), src/integration.f90:257-330. Returns
+ * O3D_ERR_NONFINITE where the reference stops. */
+O3D_API int o3d_correct_velocity(o3d_ctx *ctx);
+/* transeq(...), src/integration.f90:332-468 (passive scalar). */
+O3D_API int o3d_transeq(o3d_ctx *ctx, int itime);
+
+/* poi_type(pp, rhs, dx,dy,dz, nx,ny,nz, omega, eps, kmax, idyn),
+ * src/initialization.f90:93-102: solve A pp = rhs with the context's
+ * solver, host buffers, pp is the initial guess and the result. */
+O3D_API int o3d_poisson_solve(o3d_ctx *ctx, double *pp, const double *rhs, double *omega,
+                      double eps, int kmax, int idyn, int *iters, double *dmax);
+
+/* One iteration of the time loop, src/osinco3d_main.f90:104-128, without I/O. */
+O3D_API int o3d_step(o3d_ctx *ctx, int itime, o3d_step_info *info);
+/* Same, with the driver's host arrays: ux,uy,uz,pp are copied in before the
+ * step and out after it (the flux history stays on the device). */
+O3D_API int o3d_step_host(o3d_ctx *ctx, int itime, double *ux, double *uy, double *uz,
+                  double *pp, o3d_step_info *info);
+
+/* statistics_calc(...), src/utils.f90:243-375: out[17] = t, E_k, eps, eps2,
+ * dzeta, <u^2>, <v^2>, <w^2>, nine <(du_i/dx_j)^2>, FP64 reductions. */
+O3D_API int o3d_statistics_calc(o3d_ctx *ctx, double t, double out[17]);
+
+/* Device time of one launch of a hot kernel on the live state, averaged over
+ * `reps` back-to-back launches timed with CUDA events on the context's stream.
+ * kernel: 0 fused predictor, 1 divergence -> rhs, 2 velocity correction,
+ * 3 multigrid smoother colour pass on the finest level, 4 FP64 residual of
+ * the defect-correction loop.  The launches only rewrite scratch outputs
+ * (u*, the free flux slot, rhs, the finest-level correction and residual) or
+ * recompute the velocity identically from u* and p.  No counterpart in the
+ * reference (measurement hook). */
+O3D_API int o3d_time_kernel(o3d_ctx *ctx, int kernel, int reps, double *ms_per_launch);
+
+/* Red-black SOR sweep(s) alone on device buffers: for tests of the kernel. */
+O3D_API int o3d_rbsor_sweeps_dev(o3d_ctx *ctx, double *d_pp, const double *d_rhs, double omega,
+                         int nsweeps, double *dmax_last);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,945 @@
+// o3d_api.cu -- context management and host orchestration of the step,
+// behind the extern "C" entry points declared in include/o3d.h.
+//
+// One context = one grid, one CUDA stream, device-resident fields.  Field
+// storage is FP64 for the plain method and FP32 for the mixed method; the
+// pressure is FP64 in both (it is the unknown of the FP64 defect-correction
+// loop).  The Adams-Bashforth flux history is a ring of three buffers per
+// component, so the history shift of src/integration.f90:176-188 costs no
+// copy.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "o3d_internal.cuh"
+#include "o3d_kernels.h"
+
+using namespace o3d;
+
+static thread_local char g_err[512] = "";
+
+static void errf(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof g_err, fmt, ap);
+  va_end(ap);
+}
+
+static double bits_to_double(unsigned long long k) {
+  double d;
+  memcpy(&d, &k, 8);
+  return d;
+}
+
+#define CK(call)                                                                       \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess) {                                                           \
+      snprintf(g_err, sizeof g_err, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+               __FILE__, __LINE__);                                                    \
+      return O3D_ERR_CUDA;                                                             \
+    }                                                                                  \
+  } while (0)
+
+#define CKL()                                                                          \
+  do {                                                                                 \
+    cudaError_t e_ = cudaGetLastError();                                               \
+    if (e_ != cudaSuccess) {                                                           \
+      snprintf(g_err, sizeof g_err, "kernel launch failed: %s (%s:%d)",               \
+               cudaGetErrorString(e_), __FILE__, __LINE__);                            \
+      return O3D_ERR_CUDA;                                                             \
+    }                                                                                  \
+  } while (0)
+
+struct o3d_ctx {
+  o3d_params P;
+  Grid g;        // stencil grid: per-axis closure of the derivative routines
+  Grid gp;       // Poisson grid: remap of the chosen poisson_solver_* routine
+  Coef3<double> cf;
+  double dx, dy, dz, delta;
+  double adt[3], bdt[3], cdt[3];
+  double omega;
+  int mixed;
+  size_t esz;
+  cudaStream_t s;
+
+  void* u[3];
+  void* up[3];
+  void* fu[3][3];    // ring: [0] newest flux, [1] one older, [2] free
+  void* nu_t;
+  void* phi;
+  void* phi2;
+  void* src;
+  void* fphi[3];
+  void* rhs;
+  double* pp;
+  double* stage[4];  // FP64 staging buffers for host transfers (lazy)
+
+  double* part;      // per-block reduction records
+  StatPart* spart;
+  DevDiag* diag;
+  DevDiag* diag_h;   // pinned
+  SolveCtrl* ctrl;
+  SolveCtrl* ctrl_h; // pinned
+
+  std::vector<MGLevel> mg;
+  int mg_ok;
+  cudaGraphExec_t sor_exec;
+  int sor_batch;
+  long long sor_nodes;
+  cudaGraphExec_t mg_exec;
+  int mg_batch;
+  long long mg_nodes;
+
+  cudaEvent_t ev[4];
+  long long launches;
+};
+
+namespace {
+
+// Allocates and zero-fills on the context's stream.  The stream is
+// non-blocking, so a plain cudaMemset (legacy default stream) could land
+// after later uploads on the context's stream.
+int dalloc(cudaStream_t s, void** p, size_t bytes) {
+  if (cudaMalloc(p, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    snprintf(g_err, sizeof g_err, "cudaMalloc of %zu bytes failed", bytes);
+    *p = nullptr;
+    return O3D_ERR_NOMEM;
+  }
+  if (cudaMemsetAsync(*p, 0, bytes, s) != cudaSuccess) return O3D_ERR_CUDA;
+  return O3D_OK;
+}
+
+size_t fbytes(const o3d_ctx* c) { return (size_t)c->g.n * c->esz; }
+
+int stage_ready(o3d_ctx* c, int k) {
+  for (int q = 0; q <= k; ++q)
+    if (!c->stage[q]) {
+      int st = dalloc(c->s, (void**)&c->stage[q], (size_t)c->g.n * sizeof(double));
+      if (st) return st;
+    }
+  return O3D_OK;
+}
+
+// host double buffer -> device field of the context's storage type
+int put_field(o3d_ctx* c, void* dst, const double* host) {
+  if (!c->mixed) {
+    CK(cudaMemcpyAsync(dst, host, (size_t)c->g.n * 8, cudaMemcpyHostToDevice, c->s));
+    return O3D_OK;
+  }
+  int st = stage_ready(c, 0);
+  if (st) return st;
+  CK(cudaMemcpyAsync(c->stage[0], host, (size_t)c->g.n * 8, cudaMemcpyHostToDevice, c->s));
+  launch_convert<double, float>(c->stage[0], (float*)dst, c->g.n, c->s);
+  c->launches++;
+  CKL();
+  return O3D_OK;
+}
+
+int get_field(o3d_ctx* c, const void* src, double* host) {
+  if (!c->mixed) {
+    CK(cudaMemcpyAsync(host, src, (size_t)c->g.n * 8, cudaMemcpyDeviceToHost, c->s));
+    return O3D_OK;
+  }
+  int st = stage_ready(c, 0);
+  if (st) return st;
+  launch_convert<float, double>((const float*)src, c->stage[0], c->g.n, c->s);
+  c->launches++;
+  CKL();
+  CK(cudaMemcpyAsync(host, c->stage[0], (size_t)c->g.n * 8, cudaMemcpyDeviceToHost, c->s));
+  return O3D_OK;
+}
+
+void* field_ptr(o3d_ctx* c, int f, bool* is_pp) {
+  *is_pp = false;
+  switch (f) {
+    case O3D_FIELD_UX: return c->u[0];
+    case O3D_FIELD_UY: return c->u[1];
+    case O3D_FIELD_UZ: return c->u[2];
+    case O3D_FIELD_PP: *is_pp = true; return c->pp;
+    case O3D_FIELD_UX_PRED: return c->up[0];
+    case O3D_FIELD_UY_PRED: return c->up[1];
+    case O3D_FIELD_UZ_PRED: return c->up[2];
+    case O3D_FIELD_PHI: return c->phi;
+    case O3D_FIELD_SRC: return c->src;
+    case O3D_FIELD_NU_T: return c->nu_t;
+    case O3D_FIELD_RHS: return c->rhs;
+    default: break;
+  }
+  if (f >= O3D_FIELD_FU0 && f < O3D_FIELD_FU0 + 6) {
+    int q = f - O3D_FIELD_FU0;
+    return c->fu[q / 2][q % 2];
+  }
+  if (f >= O3D_FIELD_FPHI0 && f < O3D_FIELD_FPHI0 + 2) return c->fphi[f - O3D_FIELD_FPHI0];
+  return nullptr;
+}
+
+// AB coefficients of the step, src/integration.f90:84-98
+void ab_coefs(const o3d_ctx* c, int itime, double* a, double* b, double* cc) {
+  int s = (c->P.itscheme == 1 || itime == 1) ? 0 : (c->P.itscheme == 2 || itime == 2) ? 1 : 2;
+  *a = c->adt[s];
+  *b = c->bdt[s];
+  *cc = c->cdt[s];
+}
+
+void rotate_ring(void* r[3]) {
+  void* a = r[0];
+  void* b = r[1];
+  void* f = r[2];
+  r[0] = f;  // the new flux becomes the newest history
+  r[1] = a;  // the previous newest ages by one
+  r[2] = b;  // the oldest buffer is free for the next step
+}
+
+template <class T>
+int predict_t(o3d_ctx* c, int itime) {
+  double a, b, cc;
+  ab_coefs(c, itime, &a, &b, &cc);
+  PredArgs<T> A;
+  for (int q = 0; q < 3; ++q) {
+    A.u[q] = (const T*)c->u[q];
+    A.up[q] = (T*)c->up[q];
+    A.fnew[q] = (T*)c->fu[q][2];
+    A.f2[q] = b != 0.0 ? (const T*)c->fu[q][0] : nullptr;
+    A.f3[q] = cc != 0.0 ? (const T*)c->fu[q][1] : nullptr;
+  }
+  A.nu_t = (T*)c->nu_t;
+  A.g = c->g;
+  A.cf = cast_coef<T>(c->cf);
+  A.adu = (T)a;
+  A.bdu = (T)b;
+  A.cdu = (T)cc;
+  A.onere = (T)(1.0 / c->P.re);
+  const double csd = c->P.cs * c->delta;
+  A.csd2 = (T)(csd * csd);
+  A.les = c->P.iles == 1;
+  launch_predict<T>(A, c->s);
+  c->launches++;
+  CKL();
+  // history shift (src/integration.f90:176-188) as a ring rotation; with
+  // Euler (itscheme 1) the history is never read, so rotating is harmless
+  for (int q = 0; q < 3; ++q) {
+    if (c->P.itscheme == 2) {
+      void* t = c->fu[q][0];
+      c->fu[q][0] = c->fu[q][2];
+      c->fu[q][2] = t;
+    } else {
+      rotate_ring(c->fu[q]);
+    }
+  }
+  return O3D_OK;
+}
+
+template <class T>
+int rhs_t(o3d_ctx* c) {
+  Coef3<T> cf = cast_coef<T>(c->cf);
+  launch_div<T, T>((const T*)c->up[0], (const T*)c->up[1], (const T*)c->up[2], (T*)c->rhs, c->g, cf,
+                   1, (T)c->P.dt, 1, c->spart, c->s);
+  launch_finalize_stats(c->spart, pt_blocks(c->g), c->g, c->diag->divp, c->s);
+  c->launches += 2;
+  CKL();
+  return O3D_OK;
+}
+
+template <class T>
+int correct_t(o3d_ctx* c) {
+  CorrArgs<T, double> A;
+  A.p = c->pp;
+  for (int q = 0; q < 3; ++q) {
+    A.up[q] = (const T*)c->up[q];
+    A.u[q] = (T*)c->u[q];
+  }
+  A.g = c->g;
+  A.cf = cast_coef<T>(c->cf);
+  A.dt = (T)c->P.dt;
+  A.part = c->part;
+  launch_correct<T, double>(A, c->s);
+  // min x3, max x3, |max| x3, nan flag
+  unsigned long long ops = 0;
+  for (int q = 0; q < 10; ++q) ops |= (unsigned long long)(q < 3 ? RED_MIN : RED_MAX) << (2 * q);
+  launch_finalize(c->part, pt_blocks(c->g), 10, ops, c->diag->sums, c->s);
+  c->launches += 2;
+  CKL();
+  return O3D_OK;
+}
+
+template <class T>
+int divu_diag_t(o3d_ctx* c) {
+  Coef3<T> cf = cast_coef<T>(c->cf);
+  launch_div<T, T>((const T*)c->u[0], (const T*)c->u[1], (const T*)c->u[2], (T*)nullptr, c->g, cf, 1,
+                   (T)c->P.dt, 0, c->spart, c->s);
+  launch_finalize_stats(c->spart, pt_blocks(c->g), c->g, c->diag->divu, c->s);
+  c->launches += 2;
+  CKL();
+  return O3D_OK;
+}
+
+template <class T>
+int transeq_t(o3d_ctx* c, int itime) {
+  double a, b, cc;
+  ab_coefs(c, itime, &a, &b, &cc);
+  ScalArgs<T> A;
+  A.phi = (const T*)c->phi;
+  A.phi_out = (T*)c->phi2;
+  for (int q = 0; q < 3; ++q) A.u[q] = (const T*)c->u[q];
+  A.src = (const T*)c->src;
+  A.nu_t = (const T*)c->nu_t;
+  A.fnew = (T*)c->fphi[2];
+  A.f2 = b != 0.0 ? (const T*)c->fphi[0] : nullptr;
+  A.f3 = cc != 0.0 ? (const T*)c->fphi[1] : nullptr;
+  A.g = c->g;
+  A.cf = cast_coef<T>(c->cf);
+  A.adu = (T)a;
+  A.bdu = (T)b;
+  A.cdu = (T)cc;
+  A.alpha0 = (T)(1.0 / (c->P.re * c->P.sc));
+  A.sc = (T)c->P.sc;
+  A.les = c->P.iles == 1;
+  A.part = c->part;
+  launch_transeq<T>(A, c->diag->sums + 16, c->s, &c->launches);
+  CKL();
+  std::swap(c->phi, c->phi2);
+  if (c->P.itscheme == 2) std::swap(c->fphi[0], c->fphi[2]);
+  else rotate_ring(c->fphi);
+  return O3D_OK;
+}
+
+// ---- pressure solve --------------------------------------------------------
+
+int build_mg(o3d_ctx* c) {
+  const int maxlev = c->P.mg_levels > 0 ? c->P.mg_levels : 32;
+  Grid g = c->gp;
+  double h[3] = {c->dx, c->dy, c->dz};
+  c->mg.clear();
+  for (;;) {
+    MGLevel L;
+    memset(&L, 0, sizeof L);
+    L.g = g;
+    for (int a = 0; a < 3; ++a) L.h[a] = h[a];
+    int any = 0;
+    Grid ng = g;
+    for (int a = 0; a < 3; ++a) {
+      const int n = g.len(a);
+      int cn = 0;
+      if (g.bc[a] == AX_PERIODIC && n % 2 == 0 && n / 2 >= 4) cn = n / 2;
+      if (g.bc[a] == AX_MIRROR && n % 2 == 1 && (n + 1) / 2 >= 3) cn = (n + 1) / 2;
+      L.coarsen[a] = cn > 0;
+      if (cn) {
+        any = 1;
+        if (a == 0) ng.nx = cn;
+        if (a == 1) ng.ny = cn;
+        if (a == 2) ng.nz = cn;
+      }
+    }
+    ng.n = (long long)ng.nx * ng.ny * ng.nz;
+    const bool last = !any || (int)c->mg.size() + 1 >= maxlev || g.n <= 512;
+    if (last) for (int a = 0; a < 3; ++a) L.coarsen[a] = 0;
+    c->mg.push_back(L);
+    if (last) break;
+    for (int a = 0; a < 3; ++a)
+      if (c->mg.back().coarsen[a]) h[a] *= 2.0;
+    g = ng;
+  }
+  const size_t tsz = c->mixed ? 4 : 8;
+  for (auto& L : c->mg) {
+    int st;
+    if ((st = dalloc(c->s, &L.e, (size_t)L.g.n * tsz))) return st;
+    if ((st = dalloc(c->s, &L.r, (size_t)L.g.n * tsz))) return st;
+    if ((st = dalloc(c->s, &L.t, (size_t)L.g.n * tsz))) return st;
+  }
+  c->mg_ok = 1;
+  return O3D_OK;
+}
+
+int reset_ctrl(o3d_ctx* c, double omega, double eps, int kmax, int idyn) {
+  SolveCtrl* h = c->ctrl_h;
+  memset(h, 0, sizeof *h);
+  h->omega = omega;
+  h->dmax_old = 1609.0;  // src/poisson.f90:52
+  h->eps = eps;
+  // factor of the dynamic omega rule: 1.01 for the x-periodic/y-free-slip
+  // solver, 1.05 otherwise (src/poisson.f90:35,162,288)
+  h->factor = (c->gp.bc[0] == AX_PERIODIC && c->gp.bc[1] == AX_MIRROR) ? 1.01 : 1.05;
+  h->kmax = kmax;
+  h->idyn = idyn;
+  CK(cudaMemcpyAsync(c->ctrl, h, sizeof *h, cudaMemcpyHostToDevice, c->s));
+  return O3D_OK;
+}
+
+int read_ctrl(o3d_ctx* c) {
+  CK(cudaMemcpyAsync(c->ctrl_h, c->ctrl, sizeof(SolveCtrl), cudaMemcpyDeviceToHost, c->s));
+  CK(cudaStreamSynchronize(c->s));
+  return O3D_OK;
+}
+
+int capture_sor(o3d_ctx* c) {
+  if (c->sor_exec) return O3D_OK;
+  c->sor_batch = 16;
+  PoiCoef<double> pc = make_poi<double>(c->dx, c->dy, c->dz);
+  cudaGraph_t graph;
+  CK(cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal));
+  for (int q = 0; q < c->sor_batch; ++q) {
+    launch_sor_sweep_ctrl(c->pp, (const double*)c->rhs, c->gp, pc, c->ctrl, c->s);
+    launch_sor_control(c->ctrl, c->s);
+  }
+  CK(cudaStreamEndCapture(c->s, &graph));
+  CK(cudaGraphInstantiate(&c->sor_exec, graph, 0));
+  CK(cudaGraphDestroy(graph));
+  c->sor_nodes = 3LL * c->sor_batch;
+  return O3D_OK;
+}
+
+int mg_smooth_cfg(const o3d_ctx* c, int* pre, int* post) {
+  *pre = c->P.mg_pre > 0 ? c->P.mg_pre : 2;
+  *post = c->P.mg_post > 0 ? c->P.mg_post : 2;
+  return 0;
+}
+
+int capture_mg(o3d_ctx* c) {
+  if (c->mg_exec) return O3D_OK;
+  if (!c->mg_ok) {
+    int st = build_mg(c);
+    if (st) return st;
+  }
+  c->mg_batch = 2;
+  int pre, post;
+  mg_smooth_cfg(c, &pre, &post);
+  const int coarse_sweeps = 40;
+  long long nl = 0;
+  cudaGraph_t graph;
+  CK(cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal));
+  for (int q = 0; q < c->mg_batch; ++q) {
+    if (c->mixed)
+      launch_mg_outer<float, float>(c->pp, (const float*)c->rhs, c->mg.data(), (int)c->mg.size(), pre,
+                                    post, coarse_sweeps, 1.0f, c->ctrl, c->part, c->s, &nl);
+    else
+      launch_mg_outer<double, double>(c->pp, (const double*)c->rhs, c->mg.data(), (int)c->mg.size(),
+                                      pre, post, coarse_sweeps, 1.0, c->ctrl, c->part, c->s, &nl);
+  }
+  CK(cudaStreamEndCapture(c->s, &graph));
+  CK(cudaGraphInstantiate(&c->mg_exec, graph, 0));
+  CK(cudaGraphDestroy(graph));
+  c->mg_nodes = nl;
+  return O3D_OK;
+}
+
+// Solves A pp = rhs with the context's solver; pp holds the initial guess.
+int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step_info* info) {
+  if (c->P.guess == O3D_GUESS_ZERO) CK(cudaMemsetAsync(c->pp, 0, (size_t)c->g.n * 8, c->s));
+  if (c->P.guess == O3D_GUESS_LEARNED) {
+    snprintf(g_err, sizeof g_err, "learned initial guess is not available in this build");
+    return O3D_ERR_NOT_BUILT;
+  }
+  int st = reset_ctrl(c, *omega_io, eps, kmax, idyn);
+  if (st) return st;
+  CK(cudaEventRecord(c->ev[2], c->s));
+  const bool use_mg = c->P.solver == O3D_SOLVER_MG;
+  if (use_mg) {
+    if ((st = capture_mg(c))) return st;
+    if (c->mixed) launch_rhs_wmean<float>((const float*)c->rhs, c->gp, c->part, c->ctrl, c->s, &c->launches);
+    else launch_rhs_wmean<double>((const double*)c->rhs, c->gp, c->part, c->ctrl, c->s, &c->launches);
+    CKL();
+  } else {
+    if ((st = capture_sor(c))) return st;
+  }
+  for (;;) {
+    if (use_mg) {
+      CK(cudaGraphLaunch(c->mg_exec, c->s));
+      c->launches += c->mg_nodes;
+    } else {
+      CK(cudaGraphLaunch(c->sor_exec, c->s));
+      c->launches += c->sor_nodes;
+    }
+    if ((st = read_ctrl(c))) return st;
+    if (c->ctrl_h->done) break;
+  }
+  PoiCoef<double> pc = make_poi<double>(c->dx, c->dy, c->dz);
+  if (c->mixed) launch_residual_inf<float>(c->pp, (const float*)c->rhs, c->gp, pc, use_mg, c->ctrl, c->s);
+  else launch_residual_inf<double>(c->pp, (const double*)c->rhs, c->gp, pc, use_mg, c->ctrl, c->s);
+  c->launches++;
+  CKL();
+  CK(cudaEventRecord(c->ev[3], c->s));
+  if ((st = read_ctrl(c))) return st;
+  const SolveCtrl* h = c->ctrl_h;
+  *omega_io = h->omega;
+  if (info) {
+    info->poisson_iters = h->iter;
+    info->poisson_cycles = h->cycles;
+    info->poisson_dmax = h->dmax;
+    info->poisson_res_inf = bits_to_double(h->res_key);
+    info->omega = h->omega;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
+    info->poisson_ms = ms;
+    info->poisson_status = h->status == 0 ? O3D_OK : h->status == 1 ? O3D_WARN_STAGNATION : O3D_WARN_POISSON_MAXIT;
+  }
+  return h->status == 0 ? O3D_OK : h->status == 1 ? O3D_WARN_STAGNATION : O3D_WARN_POISSON_MAXIT;
+}
+
+int check_params(const o3d_params* p) {
+  if (p->nx < 8 || p->ny < 8 || p->nz < 8) {
+    errf("grid too small: every axis needs at least 8 points (got %d x %d x %d)", p->nx, p->ny, p->nz);
+    return O3D_ERR_BADARG;
+  }
+  if ((long long)p->nx * p->ny * p->nz > (1LL << 31)) {
+    errf("grid of %lld points exceeds 2^31", (long long)p->nx * p->ny * p->nz);
+    return O3D_ERR_BADARG;
+  }
+  auto bc_ok = [](int a, int b) { return (a == 0 && b == 0) || (a == 1 && b == 1); };
+  if (!bc_ok(p->nbcx1, p->nbcxn)) { errf("unrecognized x boundary types nbcx1=%d nbcxn=%d", p->nbcx1, p->nbcxn); return O3D_ERR_BADARG; }
+  if (!bc_ok(p->nbcy1, p->nbcyn)) { errf("unrecognized y boundary types nbcy1=%d nbcyn=%d", p->nbcy1, p->nbcyn); return O3D_ERR_BADARG; }
+  if (!p->sim2d && !bc_ok(p->nbcz1, p->nbczn)) { errf("unrecognized z boundary types nbcz1=%d nbczn=%d", p->nbcz1, p->nbczn); return O3D_ERR_BADARG; }
+  if (p->nbcx1 == 1 && p->nbcy1 == 0) {
+    errf("no Poisson solver for free-slip x with periodic y");
+    return O3D_ERR_BADARG;
+  }
+  if (p->itscheme < 1 || p->itscheme > 3) { errf("itscheme %d unrecognized", p->itscheme); return O3D_ERR_BADARG; }
+  if (p->precision != O3D_PREC_FP64 && p->precision != O3D_PREC_MIXED) { errf("precision %d unknown", p->precision); return O3D_ERR_BADARG; }
+  if (p->solver != O3D_SOLVER_SOR && p->solver != O3D_SOLVER_MG) { errf("solver %d unknown", p->solver); return O3D_ERR_BADARG; }
+  if (!(p->dt > 0.0) || !(p->re > 0.0) || !(p->xlx > 0.0) || !(p->yly > 0.0) || !(p->zlz > 0.0)) {
+    errf("dt, re and the domain lengths must be positive");
+    return O3D_ERR_BADARG;
+  }
+  return O3D_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char* o3d_last_error(void) { return g_err; }
+
+void o3d_default_params(o3d_params* p) {
+  memset(p, 0, sizeof *p);
+  const double twopi = 2.0 * 3.14159265358979323846;
+  p->nx = p->ny = p->nz = 64;
+  p->xlx = p->yly = p->zlz = twopi * 63.0 / 64.0;  // dx = 2 pi / 64 on the node-inclusive grid
+  p->itscheme = 3;
+  p->dt = 0.2 * twopi / 64.0;
+  p->re = 1600.0;
+  p->omega = 2.0 / (1.0 + sin(3.14159265358979323846 * twopi / 64.0));
+  p->eps = 1e-8;
+  p->kmax = 2000;
+  p->sc = 1.0;
+  p->cs = 0.17;
+  p->precision = O3D_PREC_FP64;
+  p->solver = O3D_SOLVER_SOR;
+  p->guess = O3D_GUESS_PREVIOUS;
+  p->diagnostics = 1;
+}
+
+int o3d_create(const o3d_params* p, o3d_ctx** out) {
+  if (!p || !out) { errf("null argument"); return O3D_ERR_BADARG; }
+  *out = nullptr;
+  int st = check_params(p);
+  if (st) return st;
+  o3d_ctx* c = new (std::nothrow) o3d_ctx();
+  if (!c) return O3D_ERR_NOMEM;
+  c->P = *p;
+  c->mixed = p->precision == O3D_PREC_MIXED;
+  c->esz = c->mixed ? 4 : 8;
+  c->g.nx = p->nx; c->g.ny = p->ny; c->g.nz = p->nz;
+  c->g.n = (long long)p->nx * p->ny * p->nz;
+  c->g.bc[0] = p->nbcx1 == 0 ? AX_PERIODIC : AX_MIRROR;
+  c->g.bc[1] = p->nbcy1 == 0 ? AX_PERIODIC : AX_MIRROR;
+  c->g.bc[2] = p->sim2d ? AX_ZERO : (p->nbcz1 == 0 ? AX_PERIODIC : AX_MIRROR);
+  // Poisson variant chosen from the x and y types (src/initialization.f90:283-301):
+  // 0000 all periodic, 0011 y mirror, 111111 x, y and z mirror
+  c->gp = c->g;
+  if (p->nbcx1 == 0 && p->nbcy1 == 0) { c->gp.bc[0] = c->gp.bc[1] = c->gp.bc[2] = AX_PERIODIC; }
+  else if (p->nbcx1 == 0) { c->gp.bc[0] = AX_PERIODIC; c->gp.bc[1] = AX_MIRROR; c->gp.bc[2] = AX_PERIODIC; }
+  else { c->gp.bc[0] = c->gp.bc[1] = c->gp.bc[2] = AX_MIRROR; }
+  for (int a = 0; a < 3; ++a)
+    if (c->gp.bc[a] == AX_PERIODIC && c->gp.len(a) % 2) {
+      errf("periodic axis %c needs an even point count for red-black ordering (got %d)",
+           "xyz"[a], c->gp.len(a));
+      delete c;
+      return O3D_ERR_BADARG;
+    }
+  // src/initialization.f90:182-202
+  c->dx = p->xlx / (double)(p->nx - 1);
+  c->dy = p->yly / (double)(p->ny - 1);
+  c->dz = p->zlz / (double)(p->nz - 1);
+  c->delta = std::pow(c->dx * c->dy * c->dz, 1.0 / 3.0);
+  const double dt = p->dt;
+  c->adt[0] = dt; c->bdt[0] = 0.0; c->cdt[0] = 0.0;
+  c->adt[1] = 3.0 * dt / 2.0; c->bdt[1] = -1.0 * dt / 2.0; c->cdt[1] = 0.0;
+  c->adt[2] = 23.0 * dt / 12.0; c->bdt[2] = -16.0 * dt / 12.0; c->cdt[2] = 5.0 * dt / 12.0;
+  c->omega = p->omega;
+  make_coef(c->dx, c->cf.ax[0]);
+  make_coef(c->dy, c->cf.ax[1]);
+  make_coef(c->dz, c->cf.ax[2]);
+
+  if (cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) != cudaSuccess) {
+    snprintf(g_err, sizeof g_err, "cudaStreamCreate failed: %s", cudaGetErrorString(cudaGetLastError()));
+    delete c;
+    return O3D_ERR_CUDA;
+  }
+  for (int q = 0; q < 4; ++q) cudaEventCreate(&c->ev[q]);
+  const size_t fb = fbytes(c);
+  st = 0;
+  for (int q = 0; q < 3 && !st; ++q) {
+    st = st ? st : dalloc(c->s, &c->u[q], fb);
+    st = st ? st : dalloc(c->s, &c->up[q], fb);
+    for (int h = 0; h < 3 && !st; ++h) st = dalloc(c->s, &c->fu[q][h], fb);
+  }
+  st = st ? st : dalloc(c->s, &c->nu_t, fb);
+  st = st ? st : dalloc(c->s, &c->rhs, fb);
+  st = st ? st : dalloc(c->s, (void**)&c->pp, (size_t)c->g.n * 8);
+  if (!st && p->nscr) {
+    st = st ? st : dalloc(c->s, &c->phi, fb);
+    st = st ? st : dalloc(c->s, &c->phi2, fb);
+    st = st ? st : dalloc(c->s, &c->src, fb);
+    for (int h = 0; h < 3 && !st; ++h) st = dalloc(c->s, &c->fphi[h], fb);
+  }
+  const long long nb = pt_blocks(c->g) + 1;
+  st = st ? st : dalloc(c->s, (void**)&c->part, (size_t)nb * 16 * sizeof(double));
+  st = st ? st : dalloc(c->s, (void**)&c->spart, (size_t)nb * sizeof(StatPart));
+  st = st ? st : dalloc(c->s, (void**)&c->diag, sizeof(DevDiag));
+  st = st ? st : dalloc(c->s, (void**)&c->ctrl, sizeof(SolveCtrl));
+  if (!st && cudaMallocHost((void**)&c->diag_h, sizeof(DevDiag)) != cudaSuccess) st = O3D_ERR_NOMEM;
+  if (!st && cudaMallocHost((void**)&c->ctrl_h, sizeof(SolveCtrl)) != cudaSuccess) st = O3D_ERR_NOMEM;
+  if (!st && cudaStreamSynchronize(c->s) != cudaSuccess) st = O3D_ERR_CUDA;
+  if (st) {
+    o3d_destroy(c);
+    return st;
+  }
+  *out = c;
+  return O3D_OK;
+}
+
+int o3d_destroy(o3d_ctx* c) {
+  if (!c) return O3D_OK;
+  if (c->s) cudaStreamSynchronize(c->s);
+  for (int q = 0; q < 3; ++q) {
+    cudaFree(c->u[q]);
+    cudaFree(c->up[q]);
+    for (int h = 0; h < 3; ++h) cudaFree(c->fu[q][h]);
+    cudaFree(c->fphi[q]);
+  }
+  cudaFree(c->nu_t); cudaFree(c->rhs); cudaFree(c->pp);
+  cudaFree(c->phi); cudaFree(c->phi2); cudaFree(c->src);
+  for (int q = 0; q < 4; ++q) cudaFree(c->stage[q]);
+  cudaFree(c->part); cudaFree(c->spart); cudaFree(c->diag); cudaFree(c->ctrl);
+  if (c->diag_h) cudaFreeHost(c->diag_h);
+  if (c->ctrl_h) cudaFreeHost(c->ctrl_h);
+  for (auto& L : c->mg) { cudaFree(L.e); cudaFree(L.r); cudaFree(L.t); }
+  if (c->sor_exec) cudaGraphExecDestroy(c->sor_exec);
+  if (c->mg_exec) cudaGraphExecDestroy(c->mg_exec);
+  for (int q = 0; q < 4; ++q) if (c->ev[q]) cudaEventDestroy(c->ev[q]);
+  if (c->s) cudaStreamDestroy(c->s);
+  delete c;
+  return O3D_OK;
+}
+
+long long o3d_launch_count(const o3d_ctx* c) { return c ? c->launches : 0; }
+void* o3d_stream(o3d_ctx* c) { return c ? (void*)c->s : nullptr; }
+
+int o3d_upload(o3d_ctx* c, int field, const double* host) {
+  if (!c || !host) return O3D_ERR_BADARG;
+  bool is_pp;
+  void* d = field_ptr(c, field, &is_pp);
+  if (!d) { errf("field %d not allocated or unknown", field); return O3D_ERR_BADARG; }
+  if (is_pp) {
+    CK(cudaMemcpyAsync(d, host, (size_t)c->g.n * 8, cudaMemcpyHostToDevice, c->s));
+  } else {
+    int st = put_field(c, d, host);
+    if (st) return st;
+  }
+  CK(cudaStreamSynchronize(c->s));
+  return O3D_OK;
+}
+
+int o3d_download(o3d_ctx* c, int field, double* host) {
+  if (!c || !host) return O3D_ERR_BADARG;
+  bool is_pp;
+  void* d = field_ptr(c, field, &is_pp);
+  if (!d) { errf("field %d not allocated or unknown", field); return O3D_ERR_BADARG; }
+  if (is_pp) {
+    CK(cudaMemcpyAsync(host, d, (size_t)c->g.n * 8, cudaMemcpyDeviceToHost, c->s));
+  } else {
+    int st = get_field(c, d, host);
+    if (st) return st;
+  }
+  CK(cudaStreamSynchronize(c->s));
+  return O3D_OK;
+}
+
+int o3d_der_dev(o3d_ctx* c, int axis, int order, int odd, const double* d_f, double* d_df) {
+  if (!c || axis < 0 || axis > 2 || (order != 1 && order != 2)) { errf("bad derivative request"); return O3D_ERR_BADARG; }
+  launch_der<double>(d_f, d_df, c->g, c->cf.ax[axis], axis, order, odd, c->s);
+  c->launches++;
+  CKL();
+  return O3D_OK;
+}
+
+int o3d_der(o3d_ctx* c, int axis, int order, int odd, const double* f, double* df) {
+  if (!c || !f || !df) return O3D_ERR_BADARG;
+  int st = stage_ready(c, 1);
+  if (st) return st;
+  const size_t b = (size_t)c->g.n * 8;
+  CK(cudaMemcpyAsync(c->stage[0], f, b, cudaMemcpyHostToDevice, c->s));
+  if ((st = o3d_der_dev(c, axis, order, odd, c->stage[0], c->stage[1]))) return st;
+  CK(cudaMemcpyAsync(df, c->stage[1], b, cudaMemcpyDeviceToHost, c->s));
+  CK(cudaStreamSynchronize(c->s));
+  return O3D_OK;
+}
+
+int o3d_divergence(o3d_ctx* c, const double* fx, const double* fy, const double* fz, int odd,
+                   double* divf) {
+  if (!c || !fx || !fy || !fz || !divf) return O3D_ERR_BADARG;
+  int st = stage_ready(c, 3);
+  if (st) return st;
+  const size_t b = (size_t)c->g.n * 8;
+  CK(cudaMemcpyAsync(c->stage[0], fx, b, cudaMemcpyHostToDevice, c->s));
+  CK(cudaMemcpyAsync(c->stage[1], fy, b, cudaMemcpyHostToDevice, c->s));
+  CK(cudaMemcpyAsync(c->stage[2], fz, b, cudaMemcpyHostToDevice, c->s));
+  launch_div<double, double>(c->stage[0], c->stage[1], c->stage[2], c->stage[3], c->g, c->cf, odd, 1.0,
+                             0, c->spart, c->s);
+  c->launches++;
+  CKL();
+  CK(cudaMemcpyAsync(divf, c->stage[3], b, cudaMemcpyDeviceToHost, c->s));
+  CK(cudaStreamSynchronize(c->s));
+  return O3D_OK;
+}
+
+int o3d_calculate_nu_t(o3d_ctx* c) {
+  if (!c) return O3D_ERR_BADARG;
+  const double csd = c->P.cs * c->delta;
+  if (c->mixed)
+    launch_nu_t<float>((const float*)c->u[0], (const float*)c->u[1], (const float*)c->u[2], (float*)c->nu_t,
+                       c->g, cast_coef<float>(c->cf), (float)(csd * csd), c->s);
+  else
+    launch_nu_t<double>((const double*)c->u[0], (const double*)c->u[1], (const double*)c->u[2],
+                        (double*)c->nu_t, c->g, c->cf, csd * csd, c->s);
+  c->launches++;
+  CKL();
+  CK(cudaStreamSynchronize(c->s));
+  return O3D_OK;
+}
+
+int o3d_predict_velocity(o3d_ctx* c, int itime) {
+  if (!c) return O3D_ERR_BADARG;
+  int st = c->mixed ? predict_t<float>(c, itime) : predict_t<double>(c, itime);
+  if (st) return st;
+  CK(cudaStreamSynchronize(c->s));
+  return O3D_OK;
+}
+
+int o3d_correct_pression(o3d_ctx* c, double* omega, o3d_step_info* info) {
+  if (!c || !omega) return O3D_ERR_BADARG;
+  int st = c->mixed ? rhs_t<float>(c) : rhs_t<double>(c);
+  if (st) return st;
+  return solve(c, omega, c->P.eps, c->P.kmax, c->P.idyn, info);
+}
+
+int o3d_correct_velocity(o3d_ctx* c) {
+  if (!c) return O3D_ERR_BADARG;
+  int st = c->mixed ? correct_t<float>(c) : correct_t<double>(c);
+  if (st) return st;
+  CK(cudaMemcpyAsync(c->diag_h, c->diag, sizeof(DevDiag), cudaMemcpyDeviceToHost, c->s));
+  CK(cudaStreamSynchronize(c->s));
+  const double* r = c->diag_h->sums;
+  if (r[9] != 0.0 || r[3] > 1000.0 || r[4] > 1000.0 || r[5] > 1000.0) {
+    errf("velocity diverged (NaN or max > 1000)");
+    return O3D_ERR_NONFINITE;
+  }
+  return O3D_OK;
+}
+
+int o3d_transeq(o3d_ctx* c, int itime) {
+  if (!c) return O3D_ERR_BADARG;
+  if (!c->phi) { errf("scalar transport needs nscr = 1 at creation"); return O3D_ERR_BADARG; }
+  int st = c->mixed ? transeq_t<float>(c, itime) : transeq_t<double>(c, itime);
+  if (st) return st;
+  CK(cudaStreamSynchronize(c->s));
+  return O3D_OK;
+}
+
+int o3d_poisson_solve(o3d_ctx* c, double* pp, const double* rhs, double* omega, double eps, int kmax,
+                      int idyn, int* iters, double* dmax) {
+  if (!c || !pp || !rhs || !omega) return O3D_ERR_BADARG;
+  CK(cudaMemcpyAsync(c->pp, pp, (size_t)c->g.n * 8, cudaMemcpyHostToDevice, c->s));
+  int st = put_field(c, c->rhs, rhs);
+  if (st) return st;
+  o3d_step_info info;
+  memset(&info, 0, sizeof info);
+  const int guess = c->P.guess;
+  c->P.guess = O3D_GUESS_PREVIOUS;  // pp is the caller's initial guess
+  int rs = solve(c, omega, eps, kmax, idyn, &info);
+  c->P.guess = guess;
+  if (rs < 0) return rs;
+  CK(cudaMemcpyAsync(pp, c->pp, (size_t)c->g.n * 8, cudaMemcpyDeviceToHost, c->s));
+  CK(cudaStreamSynchronize(c->s));
+  if (iters) *iters = info.poisson_iters;
+  if (dmax) *dmax = info.poisson_dmax;
+  return rs;
+}
+
+int o3d_step(o3d_ctx* c, int itime, o3d_step_info* info) {
+  if (!c) return O3D_ERR_BADARG;
+  o3d_step_info loc;
+  if (!info) info = &loc;
+  memset(info, 0, sizeof *info);
+  CK(cudaEventRecord(c->ev[0], c->s));
+  int st = c->mixed ? predict_t<float>(c, itime) : predict_t<double>(c, itime);
+  if (st) return st;
+  st = c->mixed ? rhs_t<float>(c) : rhs_t<double>(c);
+  if (st) return st;
+  const int ps = solve(c, &c->omega, c->P.eps, c->P.kmax, c->P.idyn, info);
+  if (ps < 0) return ps;
+  st = c->mixed ? correct_t<float>(c) : correct_t<double>(c);
+  if (st) return st;
+  if (c->P.nscr) {
+    st = c->mixed ? transeq_t<float>(c, itime) : transeq_t<double>(c, itime);
+    if (st) return st;
+  }
+  if (c->P.diagnostics) {
+    st = c->mixed ? divu_diag_t<float>(c) : divu_diag_t<double>(c);
+    if (st) return st;
+  }
+  CK(cudaEventRecord(c->ev[1], c->s));
+  CK(cudaMemcpyAsync(c->diag_h, c->diag, sizeof(DevDiag), cudaMemcpyDeviceToHost, c->s));
+  CK(cudaStreamSynchronize(c->s));
+  const DevDiag* d = c->diag_h;
+  for (int q = 0; q < 6; ++q) {
+    info->divu_pred_stats[q] = d->divp[q];
+    info->divu_stats[q] = d->divu[q];
+  }
+  const double h[3] = {c->dx, c->dy, c->dz};
+  for (int a = 0; a < 3; ++a) {
+    info->umin[a] = d->sums[a];
+    info->umax[a] = d->sums[3 + a];
+    info->cfl[a] = d->sums[6 + a] * c->P.dt / h[a];
+  }
+  info->diverged = d->sums[9] != 0.0 || d->sums[3] > 1000.0 || d->sums[4] > 1000.0 || d->sums[5] > 1000.0;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+  info->step_ms = ms;
+  if (info->diverged) {
+    errf("velocity diverged at step %d (NaN or max > 1000)", itime);
+    return O3D_ERR_NONFINITE;
+  }
+  return ps;
+}
+
+int o3d_step_host(o3d_ctx* c, int itime, double* ux, double* uy, double* uz, double* pp,
+                  o3d_step_info* info) {
+  if (!c || !ux || !uy || !uz || !pp) return O3D_ERR_BADARG;
+  int st;
+  if ((st = put_field(c, c->u[0], ux))) return st;
+  if ((st = put_field(c, c->u[1], uy))) return st;
+  if ((st = put_field(c, c->u[2], uz))) return st;
+  CK(cudaMemcpyAsync(c->pp, pp, (size_t)c->g.n * 8, cudaMemcpyHostToDevice, c->s));
+  const int rs = o3d_step(c, itime, info);
+  if (rs < 0) return rs;
+  if ((st = get_field(c, c->u[0], ux))) return st;
+  if ((st = get_field(c, c->u[1], uy))) return st;
+  if ((st = get_field(c, c->u[2], uz))) return st;
+  CK(cudaMemcpyAsync(pp, c->pp, (size_t)c->g.n * 8, cudaMemcpyDeviceToHost, c->s));
+  CK(cudaStreamSynchronize(c->s));
+  return rs;
+}
+
+int o3d_statistics_calc(o3d_ctx* c, double t, double out[17]) {
+  if (!c || !out) return O3D_ERR_BADARG;
+  const double xnu = 1.0 / c->P.re;
+  if (c->mixed)
+    launch_stats<float>((const float*)c->u[0], (const float*)c->u[1], (const float*)c->u[2], c->g,
+                        cast_coef<float>(c->cf), xnu, c->part, c->s);
+  else
+    launch_stats<double>((const double*)c->u[0], (const double*)c->u[1], (const double*)c->u[2], c->g,
+                         c->cf, xnu, c->part, c->s);
+  launch_finalize(c->part, pt_blocks(c->g), 16, 0ull, c->diag->sums, c->s);
+  c->launches += 2;
+  CKL();
+  CK(cudaMemcpyAsync(c->diag_h, c->diag, sizeof(DevDiag), cudaMemcpyDeviceToHost, c->s));
+  CK(cudaStreamSynchronize(c->s));
+  const double* S = c->diag_h->sums;
+  const double N = (double)c->g.n;
+  out[0] = t;
+  out[1] = S[12] / N;
+  out[2] = S[13] / N;
+  out[3] = S[15] / N;
+  out[4] = S[14] / N;
+  for (int q = 0; q < 3; ++q) out[5 + q] = S[q] / N;
+  for (int q = 0; q < 9; ++q) out[8 + q] = S[3 + q] / N;
+  return O3D_OK;
+}
+
+int o3d_rbsor_sweeps_dev(o3d_ctx* c, double* d_pp, const double* d_rhs, double omega, int nsweeps,
+                         double* dmax_last) {
+  if (!c || !d_pp || !d_rhs || nsweeps < 1) return O3D_ERR_BADARG;
+  PoiCoef<double> pc = make_poi<double>(c->dx, c->dy, c->dz);
+  int st = reset_ctrl(c, omega, 0.0, 1 << 30, 0);
+  if (st) return st;
+  for (int q = 0; q < nsweeps; ++q) {
+    if (q == nsweeps - 1) CK(cudaMemsetAsync(&c->ctrl->dmax_key, 0, 8, c->s));
+    launch_sor_fixed(d_pp, d_rhs, c->gp, pc, omega, c->ctrl, c->s);
+    c->launches += 2;
+  }
+  CKL();
+  if ((st = read_ctrl(c))) return st;
+  if (dmax_last) *dmax_last = bits_to_double(c->ctrl_h->dmax_key);
+  return O3D_OK;
+}
+
+int o3d_time_kernel(o3d_ctx* c, int kernel, int reps, double* ms_per_launch) {
+  if (!c || reps < 1 || !ms_per_launch || kernel < 0 || kernel > 4) {
+    errf("bad o3d_time_kernel request");
+    return O3D_ERR_BADARG;
+  }
+  if (kernel >= 3) {
+    if (!c->mg_ok) {
+      int st = build_mg(c);
+      if (st) return st;
+    }
+    // the multigrid kernels return at once on a finished solve: re-open it
+    CK(cudaMemsetAsync(&c->ctrl->done, 0, sizeof(int), c->s));
+  }
+  auto launch = [&]() -> int {
+    switch (kernel) {
+      case 0: {
+        // predictor on the live state, without rotating the flux ring
+        void* saved[3][3];
+        memcpy(saved, c->fu, sizeof saved);
+        int st = c->mixed ? predict_t<float>(c, 3) : predict_t<double>(c, 3);
+        memcpy(c->fu, saved, sizeof saved);
+        return st;
+      }
+      case 1: return c->mixed ? rhs_t<float>(c) : rhs_t<double>(c);
+      case 2: return c->mixed ? correct_t<float>(c) : correct_t<double>(c);
+      default:
+        if (c->mixed)
+          launch_level_kernel<float, float>(kernel - 3, c->pp, (const float*)c->rhs, c->mg[0], c->ctrl, c->s);
+        else
+          launch_level_kernel<double, double>(kernel - 3, c->pp, (const double*)c->rhs, c->mg[0], c->ctrl, c->s);
+        c->launches++;
+        CKL();
+        return O3D_OK;
+    }
+  };
+  int st = launch();  // warm
+  if (st) return st;
+  CK(cudaEventRecord(c->ev[2], c->s));
+  for (int q = 0; q < reps; ++q)
+    if ((st = launch())) return st;
+  CK(cudaEventRecord(c->ev[3], c->s));
+  CK(cudaEventSynchronize(c->ev[3]));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]));
+  *ms_per_launch = ms / reps;
+  if (kernel >= 3) CK(cudaMemsetAsync(&c->ctrl->done, 0xff, sizeof(int), c->s));
+  CK(cudaStreamSynchronize(c->s));
+  return O3D_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,303 @@
+// o3d_internal.cuh -- shared device/host machinery of libo3d.so.
+//
+// Grid model: node-inclusive axes of n points (x fastest, column-major like
+// the Fortran fields).  Each axis is periodic (wrap with period n points,
+// src/derivation.f90:34-56), free-slip (mirror about the end nodes; even
+// fields reflect, odd fields reflect with a sign flip, src/derivation.f90:
+// 87-159) or collapsed (2D mode, every z-derivative is zero,
+// src/derivation.f90:481-495).
+//
+// Every boundary row of the reference's explicit closures equals the
+// interior stencil applied to ghost values f(-m) = s f(m), f(n-1+m) =
+// s f(n-1-m) (s = +1 even, -1 odd) or f(-m) = f(n-m) (periodic), evaluated
+// in the same operation order; the kernels use that ghost form, so one
+// stencil covers the 18 derivative routines.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include "../../include/o3d.h"
+
+namespace o3d {
+
+enum AxisBC { AX_PERIODIC = 0, AX_MIRROR = 1, AX_ZERO = 2 };
+
+struct Grid {
+  int nx, ny, nz;
+  int bc[3];         // AxisBC per axis
+  long long n;       // nx*ny*nz
+  __host__ __device__ long long sy() const { return nx; }
+  __host__ __device__ long long sz() const { return (long long)nx * ny; }
+  __host__ __device__ int len(int a) const { return a == 0 ? nx : a == 1 ? ny : nz; }
+  __host__ __device__ long long stride(int a) const { return a == 0 ? 1 : a == 1 ? (long long)nx : (long long)nx * ny; }
+};
+
+// Stencil coefficients of one axis, computed on the host exactly as the
+// reference does (src/derivation.f90:26-30 and :518-522).
+template <class T>
+struct AxisCoef {
+  T a1, b1, c1;   // 1/(60h), 9/(60h), 45/(60h)
+  T a2, b2, c2;   // 1/(12h^2), 16/(12h^2), 30/(12h^2)
+};
+
+template <class T>
+struct Coef3 {
+  AxisCoef<T> ax[3];
+};
+
+inline void make_coef(double h, AxisCoef<double>& c) {
+  double sixtyd = 60.0 * h;
+  c.a1 = 1.0 / sixtyd; c.b1 = 9.0 / sixtyd; c.c1 = 45.0 / sixtyd;
+  double twelved2 = 12.0 * h * h;
+  c.a2 = 1.0 / twelved2; c.b2 = 16.0 / twelved2; c.c2 = 30.0 / twelved2;
+}
+template <class T>
+inline Coef3<T> cast_coef(const Coef3<double>& d) {
+  Coef3<T> r;
+  for (int a = 0; a < 3; ++a) {
+    r.ax[a].a1 = (T)d.ax[a].a1; r.ax[a].b1 = (T)d.ax[a].b1; r.ax[a].c1 = (T)d.ax[a].c1;
+    r.ax[a].a2 = (T)d.ax[a].a2; r.ax[a].b2 = (T)d.ax[a].b2; r.ax[a].c2 = (T)d.ax[a].c2;
+  }
+  return r;
+}
+
+// Ghost map of index m in [-3, n+2] onto [0, n-1]; *flip tells whether an odd
+// field changes sign there.  Indices farther out (only reached by threads of
+// a partial tile, whose results are discarded) are clamped.
+__device__ __forceinline__ int ghost(int m, int n, int bc, bool* flip) {
+  *flip = false;
+  if (m >= 0 && m < n) return m;
+  int r;
+  if (bc == AX_PERIODIC) {
+    r = m < 0 ? m + n : m - n;
+  } else {
+    *flip = true;
+    r = m < 0 ? -m : 2 * (n - 1) - m;
+  }
+  return r < 0 ? 0 : (r >= n ? n - 1 : r);
+}
+
+template <class T>
+__device__ __forceinline__ T ld(const T* __restrict__ p, long long i) { return __ldg(p + i); }
+
+// Loads f at offsets -R..R along axis `a` of point (i,j,k) into v[0..2R].
+// Interior points take the fast path; points within R of an end use ghost().
+template <int R, class T, class S>
+__device__ __forceinline__ void load_line(const S* __restrict__ f, const Grid& g, int a,
+                                          int i, int j, int k, bool odd, T* v) {
+  const int n = g.len(a);
+  const int pos = a == 0 ? i : a == 1 ? j : k;
+  const long long st = g.stride(a);
+  const long long c = (long long)i + g.sy() * j + g.sz() * k;
+  if (pos >= R && pos < n - R) {
+#pragma unroll
+    for (int o = -R; o <= R; ++o) v[o + R] = (T)ld(f, c + st * o);
+  } else {
+    const long long base = c - st * pos;
+#pragma unroll
+    for (int o = -R; o <= R; ++o) {
+      bool flip;
+      int m = ghost(pos + o, n, g.bc[a], &flip);
+      T x = (T)ld(f, base + st * m);
+      v[o + R] = (flip && odd) ? -x : x;
+    }
+  }
+}
+
+// 6th-order first derivative a(f3-f-3) - b(f2-f-2) + c(f1-f-1), in the order
+// of src/derivation.f90:44-46.
+template <class T>
+__device__ __forceinline__ T d1(const T* v, const AxisCoef<T>& c) {
+  return c.a1 * (v[6] - v[0]) - c.b1 * (v[5] - v[1]) + c.c1 * (v[4] - v[2]);
+}
+// 4th-order second derivative -a(f-2+f2) + b(f-1+f1) - c f0, in the order of
+// src/derivation.f90:530-532; v is the 7-point line (centre v[3]).
+template <class T>
+__device__ __forceinline__ T d2(const T* v, const AxisCoef<T>& c) {
+  return -c.a2 * (v[1] + v[5]) + c.b2 * (v[2] + v[4]) - c.c2 * v[3];
+}
+
+// ---- order-preserving keys for atomic min/max of doubles ----------------
+__device__ __forceinline__ unsigned long long dkey(double x) {
+  unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+__host__ __device__ inline double dkey_inv(unsigned long long k) {
+  unsigned long long u = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+  double d;
+  memcpy(&d, &u, 8);
+  return d;
+}
+constexpr unsigned long long KEY_MIN = 0ull;             // below every double
+constexpr unsigned long long KEY_MAX = ~0ull;            // above every double
+
+// ---- warp/block reductions ------------------------------------------------
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ double warp_min(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide max, result valid in thread 0.  blockDim.x*y*z <= 1024.
+__device__ inline double block_max(double v) {
+  __shared__ double sh[32];
+  const int t = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int nt = blockDim.x * blockDim.y * blockDim.z;
+  v = warp_max(v);
+  __syncthreads();
+  if ((t & 31) == 0) sh[t >> 5] = v;
+  __syncthreads();
+  if (t < 32) {
+    v = t < (nt + 31) / 32 ? sh[t] : -INFINITY;
+    v = warp_max(v);
+  }
+  return v;
+}
+__device__ inline double block_sum(double v) {
+  __shared__ double sh[32];
+  const int t = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int nt = blockDim.x * blockDim.y * blockDim.z;
+  v = warp_sum(v);
+  __syncthreads();
+  if ((t & 31) == 0) sh[t >> 5] = v;
+  __syncthreads();
+  if (t < 32) {
+    v = t < (nt + 31) / 32 ? sh[t] : 0.0;
+    v = warp_sum(v);
+  }
+  return v;
+}
+
+// Field statistics of function_stats (src/functions.f90:27-63): min, max,
+// sum and the first linear index of the max.  One record per block, reduced
+// in a fixed order by finalize_stats so the sums are deterministic.
+struct StatPart {
+  double mn, mx, sum;
+  long long imx;
+};
+
+__device__ inline void stat_merge(StatPart& a, const StatPart& b) {
+  a.mn = fmin(a.mn, b.mn);
+  if (b.mx > a.mx || (b.mx == a.mx && b.imx < a.imx)) { a.mx = b.mx; a.imx = b.imx; }
+  a.sum += b.sum;
+}
+
+__device__ inline StatPart stat_shfl(const StatPart& s, int o) {
+  StatPart r;
+  r.mn = __shfl_xor_sync(0xffffffffu, s.mn, o);
+  r.mx = __shfl_xor_sync(0xffffffffu, s.mx, o);
+  r.sum = __shfl_xor_sync(0xffffffffu, s.sum, o);
+  r.imx = __shfl_xor_sync(0xffffffffu, s.imx, o);
+  return r;
+}
+
+// Reduces s over the block and stores the block's record at part[blk].
+__device__ inline void block_stat(StatPart s, StatPart* part, long long blk) {
+  __shared__ StatPart sh[32];
+  const int t = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int nt = blockDim.x * blockDim.y * blockDim.z;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) stat_merge(s, stat_shfl(s, o));
+  __syncthreads();
+  if ((t & 31) == 0) sh[t >> 5] = s;
+  __syncthreads();
+  if (t < 32) {
+    if (t < (nt + 31) / 32) s = sh[t];
+    else { s.mn = INFINITY; s.mx = -INFINITY; s.sum = 0; s.imx = 0x7fffffffffffffffll; }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) stat_merge(s, stat_shfl(s, o));
+    if (t == 0) part[blk] = s;
+  }
+}
+
+__device__ __forceinline__ StatPart stat_of(double v, long long idx, bool valid) {
+  StatPart s;
+  if (valid && !(v != v)) { s.mn = v; s.mx = v; s.sum = v; s.imx = idx; }
+  else { s.mn = INFINITY; s.mx = -INFINITY; s.sum = valid ? v : 0.0; s.imx = 0x7fffffffffffffffll; }
+  return s;
+}
+
+// ---- M-slot block reductions with per-slot operator -----------------------
+// ops is a compile-time list of RED_SUM / RED_MIN / RED_MAX; one record of M
+// doubles per block goes to part[blk*M ..]; k_finalize reduces the records in
+// a fixed order (deterministic sums).
+enum RedOp { RED_SUM = 0, RED_MIN = 1, RED_MAX = 2 };
+
+__device__ __forceinline__ double red_apply(int op, double a, double b) {
+  return op == RED_SUM ? a + b : op == RED_MIN ? fmin(a, b) : fmax(a, b);
+}
+__device__ __forceinline__ double red_ident(int op) {
+  return op == RED_SUM ? 0.0 : op == RED_MIN ? INFINITY : -INFINITY;
+}
+
+template <int M>
+__device__ inline void block_reduce_store(double (&v)[M], const int (&ops)[M], double* part,
+                                          long long blk) {
+  __shared__ double sh[M][32];
+  const int t = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int nt = blockDim.x * blockDim.y * blockDim.z;
+  const int nw = (nt + 31) / 32;
+#pragma unroll
+  for (int q = 0; q < M; ++q) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[q] = red_apply(ops[q], v[q], __shfl_xor_sync(0xffffffffu, v[q], o));
+  }
+  __syncthreads();
+  if ((t & 31) == 0) {
+#pragma unroll
+    for (int q = 0; q < M; ++q) sh[q][t >> 5] = v[q];
+  }
+  __syncthreads();
+  if (t < 32) {
+#pragma unroll
+    for (int q = 0; q < M; ++q) {
+      double x = t < nw ? sh[q][t] : red_ident(ops[q]);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x = red_apply(ops[q], x, __shfl_xor_sync(0xffffffffu, x, o));
+      if (t == 0) part[blk * M + q] = x;
+    }
+  }
+}
+
+__device__ __forceinline__ long long block_linear_id() {
+  return (long long)blockIdx.x + (long long)gridDim.x * ((long long)blockIdx.y + (long long)gridDim.y * blockIdx.z);
+}
+
+// ---- per-step device diagnostics ------------------------------------------
+struct DevDiag {
+  unsigned long long umin[3], umax[3], uabs[3];  // ordered keys
+  int nan_flag;
+  int pad;
+  double divp[6], divu[6];                       // function_stats of div(u*), div(u)
+  double sums[32];                               // finalized sums (statistics, scalar clipping)
+};
+
+// Device-side state of a pressure solve.  Every Poisson kernel returns at
+// once when `done` is set, so batches of sweeps/cycles can be queued (and
+// captured in a CUDA graph) without a host round trip per iteration.
+struct SolveCtrl {
+  unsigned long long dmax_key;   // max |update| of the current sweep/cycle (raw bits, >= 0)
+  unsigned long long res_key;    // max |residual|
+  double omega;                  // SOR relaxation (dynamic update of src/poisson.f90:115-121)
+  double dmax_old;               // starts at 1609 (src/poisson.f90:52)
+  double dmax;                   // last completed sweep
+  double eps, factor;
+  double rhs_mean;               // weighted mean removed from the rhs (multigrid)
+  double res_inf;
+  int iter, kmax, idyn, done, status;
+  int cycles;
+};
+
+}  // namespace o3d

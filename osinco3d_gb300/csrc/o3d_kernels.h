@@ -1,0 +1,132 @@
+// o3d_kernels.h -- argument blocks and launchers shared by the kernel files
+// and the host orchestration in o3d_api.cu.
+#pragma once
+
+#include "o3d_internal.cuh"
+
+namespace o3d {
+
+template <class T>
+struct PredArgs {
+  const T* u[3];
+  T* up[3];
+  T* fnew[3];
+  const T* f2[3];  // previous flux (nullptr when its AB weight is zero)
+  const T* f3[3];  // flux two steps back (nullptr when its AB weight is zero)
+  T* nu_t;
+  Grid g;
+  Coef3<T> cf;
+  T adu, bdu, cdu, onere, csd2;
+  int les;
+};
+
+template <class T, class P>
+struct CorrArgs {
+  const P* p;
+  const T* up[3];
+  T* u[3];
+  Grid g;
+  Coef3<T> cf;
+  T dt;
+  double* part;  // 10 doubles per block: min[3], max[3], |max|[3], nan
+};
+
+template <class T>
+struct ScalArgs {
+  const T* phi;
+  T* phi_out;
+  const T* u[3];
+  const T* src;
+  const T* nu_t;
+  T* fnew;
+  const T* f2;
+  const T* f3;
+  Grid g;
+  Coef3<T> cf;
+  T adu, bdu, cdu, alpha0, sc;
+  int les;
+  double* part;  // 3 doubles per block
+};
+
+long long pt_blocks(const Grid& g);
+
+template <class T>
+void launch_der(const T* f, T* df, const Grid& g, const AxisCoef<T>& c, int axis, int order,
+                int odd, cudaStream_t s);
+template <class T>
+void launch_predict(const PredArgs<T>& a, cudaStream_t s);
+template <class T>
+void launch_nu_t(const T* ux, const T* uy, const T* uz, T* nu, const Grid& g, const Coef3<T>& cf,
+                 T csd2, cudaStream_t s);
+template <class T, class O>
+void launch_div(const T* fx, const T* fy, const T* fz, O* out, const Grid& g, const Coef3<T>& cf,
+                int odd, T dt, int divide, StatPart* part, cudaStream_t s);
+template <class T, class P>
+void launch_correct(const CorrArgs<T, P>& a, cudaStream_t s);
+template <class T>
+void launch_stats(const T* ux, const T* uy, const T* uz, const Grid& g, const Coef3<T>& cf,
+                  double xnu, double* part, cudaStream_t s);
+template <class T>
+void launch_transeq(const ScalArgs<T>& a, const double* sums, cudaStream_t s, long long* nl);
+void launch_finalize(const double* part, long long nblk, int M, unsigned long long opmask,
+                     double* out, cudaStream_t s);
+void launch_finalize_stats(const StatPart* part, long long nblk, const Grid& g, double* out6,
+                           cudaStream_t s);
+template <class S, class D>
+void launch_convert(const S* s_, D* d, long long n, cudaStream_t s);
+
+// ---- pressure solve (k_poisson.cu) ----------------------------------------
+
+// 7-point operator of src/poisson.f90:95-98 on one grid level.
+template <class T>
+struct PoiCoef {
+  T ox, oy, oz;   // 1/dx^2, 1/dy^2, 1/dz^2
+  T A;            // -(2/dx^2 + 2/dy^2 + 2/dz^2)
+  T invA;
+};
+template <class T>
+inline PoiCoef<T> make_poi(double dx, double dy, double dz) {
+  PoiCoef<T> c;
+  double ox = 1.0 / (dx * dx), oy = 1.0 / (dy * dy), oz = 1.0 / (dz * dz);
+  double A = -(2.0 * ox + 2.0 * oy + 2.0 * oz);
+  c.ox = (T)ox; c.oy = (T)oy; c.oz = (T)oz; c.A = (T)A; c.invA = (T)(1.0 / A);
+  return c;
+}
+
+// Largest coarsest level solved in one block's shared memory (16 KB per array).
+template <class T>
+constexpr int coarse_max() { return (int)(16384 / sizeof(T)); }
+
+// One level of the multigrid hierarchy.
+struct MGLevel {
+  Grid g;
+  double h[3];
+  int coarsen[3];   // axis coarsened towards the next level
+  void* e;          // correction (T)
+  void* r;          // right-hand side (T)
+  void* t;          // residual scratch (T)
+};
+
+void launch_sor_sweep_ctrl(double* p, const double* rhs, const Grid& g, const PoiCoef<double>& c,
+                           SolveCtrl* ctrl, cudaStream_t s);
+void launch_sor_control(SolveCtrl* ctrl, cudaStream_t s);
+void launch_sor_fixed(double* p, const double* rhs, const Grid& g, const PoiCoef<double>& c,
+                      double omega, SolveCtrl* ctrl, cudaStream_t s);
+
+// Multigrid: T is the arithmetic of the cycles, R the type of the top rhs.
+template <class T, class R>
+void launch_mg_outer(double* p, const R* rhs, MGLevel* lv, int nlev, int pre, int post,
+                     int coarse_sweeps, T smooth_omega, SolveCtrl* ctrl, double* wpart,
+                     cudaStream_t s, long long* nl);
+// one finest-level kernel for timing: 0 smoother colour pass, 1 FP64 residual
+template <class T, class R>
+void launch_level_kernel(int which, double* p, const R* rhs, const MGLevel& L, SolveCtrl* ctrl,
+                         cudaStream_t s);
+template <class R>
+void launch_rhs_wmean(const R* rhs, const Grid& g, double* part, SolveCtrl* ctrl, cudaStream_t s,
+                      long long* nl);
+template <class R>
+void launch_residual_inf(const double* p, const R* rhs, const Grid& g, const PoiCoef<double>& c,
+                         int use_mean, SolveCtrl* ctrl, cudaStream_t s);
+
+}  // namespace o3d

@@ -1,0 +1,312 @@
+"""ctypes binding of libo3d.so (include/o3d.h).
+
+The class :class:`Context` mirrors the Fortran interface of the osinco3d hot
+path: ``predict_velocity`` (src/integration.f90:14), ``correct_pression``
+(:199), ``correct_velocity`` (:257), ``transeq`` (:332), the ``der_type``
+derivative operators (src/initialization.f90:86-91), ``poi_type`` Poisson
+solvers (:93-102) and ``statistics_calc`` (src/utils.f90:243).  Fields are
+numpy float64 arrays in Fortran order with shape (nx, ny, nz).
+
+There is no CPU fallback: every call runs the CUDA kernels of libo3d.so, and
+loading fails with an error if the library has not been built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+import re
+
+import numpy as np
+
+from . import build as _build
+
+OK = 0
+WARN_POISSON_MAXIT = 1
+WARN_STAGNATION = 2
+ERR_BADARG = -1
+ERR_CUDA = -2
+ERR_NONFINITE = -3
+ERR_NOMEM = -4
+ERR_NOT_BUILT = -5
+
+PREC_FP64, PREC_MIXED = 0, 1
+SOLVER_SOR, SOLVER_MG = 0, 1
+GUESS_PREVIOUS, GUESS_ZERO, GUESS_LEARNED = 0, 1, 2
+
+FIELD = {"ux": 0, "uy": 1, "uz": 2, "pp": 3, "ux_pred": 4, "uy_pred": 5, "uz_pred": 6,
+         "phi": 7, "src": 8, "nu_t": 9, "rhs": 10}
+FIELD_FU0, FIELD_FPHI0 = 16, 24
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "o3d.h")
+
+
+class O3DError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"libo3d error {code}: {msg}")
+        self.code = code
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+        ("xlx", C.c_double), ("yly", C.c_double), ("zlz", C.c_double),
+        ("x0", C.c_double), ("y0", C.c_double), ("z0", C.c_double),
+        ("nbcx1", C.c_int), ("nbcxn", C.c_int), ("nbcy1", C.c_int), ("nbcyn", C.c_int),
+        ("nbcz1", C.c_int), ("nbczn", C.c_int), ("sim2d", C.c_int),
+        ("itscheme", C.c_int), ("dt", C.c_double),
+        ("re", C.c_double),
+        ("omega", C.c_double), ("eps", C.c_double), ("kmax", C.c_int), ("idyn", C.c_int),
+        ("nscr", C.c_int), ("sc", C.c_double),
+        ("iles", C.c_int), ("cs", C.c_double),
+        ("precision", C.c_int), ("solver", C.c_int), ("mg_levels", C.c_int),
+        ("mg_pre", C.c_int), ("mg_post", C.c_int), ("guess", C.c_int), ("diagnostics", C.c_int),
+    ]
+
+
+class StepInfo(C.Structure):
+    _fields_ = [
+        ("poisson_status", C.c_int), ("poisson_iters", C.c_int), ("poisson_cycles", C.c_int),
+        ("poisson_dmax", C.c_double), ("poisson_res_inf", C.c_double), ("omega", C.c_double),
+        ("diverged", C.c_int),
+        ("divu_pred_stats", C.c_double * 6), ("divu_stats", C.c_double * 6),
+        ("cfl", C.c_double * 3), ("umin", C.c_double * 3), ("umax", C.c_double * 3),
+        ("poisson_ms", C.c_double), ("step_ms", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        out = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            out[name] = list(v) if hasattr(v, "__len__") else v
+        return out
+
+
+_dp = C.POINTER(C.c_double)
+_LIB = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def lib(build_if_missing: bool = True):
+    """Loads libo3d.so, building it first if it is missing or stale."""
+    global _LIB
+    if _LIB is None:
+        if build_if_missing:
+            _build.build()
+        path = library_path()
+        if not os.path.exists(path):
+            raise RuntimeError(f"libo3d.so is not built ({path}); run osinco3d_gb300.build.build()")
+        L = C.CDLL(path)
+        vp = C.c_void_p
+        sig = {
+            "o3d_default_params": (None, [C.POINTER(Params)]),
+            "o3d_create": (C.c_int, [C.POINTER(Params), C.POINTER(vp)]),
+            "o3d_destroy": (C.c_int, [vp]),
+            "o3d_last_error": (C.c_char_p, []),
+            "o3d_launch_count": (C.c_longlong, [vp]),
+            "o3d_stream": (vp, [vp]),
+            "o3d_upload": (C.c_int, [vp, C.c_int, _dp]),
+            "o3d_download": (C.c_int, [vp, C.c_int, _dp]),
+            "o3d_der": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, _dp, _dp]),
+            "o3d_der_dev": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, vp, vp]),
+            "o3d_divergence": (C.c_int, [vp, _dp, _dp, _dp, C.c_int, _dp]),
+            "o3d_calculate_nu_t": (C.c_int, [vp]),
+            "o3d_predict_velocity": (C.c_int, [vp, C.c_int]),
+            "o3d_correct_pression": (C.c_int, [vp, _dp, C.POINTER(StepInfo)]),
+            "o3d_correct_velocity": (C.c_int, [vp]),
+            "o3d_transeq": (C.c_int, [vp, C.c_int]),
+            "o3d_poisson_solve": (C.c_int, [vp, _dp, _dp, _dp, C.c_double, C.c_int, C.c_int,
+                                            C.POINTER(C.c_int), _dp]),
+            "o3d_step": (C.c_int, [vp, C.c_int, C.POINTER(StepInfo)]),
+            "o3d_step_host": (C.c_int, [vp, C.c_int, _dp, _dp, _dp, _dp, C.POINTER(StepInfo)]),
+            "o3d_statistics_calc": (C.c_int, [vp, C.c_double, _dp]),
+            "o3d_rbsor_sweeps_dev": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, _dp]),
+            "o3d_time_kernel": (C.c_int, [vp, C.c_int, C.c_int, _dp]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def declared_symbols() -> list[str]:
+    """Every o3d_* function declared in include/o3d.h."""
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"O3D_API\s+[\w\s\*]+?\b(o3d_\w+)\s*\(", txt)))
+
+
+def default_params(**kw) -> Params:
+    p = Params()
+    lib().o3d_default_params(C.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise AttributeError(k)
+        setattr(p, k, v)
+    return p
+
+
+def tgv_params(n: int, **kw) -> Params:
+    """Periodic Taylor-Green box [0, 2 pi)^3 on n^3 nodes: xlx = 2 pi (n-1)/n so
+    that the node-inclusive spacing xlx/(n-1) equals the period 2 pi / n."""
+    L = 2.0 * math.pi * (n - 1) / n
+    base = dict(nx=n, ny=n, nz=n, xlx=L, yly=L, zlz=L, dt=0.2 * 2.0 * math.pi / n,
+                omega=2.0 / (1.0 + math.sin(math.pi * 2.0 * math.pi / n)))
+    base.update(kw)
+    return default_params(**base)
+
+
+def _ptr(a: np.ndarray):
+    if a.dtype != np.float64 or not a.flags.f_contiguous:
+        raise TypeError("fields must be float64 Fortran-ordered arrays")
+    return a.ctypes.data_as(_dp)
+
+
+class Context:
+    """One solver context (grid, device fields, stream)."""
+
+    def __init__(self, params: Params):
+        self.L = lib()
+        self.params = params
+        self.shape = (params.nx, params.ny, params.nz)
+        h = C.c_void_p()
+        self._check(self.L.o3d_create(C.byref(params), C.byref(h)))
+        self.h = h
+        self.omega = params.omega
+
+    def _check(self, code: int) -> int:
+        if code < 0:
+            raise O3DError(code, self.L.o3d_last_error().decode())
+        return code
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.L.o3d_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- fields -------------------------------------------------------------
+    def field(self) -> np.ndarray:
+        return np.zeros(self.shape, dtype=np.float64, order="F")
+
+    def upload(self, name, arr: np.ndarray) -> None:
+        fid = FIELD[name] if isinstance(name, str) else name
+        self._check(self.L.o3d_upload(self.h, fid, _ptr(np.asfortranarray(arr, dtype=np.float64))))
+
+    def download(self, name) -> np.ndarray:
+        fid = FIELD[name] if isinstance(name, str) else name
+        out = self.field()
+        self._check(self.L.o3d_download(self.h, fid, _ptr(out)))
+        return out
+
+    def flux(self, comp: int, age: int) -> np.ndarray:
+        return self.download(FIELD_FU0 + 2 * comp + age)
+
+    @property
+    def launches(self) -> int:
+        return int(self.L.o3d_launch_count(self.h))
+
+    # -- operators ----------------------------------------------------------
+    def der(self, f: np.ndarray, axis: int, order: int, odd: bool) -> np.ndarray:
+        f = np.asfortranarray(f, dtype=np.float64)
+        out = self.field()
+        self._check(self.L.o3d_der(self.h, axis, order, int(odd), _ptr(f), _ptr(out)))
+        return out
+
+    def divergence(self, fx, fy, fz, odd: int = 1) -> np.ndarray:
+        out = self.field()
+        fx, fy, fz = (np.asfortranarray(a, dtype=np.float64) for a in (fx, fy, fz))
+        self._check(self.L.o3d_divergence(self.h, _ptr(fx), _ptr(fy), _ptr(fz), odd, _ptr(out)))
+        return out
+
+    def calculate_nu_t(self) -> np.ndarray:
+        self._check(self.L.o3d_calculate_nu_t(self.h))
+        return self.download("nu_t")
+
+    def predict_velocity(self, itime: int) -> None:
+        self._check(self.L.o3d_predict_velocity(self.h, itime))
+
+    def correct_pression(self) -> StepInfo:
+        info = StepInfo()
+        om = C.c_double(self.omega)
+        self._check(self.L.o3d_correct_pression(self.h, C.byref(om), C.byref(info)))
+        self.omega = om.value
+        return info
+
+    def correct_velocity(self) -> int:
+        return self._check(self.L.o3d_correct_velocity(self.h))
+
+    def transeq(self, itime: int) -> None:
+        self._check(self.L.o3d_transeq(self.h, itime))
+
+    def poisson_solve(self, pp: np.ndarray, rhs: np.ndarray, omega: float, eps: float, kmax: int,
+                      idyn: int = 0):
+        """poi_type(pp, rhs, ..., omega, eps, kmax, idyn): pp is updated in place."""
+        om = C.c_double(omega)
+        it = C.c_int(0)
+        dm = C.c_double(0.0)
+        rhs = np.asfortranarray(rhs, dtype=np.float64)
+        st = self._check(self.L.o3d_poisson_solve(self.h, _ptr(pp), _ptr(rhs), C.byref(om), eps, kmax,
+                                                  idyn, C.byref(it), C.byref(dm)))
+        return st, it.value, dm.value, om.value
+
+    def step(self, itime: int) -> StepInfo:
+        info = StepInfo()
+        self.last_status = self._check(self.L.o3d_step(self.h, itime, C.byref(info)))
+        return info
+
+    def step_host(self, itime: int, ux, uy, uz, pp) -> StepInfo:
+        info = StepInfo()
+        self.last_status = self._check(
+            self.L.o3d_step_host(self.h, itime, _ptr(ux), _ptr(uy), _ptr(uz), _ptr(pp), C.byref(info)))
+        return info
+
+    def statistics_calc(self, t: float) -> np.ndarray:
+        out = (C.c_double * 17)()
+        self._check(self.L.o3d_statistics_calc(self.h, t, out))
+        return np.array(out[:])
+
+    KERNELS = {"predict": 0, "rhs": 1, "correct": 2, "mg_smooth": 3, "resid64": 4}
+
+    def time_kernel(self, name: str, reps: int = 20) -> float:
+        """Milliseconds per launch of one hot kernel on the live state."""
+        ms = C.c_double(0.0)
+        self._check(self.L.o3d_time_kernel(self.h, self.KERNELS[name], reps, C.byref(ms)))
+        return ms.value
+
+    def rbsor_sweeps_dev(self, d_pp: int, d_rhs: int, omega: float, nsweeps: int) -> float:
+        dm = C.c_double(0.0)
+        self._check(self.L.o3d_rbsor_sweeps_dev(self.h, C.c_void_p(d_pp), C.c_void_p(d_rhs), omega,
+                                                nsweeps, C.byref(dm)))
+        return dm.value
+
+
+def tgv_fields(params: Params):
+    """Taylor-Green initial state of initialize_taylor_green_vortex
+    (src/initial_conditions.f90:139-151) on the context grid, u0 = l0 = ratio = 1."""
+    nx, ny, nz = params.nx, params.ny, params.nz
+    dx, dy, dz = params.xlx / (nx - 1), params.yly / (ny - 1), params.zlz / (nz - 1)
+    x = params.x0 + np.arange(nx) * dx
+    y = params.y0 + np.arange(ny) * dy
+    z = params.z0 + np.arange(nz) * dz
+    X, Y, Z = np.meshgrid(x, y, z, indexing="ij")
+    ux = np.asfortranarray(np.sin(X) * np.cos(Y) * np.cos(Z))
+    uy = np.asfortranarray(-np.cos(X) * np.sin(Y) * np.cos(Z))
+    uz = np.zeros_like(ux, order="F")
+    pp = np.asfortranarray(0.0625 * (np.cos(2 * X) + np.cos(2 * Y)) * (np.cos(2 * Z) + 2.0))
+    return ux, uy, uz, pp

@@ -1,0 +1,142 @@
+"""GPU pressure solvers against the oracle's lexicographic SOR
+(src/poisson.f90), through o3d_poisson_solve (the poi_type interface).
+
+Red-black SOR and multigrid converge to the fixed point of the same 7-point
+operator; they are compared with the oracle solved to eps * 1e-3, after
+removing the free constant of the singular problem.  Tolerance: the
+pressure error of an update-norm stop at eps is about eps * rho / (1 - rho)
+with rho the sweep's contraction factor (near 0.98 on the 33^3 mirror grid
+at omega = 1.8, measured on the oracle's red-black sweep: error 57 eps); the
+tests allow 200 eps (SOR) and 5 eps (multigrid, whose stop test is on the
+whole correction)."""
+import numpy as np
+import pytest
+
+from _util import PI, params_of, rel_err
+
+pytestmark = pytest.mark.gpu
+
+VARIANTS = [
+    # (nx, ny, nz), (bcx, bcy, bcz): 0000, 0011, 111111 solvers
+    ((32, 32, 32), (0, 0, 0)),
+    ((32, 33, 16), (0, 1, 0)),
+    ((33, 33, 33), (1, 1, 1)),
+]
+
+
+def _case(oracle, shape, bcs, **kw):
+    nx, ny, nz = shape
+    L = [2 * PI * (n - 1) / n if b == 0 else PI for n, b in zip(shape, bcs)]
+    return oracle.Case(nx, ny, nz, L[0], L[1], L[2], bcx=bcs[0], bcy=bcs[1], bcz=bcs[2], **kw)
+
+
+def _compatible_rhs(c, seed):
+    """Smooth seeded rhs with zero trapezoid-weighted mean on the Poisson grid."""
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = c.shape
+    x = np.linspace(0, 1, nx)[:, None, None]
+    y = np.linspace(0, 1, ny)[None, :, None]
+    z = np.linspace(0, 1, nz)[None, None, :]
+    r = np.zeros(c.shape)
+    for _ in range(4):
+        a, b, d = rng.integers(1, 4, 3)
+        r += rng.standard_normal() * np.cos(2 * PI * a * x) * np.cos(2 * PI * b * y) * np.cos(2 * PI * d * z)
+    r += 0.05 * rng.standard_normal(c.shape)
+    mirror = [c.bcx, c.bcy, 1 if c.bcx == 1 else 0]  # the 0011 solver keeps z periodic
+    W = np.ones(c.shape)
+    for ax, m in enumerate(mirror):
+        if m:
+            w = np.ones(c.shape[ax])
+            w[0] = w[-1] = 0.5
+            sh = [1, 1, 1]
+            sh[ax] = -1
+            W = W * w.reshape(sh)
+    r -= (W * r).sum() / W.sum()
+    return np.asfortranarray(r)
+
+
+def _demean(p):
+    return p - p.mean()
+
+
+@pytest.mark.parametrize("shape,bcs", VARIANTS)
+def test_one_red_black_sweep(oracle, o3d, shape, bcs):
+    """kmax = 1: exactly one red-black sweep, same values and same max
+    |p_gs - p| as the oracle's red-black sweep."""
+    c = _case(oracle, shape, bcs)
+    rng = np.random.default_rng(1)
+    p0 = np.asfortranarray(rng.standard_normal(c.shape))
+    rhs = np.asfortranarray(rng.standard_normal(c.shape))
+    for sweeps in (1, 3):
+        ref = p0.copy(order="F")
+        for _ in range(sweeps):
+            dref = oracle.rbsor_sweep(c, ref, rhs, 1.37)
+        with o3d.Context(params_of(o3d, c, solver=o3d.SOLVER_SOR)) as ctx:
+            got = p0.copy(order="F")
+            st, it, dm, om = ctx.poisson_solve(got, rhs, 1.37, 0.0, sweeps, 0)
+        assert st == o3d.WARN_POISSON_MAXIT and it == sweeps
+        assert rel_err(got, ref) < 1e-13
+        assert dm == pytest.approx(dref, rel=1e-11)
+
+
+@pytest.mark.parametrize("shape,bcs", VARIANTS)
+@pytest.mark.parametrize("solver", ["sor", "mg"])
+def test_fixed_point_matches_lexicographic_sor(oracle, o3d, shape, bcs, solver):
+    eps = 1e-9
+    c = _case(oracle, shape, bcs)
+    rhs = _compatible_rhs(c, 5)
+    ref = oracle.field3(c.shape)
+    st, _, _, _ = oracle.poisson_sor(c, ref, rhs, 1.8, eps * 1e-3, 200000)
+    assert st == oracle.SOR_CONVERGED
+    kind = o3d.SOLVER_SOR if solver == "sor" else o3d.SOLVER_MG
+    with o3d.Context(params_of(o3d, c, solver=kind)) as ctx:
+        got = ctx.field()
+        st, it, dm, om = ctx.poisson_solve(got, rhs, 1.8, eps, 100000 if solver == "sor" else 100, 0)
+    assert st == o3d.OK, (st, it, dm)
+    assert dm < eps
+    err = np.abs(_demean(got) - _demean(ref)).max()
+    assert err < (200 * eps if solver == "sor" else 5 * eps), (err, it)
+
+
+@pytest.mark.parametrize("shape,bcs", VARIANTS)
+def test_mixed_precision_multigrid(oracle, o3d, shape, bcs):
+    """FP32 V-cycles inside the FP64 correction loop reach the FP64 fixed point."""
+    eps = 1e-9
+    c = _case(oracle, shape, bcs)
+    rhs = _compatible_rhs(c, 9)
+    ref = oracle.field3(c.shape)
+    oracle.poisson_sor(c, ref, rhs, 1.8, eps * 1e-3, 200000)
+    with o3d.Context(params_of(o3d, c, solver=o3d.SOLVER_MG, precision=o3d.PREC_MIXED)) as ctx:
+        got = ctx.field()
+        st, it, dm, om = ctx.poisson_solve(got, rhs, 1.0, eps, 100, 0)
+    assert st == o3d.OK, (st, it, dm)
+    # the rhs itself is rounded to FP32 in the mixed method
+    err = np.abs(_demean(got) - _demean(ref)).max()
+    assert err < 1e-6 * np.abs(ref).max() + 5 * eps, err
+
+
+def test_dynamic_omega_follows_reference_rule(oracle, o3d):
+    """idyn = 1: same omega trajectory rule (src/poisson.f90:115-121); the final
+    omega of a long solve stays within the rule's bounds."""
+    c = _case(oracle, (32, 32, 32), (0, 0, 0))
+    rhs = _compatible_rhs(c, 11)
+    with o3d.Context(params_of(o3d, c)) as ctx:
+        got = ctx.field()
+        st, it, dm, om = ctx.poisson_solve(got, rhs, 1.5, 1e-8, 5000, 1)
+    assert 0.0 < om <= 2.0
+    assert st in (o3d.OK, o3d.WARN_STAGNATION)
+
+
+def test_incompatible_rhs_stagnates_like_reference(oracle, o3d):
+    """A constant rhs on the all-mirror grid has no solution; the reference's
+    SOR ends on its stagnation test (src/poisson.f90:111-114) and so does the
+    GPU red-black SOR."""
+    c = _case(oracle, (17, 17, 17), (1, 1, 1))
+    rhs = np.asfortranarray(np.ones(c.shape))
+    ref = oracle.field3(c.shape)
+    st_ref, _, _, _ = oracle.poisson_sor(c, ref, rhs, 1.5, 1e-8, 20000)
+    with o3d.Context(params_of(o3d, c)) as ctx:
+        got = ctx.field()
+        st, it, dm, om = ctx.poisson_solve(got, rhs, 1.5, 1e-8, 20000, 0)
+    assert st_ref == oracle.SOR_STAGNATED
+    assert st == o3d.WARN_STAGNATION
