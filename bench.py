@@ -276,8 +276,8 @@ def gpu_arm(args, rank, world, local):
                                precision=o3d.PREC_FP64, solver=o3d.SOLVER_SOR, kmax=20000)
         c3.close()
         variants["fp64_rbsor"] = v
-    e2e = measure_e2e(o3d, max(3, args.steps // 2), 3, world, precision=o3d.PREC_MIXED,
-                      solver=o3d.SOLVER_MG, kmax=100)
+    e2e = None if args.no_e2e else measure_e2e(o3d, max(3, args.steps // 2), 3, world,
+                                                precision=o3d.PREC_MIXED, solver=o3d.SOLVER_MG, kmax=100)
     line = {
         "metric": METRIC,
         "value": head["mpts_per_s"],
@@ -340,6 +340,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="headline variant only")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end run")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

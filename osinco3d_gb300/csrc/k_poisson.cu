@@ -103,6 +103,26 @@ void launch_sor_fixed(double* p, const double* rhs, const Grid& g, const PoiCoef
 // multigrid
 // ---------------------------------------------------------------------------
 
+// block-wide max of nonnegative floats, result valid in thread 0
+__device__ __forceinline__ float block_max_f(float v) {
+  __shared__ float sh[32];
+  const int t = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int nt = blockDim.x * blockDim.y * blockDim.z;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if ((t & 31) == 0) sh[t >> 5] = v;
+  __syncthreads();
+  if (t < 32) {
+    v = t < (nt + 31) / 32 ? sh[t] : 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  }
+  return v;
+}
+
+
+
 // trapezoid weight of the left null vector of the mirror operator (1/2 at
 // the end nodes of a mirror axis, 1 elsewhere)
 __device__ __forceinline__ double wnode(const Grid& g, int i, int j, int k) {
@@ -113,32 +133,39 @@ __device__ __forceinline__ double wnode(const Grid& g, int i, int j, int k) {
   return w;
 }
 
+// sum of w*rhs with the trapezoid weights; one thread per (i, j) column
 template <class R>
 __global__ void __launch_bounds__(256) k_wmean_part(const R* __restrict__ rhs, Grid g, double* part) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
-  double r[2] = {0.0, 0.0};
-  const int ops[2] = {RED_SUM, RED_SUM};
+  double r[1] = {0.0};
+  const int ops[1] = {RED_SUM};
   if (i < g.nx && j < g.ny) {
-    const double w = wnode(g, i, j, k);
-    r[0] = w * (double)rhs[(long long)i + g.sy() * j + g.sz() * k];
-    r[1] = w;
+    double wxy = 1.0;
+    if (g.bc[0] == AX_MIRROR && (i == 0 || i == g.nx - 1)) wxy *= 0.5;
+    if (g.bc[1] == AX_MIRROR && (j == 0 || j == g.ny - 1)) wxy *= 0.5;
+    double acc = 0.0, edge = 0.0;
+    for (int k = 0; k < g.nz; ++k) {
+      const double v = (double)rhs[(long long)i + g.sy() * j + g.sz() * k];
+      if (k == 0 || k == g.nz - 1) edge += v; else acc += v;
+    }
+    const double wz = g.bc[2] == AX_MIRROR ? 0.5 : 1.0;
+    r[0] = wxy * (acc + wz * edge);
   }
-  block_reduce_store<2>(r, ops, part, block_linear_id());
+  block_reduce_store<1>(r, ops, part, block_linear_id());
 }
 
-__global__ void k_wmean_final(const double* __restrict__ part, long long nblk, SolveCtrl* ctrl) {
-  __shared__ double s0[1024], s1[1024];
-  double a = 0.0, b = 0.0;
-  for (long long q = threadIdx.x; q < nblk; q += blockDim.x) { a += part[2 * q]; b += part[2 * q + 1]; }
-  s0[threadIdx.x] = a; s1[threadIdx.x] = b;
+__global__ void k_wmean_final(const double* __restrict__ part, long long nblk, double wsum, SolveCtrl* ctrl) {
+  __shared__ double s0[1024];
+  double a = 0.0;
+  for (long long q = threadIdx.x; q < nblk; q += blockDim.x) a += part[q];
+  s0[threadIdx.x] = a;
   __syncthreads();
   for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if ((int)threadIdx.x < s) { s0[threadIdx.x] += s0[threadIdx.x + s]; s1[threadIdx.x] += s1[threadIdx.x + s]; }
+    if ((int)threadIdx.x < s) s0[threadIdx.x] += s0[threadIdx.x + s];
     __syncthreads();
   }
-  if (threadIdx.x == 0) ctrl->rhs_mean = s0[0] / s1[0];
+  if (threadIdx.x == 0) ctrl->rhs_mean = s0[0] / wsum;
 }
 
 // r0 = (rhs - mean) - A p, FP64 arithmetic, stored in T
@@ -154,6 +181,30 @@ __global__ void __launch_bounds__(256) k_resid_top(const double* __restrict__ p,
   const long long q = (long long)i + g.sy() * j + g.sz() * k;
   const double ap = lap_nb<double>(p, g, i, j, k, c) + c.A * p[q];
   r0[q] = (T)(((double)rhs[q] - ctrl->rhs_mean) - ap);
+}
+
+// same residual, plus max |r| of the block into ctrl->res_key
+template <class T, class R>
+__global__ void __launch_bounds__(256) k_resid_top_max(const double* __restrict__ p, const R* __restrict__ rhs,
+                                                       T* __restrict__ r0, Grid g, PoiCoef<double> c,
+                                                       SolveCtrl* ctrl) {
+  if (ctrl->done) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  float m = 0.f;
+  if (i < g.nx && j < g.ny) {
+    const long long q = (long long)i + g.sy() * j + g.sz() * k;
+    const double ap = lap_nb<double>(p, g, i, j, k, c) + c.A * p[q];
+    const T rv = (T)(((double)rhs[q] - ctrl->rhs_mean) - ap);
+    r0[q] = rv;
+    m = fabsf((float)rv);
+  }
+  const float bm = block_max_f(m);
+  if (threadIdx.x == 0 && threadIdx.y == 0 && bm > 0.f) {
+    // float max as double bits: the max of nonnegative doubles orders like their bits
+    atomicMax(&ctrl->res_key, (unsigned long long)__double_as_longlong((double)bm));
+  }
 }
 
 // max |rhs - mean - A p| after a solve
@@ -337,19 +388,29 @@ __global__ void __launch_bounds__(1024) k_coarse(T* __restrict__ e, const T* __r
   for (int q = t; q < n; q += blockDim.x) e[q] = se[q];
 }
 
-// p += e (FP64), max |e| into the control block
+// p += e (FP64), max |e| into the control block.  Each thread handles
+// UPD_PER consecutive-stride elements and keeps its max in the type of e, so
+// the only FP64 work is the addition itself.
+constexpr int UPD_PER = 8;
+
 template <class T>
 __global__ void __launch_bounds__(256) k_update(double* __restrict__ p, const T* __restrict__ e, long long n,
                                                 SolveCtrl* ctrl) {
   if (ctrl->done) return;
-  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  double d = 0.0;
-  if (q < n) {
-    const double ev = (double)e[q];
-    p[q] += ev;
-    d = fabs(ev);
+  const long long base = (long long)blockIdx.x * blockDim.x * UPD_PER + threadIdx.x;
+  T m = (T)0;
+#pragma unroll
+  for (int u = 0; u < UPD_PER; ++u) {
+    const long long q = base + (long long)u * blockDim.x;
+    if (q < n) {
+      const T ev = e[q];
+      p[q] += (double)ev;
+      m = fmax(m, fabs(ev));
+    }
   }
-  const double bm = block_max(d);
+  double bm;
+  if (sizeof(T) == 4) bm = (double)block_max_f((float)m);
+  else bm = block_max((double)m);
   if (threadIdx.x == 0 && bm > 0.0) atomicMax(&ctrl->dmax_key, (unsigned long long)__double_as_longlong(bm));
 }
 
@@ -360,6 +421,9 @@ __global__ void k_mg_control(SolveCtrl* c) {
   c->iter += 1;
   c->cycles += 1;
   c->dmax = dmax;
+  // max |r| of this iteration's residual (before its correction was added)
+  c->res_inf = __longlong_as_double((long long)c->res_key);
+  c->res_key = 0ull;
   if (dmax < c->eps) { c->done = 1; c->status = ST_CONVERGED; return; }
   if (fabs(c->dmax_old - dmax) < c->eps / 1000.0) { c->done = 1; c->status = ST_STAGNATED; return; }
   c->dmax_old = dmax;
@@ -414,10 +478,11 @@ void launch_mg_outer(double* p, const R* rhs, MGLevel* lv, int nlev, int pre, in
   (void)wpart;
   const MGLevel& L0 = lv[0];
   PoiCoef<double> c64 = make_poi<double>(L0.h[0], L0.h[1], L0.h[2]);
-  k_resid_top<T, R><<<g3(L0.g), dim3(32, 8), 0, s>>>(p, rhs, (T*)L0.r, L0.g, c64, ctrl);
+  k_resid_top_max<T, R><<<g3(L0.g), dim3(32, 8), 0, s>>>(p, rhs, (T*)L0.r, L0.g, c64, ctrl);
   *nl += 1;
   vcycle<T>(lv, 0, nlev, pre, post, coarse_sweeps, smooth_omega, ctrl, s, nl);
-  k_update<T><<<(unsigned)((L0.g.n + 255) / 256), 256, 0, s>>>(p, (const T*)L0.e, L0.g.n, ctrl);
+  k_update<T><<<(unsigned)((L0.g.n + 256LL * UPD_PER - 1) / (256LL * UPD_PER)), 256, 0, s>>>(p, (const T*)L0.e,
+                                                                                         L0.g.n, ctrl);
   k_mg_control<<<1, 1, 0, s>>>(ctrl);
   *nl += 2;
 }
@@ -425,8 +490,12 @@ void launch_mg_outer(double* p, const R* rhs, MGLevel* lv, int nlev, int pre, in
 template <class R>
 void launch_rhs_wmean(const R* rhs, const Grid& g, double* part, SolveCtrl* ctrl, cudaStream_t s,
                       long long* nl) {
-  k_wmean_part<R><<<g3(g), dim3(32, 8), 0, s>>>(rhs, g, part);
-  k_wmean_final<<<1, 1024, 0, s>>>(part, (long long)g3(g).x * g3(g).y * g3(g).z, ctrl);
+  const dim3 grid((g.nx + 31) / 32, (g.ny + 7) / 8, 1);
+  // sum of the weights: per axis n (periodic) or n - 1 (mirror: halves at both ends)
+  double wsum = 1.0;
+  for (int a = 0; a < 3; ++a) wsum *= g.bc[a] == AX_MIRROR ? (double)(g.len(a) - 1) : (double)g.len(a);
+  k_wmean_part<R><<<grid, dim3(32, 8), 0, s>>>(rhs, g, part);
+  k_wmean_final<<<1, 1024, 0, s>>>(part, (long long)grid.x * grid.y, wsum, ctrl);
   *nl += 2;
 }
 

@@ -84,6 +84,262 @@ __global__ void __launch_bounds__(256) k_predict(PredArgs<T> A) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// 2.5D fused predictor.  A block owns a TX x TY column of (x, y) points and
+// marches along z over a chunk of planes.  Each thread keeps the seven
+// z-neighbours of its point for the three components in a register queue;
+// the current plane's x- and y-lines (with 3-point halos, ghost-mapped at the
+// domain ends) are staged in double-buffered shared memory, so every value
+// is read from global memory once per plane plus the halos.
+// ---------------------------------------------------------------------------
+template <class T, class S>
+__device__ __forceinline__ T ldg_map(const S* __restrict__ f, const Grid& g, int i, int j, int k,
+                                     int odd_axis) {
+  bool fx, fy, fz;
+  const int ii = ghost(i, g.nx, g.bc[0], &fx);
+  const int jj = ghost(j, g.ny, g.bc[1], &fy);
+  const int kk = ghost(k, g.nz, g.bc[2] == AX_ZERO ? AX_PERIODIC : g.bc[2], &fz);
+  const T v = (T)__ldg(f + ii + g.sy() * jj + g.sz() * kk);
+  const bool neg = (fx && odd_axis == 0) || (fy && odd_axis == 1) || (fz && odd_axis == 2);
+  return neg ? -v : v;
+}
+
+template <class T, int TX, int TY>
+__global__ void __launch_bounds__(TX * TY) k_predict25(PredArgs<T> A, int kc) {
+  const Grid& g = A.g;
+  __shared__ T sx[2][3][TY][TX + 6];
+  __shared__ T sy[2][3][TY + 6][TX];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+  const int i = i0 + tx, j = j0 + ty;
+  const bool valid = i < g.nx && j < g.ny;
+  const int ic = valid ? i : min(i, g.nx - 1), jc = valid ? j : min(j, g.ny - 1);
+  const int k0 = blockIdx.z * kc;
+  const int k1 = min(k0 + kc, g.nz);
+  const bool zon = g.bc[2] != AX_ZERO;
+
+  // register queue: q[c][m] = u_c(i, j, k - 3 + m)
+  T q[3][7];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int m = 0; m < 6; ++m) q[c][m + 1] = zon || m == 2 ? ldg_map<T>(A.u[c], g, ic, jc, k0 - 3 + m, c) : (T)0;
+
+  int buf = 0;
+  for (int k = k0; k < k1; ++k) {
+    // advance the queue: plane k+3 enters
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+#pragma unroll
+      for (int m = 0; m < 6; ++m) q[c][m] = q[c][m + 1];
+      q[c][6] = zon ? ldg_map<T>(A.u[c], g, ic, jc, k + 3, c) : (T)0;
+      if (!zon) q[c][3] = ldg_map<T>(A.u[c], g, ic, jc, k, c);
+    }
+    // stage plane k: centre from the queue, halos from global memory
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      sx[buf][c][ty][tx + 3] = q[c][3];
+      sy[buf][c][ty + 3][tx] = q[c][3];
+      if (tx < 3) {
+        sx[buf][c][ty][tx] = ldg_map<T>(A.u[c], g, i0 - 3 + tx, jc, k, c);
+        sx[buf][c][ty][TX + 3 + tx] = ldg_map<T>(A.u[c], g, i0 + TX + tx, jc, k, c);
+      }
+      if (ty < 3) {
+        sy[buf][c][ty][tx] = ldg_map<T>(A.u[c], g, ic, j0 - 3 + ty, k, c);
+        sy[buf][c][TY + 3 + ty][tx] = ldg_map<T>(A.u[c], g, ic, j0 + TY + ty, k, c);
+      }
+    }
+    __syncthreads();
+    T g1[3][3], g2[3][3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      T v[7];
+#pragma unroll
+      for (int m = 0; m < 7; ++m) v[m] = sx[buf][c][ty][tx + m];
+      g1[c][0] = d1(v, A.cf.ax[0]);
+      g2[c][0] = d2(v, A.cf.ax[0]);
+#pragma unroll
+      for (int m = 0; m < 7; ++m) v[m] = sy[buf][c][ty + m][tx];
+      g1[c][1] = d1(v, A.cf.ax[1]);
+      g2[c][1] = d2(v, A.cf.ax[1]);
+      if (zon) {
+        g1[c][2] = d1(q[c], A.cf.ax[2]);
+        g2[c][2] = d2(q[c], A.cf.ax[2]);
+      } else {
+        g1[c][2] = (T)0;
+        g2[c][2] = (T)0;
+      }
+    }
+    if (valid) {
+      const long long p = (long long)i + g.sy() * j + g.sz() * k;
+      T nut = (T)0;
+      if (A.les) {
+        const T s11 = g1[0][0], s22 = g1[1][1], s33 = g1[2][2];
+        const T s12 = (T)0.5 * (g1[0][1] + g1[1][0]);
+        const T s13 = (T)0.5 * (g1[0][2] + g1[2][0]);
+        const T s23 = (T)0.5 * (g1[1][2] + g1[2][1]);
+        const T smag = sqrt((T)2 * (s11 * s11 + s22 * s22 + s33 * s33 +
+                                    (T)2 * (s12 * s12 + s13 * s13 + s23 * s23)));
+        nut = A.csd2 * smag;
+        A.nu_t[p] = nut;
+      }
+      const T nu_eff = A.onere + nut;
+      const T uc0 = q[0][3], uc1 = q[1][3], uc2 = q[2][3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const T F = nu_eff * (g2[c][0] + g2[c][1] + g2[c][2]) -
+                    (uc0 * g1[c][0] + uc1 * g1[c][1] + uc2 * g1[c][2]);
+        T up = q[c][3] + A.adu * F;
+        if (A.f2[c]) up = up + A.bdu * __ldg(A.f2[c] + p);
+        if (A.f3[c]) up = up + A.cdu * __ldg(A.f3[c] + p);
+        A.fnew[c][p] = F;
+        A.up[c][p] = up;
+      }
+    }
+    buf ^= 1;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 2.5D divergence (src/differential_operators.f90:25-35) -> optional output
+// div*scale, with function_stats (src/functions.f90:27-63) accumulated per
+// thread over its z-column and reduced once per block.
+// ---------------------------------------------------------------------------
+template <class T, class O, int TX, int TY>
+__global__ void __launch_bounds__(TX * TY) k_div25(const T* __restrict__ fx, const T* __restrict__ fy,
+                                                   const T* __restrict__ fz, O* __restrict__ out, Grid g,
+                                                   Coef3<T> cf, int odd, T dt, int divide, StatPart* part,
+                                                   int kc) {
+  __shared__ T sx[2][TY][TX + 6];
+  __shared__ T sy[2][TY + 6][TX];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+  const int i = i0 + tx, j = j0 + ty;
+  const bool valid = i < g.nx && j < g.ny;
+  const int ic = min(i, g.nx - 1), jc = min(j, g.ny - 1);
+  const int k0 = blockIdx.z * kc;
+  const int k1 = min(k0 + kc, g.nz);
+  const bool zon = g.bc[2] != AX_ZERO;
+  const int ox = odd ? 0 : -1, oy = odd ? 1 : -1, oz = odd ? 2 : -1;
+  T q[7];
+#pragma unroll
+  for (int m = 0; m < 6; ++m) q[m + 1] = zon ? ldg_map<T>(fz, g, ic, jc, k0 - 3 + m, oz) : (T)0;
+  T mn = (T)INFINITY, mx = (T)-INFINITY;
+  long long imx = 0x7fffffffffffffffll;
+  double sum = 0.0;
+  int buf = 0;
+  for (int k = k0; k < k1; ++k) {
+#pragma unroll
+    for (int m = 0; m < 6; ++m) q[m] = q[m + 1];
+    q[6] = zon ? ldg_map<T>(fz, g, ic, jc, k + 3, oz) : (T)0;
+    sx[buf][ty][tx + 3] = ldg_map<T>(fx, g, ic, jc, k, ox);
+    sy[buf][ty + 3][tx] = ldg_map<T>(fy, g, ic, jc, k, oy);
+    if (tx < 3) {
+      sx[buf][ty][tx] = ldg_map<T>(fx, g, i0 - 3 + tx, jc, k, ox);
+      sx[buf][ty][TX + 3 + tx] = ldg_map<T>(fx, g, i0 + TX + tx, jc, k, ox);
+    }
+    if (ty < 3) {
+      sy[buf][ty][tx] = ldg_map<T>(fy, g, ic, j0 - 3 + ty, k, oy);
+      sy[buf][TY + 3 + ty][tx] = ldg_map<T>(fy, g, ic, j0 + TY + ty, k, oy);
+    }
+    __syncthreads();
+    T v[7];
+#pragma unroll
+    for (int m = 0; m < 7; ++m) v[m] = sx[buf][ty][tx + m];
+    const T ddx = d1(v, cf.ax[0]);
+#pragma unroll
+    for (int m = 0; m < 7; ++m) v[m] = sy[buf][ty + m][tx];
+    const T ddy = d1(v, cf.ax[1]);
+    const T ddz = zon ? d1(q, cf.ax[2]) : (T)0;
+    const T div = ddx + ddy + ddz;
+    if (valid) {
+      const long long p = (long long)i + g.sy() * j + g.sz() * k;
+      if (out) out[p] = (O)(divide ? div / dt : div);
+      sum += (double)div;
+      if (div < mn) mn = div;
+      if (div > mx) { mx = div; imx = p; }  // k ascends: the first max of the column is kept
+    }
+    buf ^= 1;
+  }
+  if (part) {
+    StatPart st;
+    st.mn = (double)mn; st.mx = (double)mx; st.sum = sum; st.imx = imx;
+    if (!(mx >= mn)) { st.mn = INFINITY; st.mx = -INFINITY; st.imx = 0x7fffffffffffffffll; }
+    block_stat(st, part, block_linear_id());
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 2.5D correct_velocity (src/integration.f90:297-325) with the per-step
+// extrema of the corrected velocity accumulated per thread.
+// ---------------------------------------------------------------------------
+template <class T, class P, int TX, int TY>
+__global__ void __launch_bounds__(TX * TY) k_correct25(CorrArgs<T, P> A, int kc) {
+  const Grid& g = A.g;
+  __shared__ T sx[2][TY][TX + 6];
+  __shared__ T sy[2][TY + 6][TX];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+  const int i = i0 + tx, j = j0 + ty;
+  const bool valid = i < g.nx && j < g.ny;
+  const int ic = min(i, g.nx - 1), jc = min(j, g.ny - 1);
+  const int k0 = blockIdx.z * kc;
+  const int k1 = min(k0 + kc, g.nz);
+  const bool zon = g.bc[2] != AX_ZERO;
+  T q[7];
+#pragma unroll
+  for (int m = 0; m < 6; ++m) q[m + 1] = ldg_map<T>(A.p, g, ic, jc, k0 - 3 + m, -1);
+  T mn[3], mx[3], am[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) { mn[a] = (T)INFINITY; mx[a] = (T)-INFINITY; am[a] = (T)0; }
+  bool nan = false;
+  int buf = 0;
+  for (int k = k0; k < k1; ++k) {
+#pragma unroll
+    for (int m = 0; m < 6; ++m) q[m] = q[m + 1];
+    q[6] = ldg_map<T>(A.p, g, ic, jc, k + 3, -1);
+    sx[buf][ty][tx + 3] = q[3];
+    sy[buf][ty + 3][tx] = q[3];
+    if (tx < 3) {
+      sx[buf][ty][tx] = ldg_map<T>(A.p, g, i0 - 3 + tx, jc, k, -1);
+      sx[buf][ty][TX + 3 + tx] = ldg_map<T>(A.p, g, i0 + TX + tx, jc, k, -1);
+    }
+    if (ty < 3) {
+      sy[buf][ty][tx] = ldg_map<T>(A.p, g, ic, j0 - 3 + ty, k, -1);
+      sy[buf][TY + 3 + ty][tx] = ldg_map<T>(A.p, g, ic, j0 + TY + ty, k, -1);
+    }
+    __syncthreads();
+    T v[7], gp[3];
+#pragma unroll
+    for (int m = 0; m < 7; ++m) v[m] = sx[buf][ty][tx + m];
+    gp[0] = d1(v, A.cf.ax[0]);
+#pragma unroll
+    for (int m = 0; m < 7; ++m) v[m] = sy[buf][ty + m][tx];
+    gp[1] = d1(v, A.cf.ax[1]);
+    gp[2] = zon ? d1(q, A.cf.ax[2]) : (T)0;
+    if (valid) {
+      const long long p = (long long)i + g.sy() * j + g.sz() * k;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const T un = __ldg(A.up[a] + p) - A.dt * gp[a];
+        A.u[a][p] = un;
+        if (un != un) nan = true;
+        mn[a] = fmin(mn[a], un);
+        mx[a] = fmax(mx[a], un);
+        am[a] = fmax(am[a], fabs(un));
+      }
+    }
+    buf ^= 1;
+  }
+  double r[10];
+  const int ops[10] = {RED_MIN, RED_MIN, RED_MIN, RED_MAX, RED_MAX, RED_MAX,
+                       RED_MAX, RED_MAX, RED_MAX, RED_MAX};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) { r[a] = (double)mn[a]; r[3 + a] = (double)mx[a]; r[6 + a] = (double)am[a]; }
+  r[9] = nan ? 1.0 : 0.0;
+  block_reduce_store<10>(r, ops, A.part, block_linear_id());
+}
+
 // standalone calculate_nu_t (src/les_turbulence.f90:54-88)
 template <class T>
 __global__ void k_nu_t(const T* __restrict__ ux, const T* __restrict__ uy, const T* __restrict__ uz,
@@ -302,7 +558,8 @@ __global__ void k_finalize(const double* __restrict__ part, long long nblk, int 
   for (int q = 0; q < M; ++q) {
     const int op = (int)((opmask >> (2 * q)) & 3ull);
     double acc = red_ident(op);
-    for (long long b = threadIdx.x; b < nblk; b += blockDim.x) acc = red_apply(op, acc, part[b * M + q]);
+    const double* slot = part + (long long)q * nblk;
+    for (long long b = threadIdx.x; b < nblk; b += blockDim.x) acc = red_apply(op, acc, slot[b]);
     sh[threadIdx.x] = acc;
     __syncthreads();
     for (int s = blockDim.x / 2; s > 0; s >>= 1) {
@@ -356,23 +613,34 @@ void launch_der(const T* f, T* df, const Grid& g, const AxisCoef<T>& c, int axis
                 int odd, cudaStream_t s) {
   k_der<T><<<pt_grid(g), pt_block(), 0, s>>>(f, df, g, c, axis, order, odd);
 }
+constexpr int PRED_TX = 32, PRED_TY = 8, PRED_KC = 32;
+
 template <class T>
 void launch_predict(const PredArgs<T>& a, cudaStream_t s) {
-  k_predict<T><<<pt_grid(a.g), pt_block(), 0, s>>>(a);
+  const Grid& g = a.g;
+  dim3 grid((g.nx + PRED_TX - 1) / PRED_TX, (g.ny + PRED_TY - 1) / PRED_TY, (g.nz + PRED_KC - 1) / PRED_KC);
+  k_predict25<T, PRED_TX, PRED_TY><<<grid, dim3(PRED_TX, PRED_TY), 0, s>>>(a, PRED_KC);
 }
 template <class T>
 void launch_nu_t(const T* ux, const T* uy, const T* uz, T* nu, const Grid& g, const Coef3<T>& cf,
                  T csd2, cudaStream_t s) {
   k_nu_t<T><<<pt_grid(g), pt_block(), 0, s>>>(ux, uy, uz, nu, g, cf, csd2);
 }
+constexpr int Z_TX = 32, Z_TY = 8, Z_KC = 32;
+static inline dim3 z_grid(const Grid& g) {
+  return dim3((g.nx + Z_TX - 1) / Z_TX, (g.ny + Z_TY - 1) / Z_TY, (g.nz + Z_KC - 1) / Z_KC);
+}
+long long z_blocks(const Grid& g) { dim3 b = z_grid(g); return (long long)b.x * b.y * b.z; }
+
 template <class T, class O>
 void launch_div(const T* fx, const T* fy, const T* fz, O* out, const Grid& g, const Coef3<T>& cf,
                 int odd, T dt, int divide, StatPart* part, cudaStream_t s) {
-  k_div<T, O><<<pt_grid(g), pt_block(), 0, s>>>(fx, fy, fz, out, g, cf, odd, dt, divide, part);
+  k_div25<T, O, Z_TX, Z_TY><<<z_grid(g), dim3(Z_TX, Z_TY), 0, s>>>(fx, fy, fz, out, g, cf, odd, dt, divide,
+                                                                     part, Z_KC);
 }
 template <class T, class P>
 void launch_correct(const CorrArgs<T, P>& a, cudaStream_t s) {
-  k_correct<T, P><<<pt_grid(a.g), pt_block(), 0, s>>>(a);
+  k_correct25<T, P, Z_TX, Z_TY><<<z_grid(a.g), dim3(Z_TX, Z_TY), 0, s>>>(a, Z_KC);
 }
 template <class T>
 void launch_stats(const T* ux, const T* uy, const T* uz, const Grid& g, const Coef3<T>& cf,

@@ -240,7 +240,7 @@ int rhs_t(o3d_ctx* c) {
   Coef3<T> cf = cast_coef<T>(c->cf);
   launch_div<T, T>((const T*)c->up[0], (const T*)c->up[1], (const T*)c->up[2], (T*)c->rhs, c->g, cf,
                    1, (T)c->P.dt, 1, c->spart, c->s);
-  launch_finalize_stats(c->spart, pt_blocks(c->g), c->g, c->diag->divp, c->s);
+  launch_finalize_stats(c->spart, z_blocks(c->g), c->g, c->diag->divp, c->s);
   c->launches += 2;
   CKL();
   return O3D_OK;
@@ -262,7 +262,7 @@ int correct_t(o3d_ctx* c) {
   // min x3, max x3, |max| x3, nan flag
   unsigned long long ops = 0;
   for (int q = 0; q < 10; ++q) ops |= (unsigned long long)(q < 3 ? RED_MIN : RED_MAX) << (2 * q);
-  launch_finalize(c->part, pt_blocks(c->g), 10, ops, c->diag->sums, c->s);
+  launch_finalize(c->part, z_blocks(c->g), 10, ops, c->diag->sums, c->s);
   c->launches += 2;
   CKL();
   return O3D_OK;
@@ -273,7 +273,7 @@ int divu_diag_t(o3d_ctx* c) {
   Coef3<T> cf = cast_coef<T>(c->cf);
   launch_div<T, T>((const T*)c->u[0], (const T*)c->u[1], (const T*)c->u[2], (T*)nullptr, c->g, cf, 1,
                    (T)c->P.dt, 0, c->spart, c->s);
-  launch_finalize_stats(c->spart, pt_blocks(c->g), c->g, c->diag->divu, c->s);
+  launch_finalize_stats(c->spart, z_blocks(c->g), c->g, c->diag->divu, c->s);
   c->launches += 2;
   CKL();
   return O3D_OK;
@@ -458,11 +458,17 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
     if ((st = read_ctrl(c))) return st;
     if (c->ctrl_h->done) break;
   }
-  PoiCoef<double> pc = make_poi<double>(c->dx, c->dy, c->dz);
-  if (c->mixed) launch_residual_inf<float>(c->pp, (const float*)c->rhs, c->gp, pc, use_mg, c->ctrl, c->s);
-  else launch_residual_inf<double>(c->pp, (const double*)c->rhs, c->gp, pc, use_mg, c->ctrl, c->s);
-  c->launches++;
-  CKL();
+  // SOR: max |rhs - A p| of the final pressure; multigrid: max |r| of the
+  // last outer iteration's residual, recorded by the loop itself (a second
+  // FP64 pass would cost as much as a fifth of a cycle)
+  if (!use_mg || c->P.diagnostics >= 2) {
+    PoiCoef<double> pc = make_poi<double>(c->dx, c->dy, c->dz);
+    CK(cudaMemsetAsync(&c->ctrl->res_key, 0, sizeof(unsigned long long), c->s));
+    if (c->mixed) launch_residual_inf<float>(c->pp, (const float*)c->rhs, c->gp, pc, use_mg, c->ctrl, c->s);
+    else launch_residual_inf<double>(c->pp, (const double*)c->rhs, c->gp, pc, use_mg, c->ctrl, c->s);
+    c->launches++;
+    CKL();
+  }
   CK(cudaEventRecord(c->ev[3], c->s));
   if ((st = read_ctrl(c))) return st;
   const SolveCtrl* h = c->ctrl_h;
@@ -471,7 +477,7 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
     info->poisson_iters = h->iter;
     info->poisson_cycles = h->cycles;
     info->poisson_dmax = h->dmax;
-    info->poisson_res_inf = bits_to_double(h->res_key);
+    info->poisson_res_inf = (!use_mg || c->P.diagnostics >= 2) ? bits_to_double(h->res_key) : h->res_inf;
     info->omega = h->omega;
     float ms = 0.f;
     cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);

@@ -230,9 +230,10 @@ __device__ __forceinline__ StatPart stat_of(double v, long long idx, bool valid)
 }
 
 // ---- M-slot block reductions with per-slot operator -----------------------
-// ops is a compile-time list of RED_SUM / RED_MIN / RED_MAX; one record of M
-// doubles per block goes to part[blk*M ..]; k_finalize reduces the records in
-// a fixed order (deterministic sums).
+// ops is a compile-time list of RED_SUM / RED_MIN / RED_MAX; slot q of block
+// blk goes to part[q*nblk + blk] (slot-major, so the finalizer reads each
+// slot coalesced); k_finalize reduces the records in a fixed order
+// (deterministic sums).
 enum RedOp { RED_SUM = 0, RED_MIN = 1, RED_MAX = 2 };
 
 __device__ __forceinline__ double red_apply(int op, double a, double b) {
@@ -245,6 +246,7 @@ __device__ __forceinline__ double red_ident(int op) {
 template <int M>
 __device__ inline void block_reduce_store(double (&v)[M], const int (&ops)[M], double* part,
                                           long long blk) {
+  const long long nblk = (long long)gridDim.x * gridDim.y * gridDim.z;
   __shared__ double sh[M][32];
   const int t = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
   const int nt = blockDim.x * blockDim.y * blockDim.z;
@@ -266,7 +268,7 @@ __device__ inline void block_reduce_store(double (&v)[M], const int (&ops)[M], d
       double x = t < nw ? sh[q][t] : red_ident(ops[q]);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) x = red_apply(ops[q], x, __shfl_xor_sync(0xffffffffu, x, o));
-      if (t == 0) part[blk * M + q] = x;
+      if (t == 0) part[(long long)q * nblk + blk] = x;
     }
   }
 }

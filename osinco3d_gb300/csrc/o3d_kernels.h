@@ -49,6 +49,8 @@ struct ScalArgs {
 };
 
 long long pt_blocks(const Grid& g);
+// blocks of the z-marching (2.5D) kernels: divergence and correction
+long long z_blocks(const Grid& g);
 
 template <class T>
 void launch_der(const T* f, T* df, const Grid& g, const AxisCoef<T>& c, int axis, int order,

@@ -39,12 +39,31 @@ def free_slip_case(oracle, n, **kw):
     return oracle.Case(n, n, n, PI, PI, PI, **base)
 
 
-def perturbed(u, seed, amp=1e-2):
-    """u plus a smooth seeded perturbation (keeps every field nonzero and generic)."""
+def _mode(n, kind, k, phase):
+    """One smooth mode on n nodes: 'per' has period n points, 'even'/'odd' are
+    symmetric/antisymmetric about both end nodes (the free-slip parities)."""
+    i = np.arange(n)
+    if kind == "per":
+        return np.sin(2 * PI * k * i / n + phase)
+    s = i / (n - 1)
+    return np.cos(PI * k * s) if kind == "even" else np.sin(PI * k * s)
+
+
+def perturbed(u, seed, amp=1e-2, kinds=("per", "per", "per")):
+    """u plus a smooth seeded perturbation with the given parity per axis, so
+    that it respects the closures of the field (periodic, even or odd)."""
     rng = np.random.default_rng(seed)
     nx, ny, nz = u.shape
-    x = np.linspace(0, 1, nx)[:, None, None]
-    y = np.linspace(0, 1, ny)[None, :, None]
-    z = np.linspace(0, 1, nz)[None, None, :]
-    a, b, c, d = rng.uniform(0.5, 3.0, 4)
-    return np.asfortranarray(u + amp * np.sin(a * x + d) * np.cos(b * y + 0.3) * np.sin(c * z + 0.7))
+    k = rng.integers(1, 4, 3)
+    ph = rng.uniform(0, 2 * PI, 3)
+    fx = _mode(nx, kinds[0], k[0], ph[0])[:, None, None]
+    fy = _mode(ny, kinds[1], k[1], ph[1])[None, :, None]
+    fz = _mode(nz, kinds[2], k[2], ph[2])[None, None, :]
+    return np.asfortranarray(u + amp * fx * fy * fz)
+
+
+def kinds_of(case, comp):
+    """Parity of velocity component `comp` per axis: periodic axes stay
+    periodic; on free-slip axes the component normal to the wall is odd."""
+    bcs = (case.bcx, case.bcy, case.bcz)
+    return tuple("per" if bcs[a] == 0 else ("odd" if a == comp else "even") for a in range(3))

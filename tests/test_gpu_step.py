@@ -4,11 +4,12 @@ diagnostics after N steps.
 
 Both sides solve the pressure to eps = 1e-11 so that the red-black versus
 lexicographic iterate order leaves differences far below the tolerance:
-velocity 1e-9 relative, pressure (mean removed) 1e-8 relative."""
+velocity 1e-9 relative; pressure (mean removed) 1e-8 of max |p| plus
+100 eps for the update-norm stop test."""
 import numpy as np
 import pytest
 
-from _util import PI, free_slip_case, params_of, periodic_case, perturbed, rel_err
+from _util import PI, free_slip_case, kinds_of, params_of, periodic_case, perturbed, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -21,9 +22,10 @@ def _run_both(oracle, o3d, c, nsteps, init="tgv", **extra):
         oracle.init_tgv(c, s)
     else:
         oracle.init_mixing_layer(c, s)
-    # a smooth seeded perturbation breaks the symmetries of the analytic states
+    # a smooth seeded perturbation (with each component's free-slip parity)
+    # breaks the symmetries of the analytic states
     for a in range(3):
-        s.u[a][...] = perturbed(s.u[a], 30 + a)
+        s.u[a][...] = perturbed(s.u[a], 30 + a, kinds=kinds_of(c, a))
     runner = oracle.Runner(c, s)
     ctx = o3d.Context(params_of(o3d, c, **extra))
     for a, name in enumerate(("ux", "uy", "uz")):
@@ -36,6 +38,8 @@ def _run_both(oracle, o3d, c, nsteps, init="tgv", **extra):
     for it in range(1, nsteps + 1):
         ri = runner.step(it)
         gi = ctx.step(it)
+        # a compatible right-hand side: the reference's SOR converges
+        assert ri.sor_status == oracle.SOR_CONVERGED, (it, ri.sor_status)
         infos.append((ri, gi))
     return s, ctx, infos
 
@@ -47,8 +51,11 @@ def _check_fields(s, ctx, c, tol_u=1e-9, tol_p=1e-8):
             assert np.abs(ctx.download(name)).max() < 1e-12
         else:
             assert rel_err(ctx.download(name), ref) < tol_u, name
+    # pressure up to its free constant: relative to max |p|, plus the SOR
+    # stop-test error (about 50 eps on the mirror grids)
     p = ctx.download("pp")
-    assert rel_err(p - p.mean(), s.pp - s.pp.mean()) < tol_p
+    dp = np.abs((p - p.mean()) - (s.pp - s.pp.mean())).max()
+    assert dp <= tol_p * np.abs(s.pp).max() + 100 * c.eps, dp
     if c.nscr:
         assert rel_err(ctx.download("phi"), s.phi) < tol_u
 
@@ -66,7 +73,7 @@ def test_tgv_periodic_steps(oracle, o3d, itscheme):
             assert gi.divu_pred_stats[q] == pytest.approx(ri.divu_pred_stats[q], rel=1e-7, abs=1e-9)
             assert gi.divu_stats[q] == pytest.approx(ri.divu_stats[q], rel=1e-6, abs=1e-8)
         for q in range(3):
-            assert gi.cfl[q] == pytest.approx(ri.cfl[q], rel=1e-10, abs=1e-14)
+            assert gi.cfl[q] == pytest.approx(ri.cfl[q], rel=1e-8, abs=1e-14)
     ctx.close()
 
 
