@@ -105,49 +105,80 @@ __device__ __forceinline__ T ldg_map(const S* __restrict__ f, const Grid& g, int
 }
 
 template <class T, int TX, int TY>
-__global__ void __launch_bounds__(TX * TY) k_predict25(PredArgs<T> A, int kc) {
+__global__ void __launch_bounds__(TX * TY, sizeof(T) == 4 ? 3 : 1) k_predict25(PredArgs<T> A, int kc) {
   const Grid& g = A.g;
   __shared__ T sx[2][3][TY][TX + 6];
   __shared__ T sy[2][3][TY + 6][TX];
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
   const int i = i0 + tx, j = j0 + ty;
+  // points past the grid end still stage ghost-mapped values: the lines of
+  // the last valid points read them
   const bool valid = i < g.nx && j < g.ny;
-  const int ic = valid ? i : min(i, g.nx - 1), jc = valid ? j : min(j, g.ny - 1);
   const int k0 = blockIdx.z * kc;
   const int k1 = min(k0 + kc, g.nz);
   const bool zon = g.bc[2] != AX_ZERO;
+  const bool hx = tx < 3, hy = ty < 3;
+  const int hxi0 = i0 - 3 + tx, hxi1 = i0 + TX + tx;  // x-halo columns of this thread
+  const int hyj0 = j0 - 3 + ty, hyj1 = j0 + TY + ty;  // y-halo rows of this thread
 
   // register queue: q[c][m] = u_c(i, j, k - 3 + m)
   T q[3][7];
 #pragma unroll
   for (int c = 0; c < 3; ++c)
 #pragma unroll
-    for (int m = 0; m < 6; ++m) q[c][m + 1] = zon || m == 2 ? ldg_map<T>(A.u[c], g, ic, jc, k0 - 3 + m, c) : (T)0;
+    for (int m = 0; m < 6; ++m) q[c][m + 1] = zon || m == 2 ? ldg_map<T>(A.u[c], g, i, j, k0 - 3 + m, c) : (T)0;
+  // halos of the first plane
+  T hxv[3][2], hyv[3][2];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    hxv[c][0] = hx ? ldg_map<T>(A.u[c], g, hxi0, j, k0, c) : (T)0;
+    hxv[c][1] = hx ? ldg_map<T>(A.u[c], g, hxi1, j, k0, c) : (T)0;
+    hyv[c][0] = hy ? ldg_map<T>(A.u[c], g, i, hyj0, k0, c) : (T)0;
+    hyv[c][1] = hy ? ldg_map<T>(A.u[c], g, i, hyj1, k0, c) : (T)0;
+  }
 
   int buf = 0;
   for (int k = k0; k < k1; ++k) {
-    // advance the queue: plane k+3 enters
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
 #pragma unroll
       for (int m = 0; m < 6; ++m) q[c][m] = q[c][m + 1];
-      q[c][6] = zon ? ldg_map<T>(A.u[c], g, ic, jc, k + 3, c) : (T)0;
-      if (!zon) q[c][3] = ldg_map<T>(A.u[c], g, ic, jc, k, c);
-    }
-    // stage plane k: centre from the queue, halos from global memory
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
+      if (!zon) q[c][3] = ldg_map<T>(A.u[c], g, i, j, k, c);
+      // stage plane k
       sx[buf][c][ty][tx + 3] = q[c][3];
       sy[buf][c][ty + 3][tx] = q[c][3];
-      if (tx < 3) {
-        sx[buf][c][ty][tx] = ldg_map<T>(A.u[c], g, i0 - 3 + tx, jc, k, c);
-        sx[buf][c][ty][TX + 3 + tx] = ldg_map<T>(A.u[c], g, i0 + TX + tx, jc, k, c);
+      if (hx) {
+        sx[buf][c][ty][tx] = hxv[c][0];
+        sx[buf][c][ty][TX + 3 + tx] = hxv[c][1];
       }
-      if (ty < 3) {
-        sy[buf][c][ty][tx] = ldg_map<T>(A.u[c], g, ic, j0 - 3 + ty, k, c);
-        sy[buf][c][TY + 3 + ty][tx] = ldg_map<T>(A.u[c], g, ic, j0 + TY + ty, k, c);
+      if (hy) {
+        sy[buf][c][ty][tx] = hyv[c][0];
+        sy[buf][c][TY + 3 + ty][tx] = hyv[c][1];
       }
+    }
+    // issue the loads of the next plane (queue head and halos) before computing
+    const int kn = k + 1;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      q[c][6] = zon ? ldg_map<T>(A.u[c], g, i, j, k + 3, c) : (T)0;
+      if (kn < k1) {
+        if (hx) {
+          hxv[c][0] = ldg_map<T>(A.u[c], g, hxi0, j, kn, c);
+          hxv[c][1] = ldg_map<T>(A.u[c], g, hxi1, j, kn, c);
+        }
+        if (hy) {
+          hyv[c][0] = ldg_map<T>(A.u[c], g, i, hyj0, kn, c);
+          hyv[c][1] = ldg_map<T>(A.u[c], g, i, hyj1, kn, c);
+        }
+      }
+    }
+    const long long p = (long long)min(i, g.nx - 1) + g.sy() * min(j, g.ny - 1) + g.sz() * k;
+    T h2[3], h3[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      h2[c] = A.f2[c] ? __ldg(A.f2[c] + p) : (T)0;
+      h3[c] = A.f3[c] ? __ldg(A.f3[c] + p) : (T)0;
     }
     __syncthreads();
     T g1[3][3], g2[3][3];
@@ -162,7 +193,7 @@ __global__ void __launch_bounds__(TX * TY) k_predict25(PredArgs<T> A, int kc) {
       for (int m = 0; m < 7; ++m) v[m] = sy[buf][c][ty + m][tx];
       g1[c][1] = d1(v, A.cf.ax[1]);
       g2[c][1] = d2(v, A.cf.ax[1]);
-      if (zon) {
+      if (zon) {  // q[c][0..6] holds planes k-3 .. k+3
         g1[c][2] = d1(q[c], A.cf.ax[2]);
         g2[c][2] = d2(q[c], A.cf.ax[2]);
       } else {
@@ -171,7 +202,6 @@ __global__ void __launch_bounds__(TX * TY) k_predict25(PredArgs<T> A, int kc) {
       }
     }
     if (valid) {
-      const long long p = (long long)i + g.sy() * j + g.sz() * k;
       T nut = (T)0;
       if (A.les) {
         const T s11 = g1[0][0], s22 = g1[1][1], s33 = g1[2][2];
@@ -190,8 +220,8 @@ __global__ void __launch_bounds__(TX * TY) k_predict25(PredArgs<T> A, int kc) {
         const T F = nu_eff * (g2[c][0] + g2[c][1] + g2[c][2]) -
                     (uc0 * g1[c][0] + uc1 * g1[c][1] + uc2 * g1[c][2]);
         T up = q[c][3] + A.adu * F;
-        if (A.f2[c]) up = up + A.bdu * __ldg(A.f2[c] + p);
-        if (A.f3[c]) up = up + A.cdu * __ldg(A.f3[c] + p);
+        if (A.f2[c]) up = up + A.bdu * h2[c];
+        if (A.f3[c]) up = up + A.cdu * h3[c];
         A.fnew[c][p] = F;
         A.up[c][p] = up;
       }
@@ -216,14 +246,20 @@ __global__ void __launch_bounds__(TX * TY) k_div25(const T* __restrict__ fx, con
   const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
   const int i = i0 + tx, j = j0 + ty;
   const bool valid = i < g.nx && j < g.ny;
-  const int ic = min(i, g.nx - 1), jc = min(j, g.ny - 1);
   const int k0 = blockIdx.z * kc;
   const int k1 = min(k0 + kc, g.nz);
   const bool zon = g.bc[2] != AX_ZERO;
   const int ox = odd ? 0 : -1, oy = odd ? 1 : -1, oz = odd ? 2 : -1;
+  const bool hx = tx < 3, hy = ty < 3;
   T q[7];
 #pragma unroll
-  for (int m = 0; m < 6; ++m) q[m + 1] = zon ? ldg_map<T>(fz, g, ic, jc, k0 - 3 + m, oz) : (T)0;
+  for (int m = 0; m < 6; ++m) q[m + 1] = zon ? ldg_map<T>(fz, g, i, j, k0 - 3 + m, oz) : (T)0;
+  // values of the next plane to stage: x-line centre and halos, y-line centre and halos
+  T cx = ldg_map<T>(fx, g, i, j, k0, ox), cy = ldg_map<T>(fy, g, i, j, k0, oy);
+  T hx0 = hx ? ldg_map<T>(fx, g, i0 - 3 + tx, j, k0, ox) : (T)0;
+  T hx1 = hx ? ldg_map<T>(fx, g, i0 + TX + tx, j, k0, ox) : (T)0;
+  T hy0 = hy ? ldg_map<T>(fy, g, i, j0 - 3 + ty, k0, oy) : (T)0;
+  T hy1 = hy ? ldg_map<T>(fy, g, i, j0 + TY + ty, k0, oy) : (T)0;
   T mn = (T)INFINITY, mx = (T)-INFINITY;
   long long imx = 0x7fffffffffffffffll;
   double sum = 0.0;
@@ -231,16 +267,17 @@ __global__ void __launch_bounds__(TX * TY) k_div25(const T* __restrict__ fx, con
   for (int k = k0; k < k1; ++k) {
 #pragma unroll
     for (int m = 0; m < 6; ++m) q[m] = q[m + 1];
-    q[6] = zon ? ldg_map<T>(fz, g, ic, jc, k + 3, oz) : (T)0;
-    sx[buf][ty][tx + 3] = ldg_map<T>(fx, g, ic, jc, k, ox);
-    sy[buf][ty + 3][tx] = ldg_map<T>(fy, g, ic, jc, k, oy);
-    if (tx < 3) {
-      sx[buf][ty][tx] = ldg_map<T>(fx, g, i0 - 3 + tx, jc, k, ox);
-      sx[buf][ty][TX + 3 + tx] = ldg_map<T>(fx, g, i0 + TX + tx, jc, k, ox);
-    }
-    if (ty < 3) {
-      sy[buf][ty][tx] = ldg_map<T>(fy, g, ic, j0 - 3 + ty, k, oy);
-      sy[buf][TY + 3 + ty][tx] = ldg_map<T>(fy, g, ic, j0 + TY + ty, k, oy);
+    sx[buf][ty][tx + 3] = cx;
+    sy[buf][ty + 3][tx] = cy;
+    if (hx) { sx[buf][ty][tx] = hx0; sx[buf][ty][TX + 3 + tx] = hx1; }
+    if (hy) { sy[buf][ty][tx] = hy0; sy[buf][TY + 3 + ty][tx] = hy1; }
+    q[6] = zon ? ldg_map<T>(fz, g, i, j, k + 3, oz) : (T)0;
+    const int kn = k + 1;
+    if (kn < k1) {
+      cx = ldg_map<T>(fx, g, i, j, kn, ox);
+      cy = ldg_map<T>(fy, g, i, j, kn, oy);
+      if (hx) { hx0 = ldg_map<T>(fx, g, i0 - 3 + tx, j, kn, ox); hx1 = ldg_map<T>(fx, g, i0 + TX + tx, j, kn, ox); }
+      if (hy) { hy0 = ldg_map<T>(fy, g, i, j0 - 3 + ty, kn, oy); hy1 = ldg_map<T>(fy, g, i, j0 + TY + ty, kn, oy); }
     }
     __syncthreads();
     T v[7];
@@ -282,13 +319,17 @@ __global__ void __launch_bounds__(TX * TY) k_correct25(CorrArgs<T, P> A, int kc)
   const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
   const int i = i0 + tx, j = j0 + ty;
   const bool valid = i < g.nx && j < g.ny;
-  const int ic = min(i, g.nx - 1), jc = min(j, g.ny - 1);
   const int k0 = blockIdx.z * kc;
   const int k1 = min(k0 + kc, g.nz);
   const bool zon = g.bc[2] != AX_ZERO;
+  const bool hx = tx < 3, hy = ty < 3;
   T q[7];
 #pragma unroll
-  for (int m = 0; m < 6; ++m) q[m + 1] = ldg_map<T>(A.p, g, ic, jc, k0 - 3 + m, -1);
+  for (int m = 0; m < 6; ++m) q[m + 1] = ldg_map<T>(A.p, g, i, j, k0 - 3 + m, -1);
+  T hx0 = hx ? ldg_map<T>(A.p, g, i0 - 3 + tx, j, k0, -1) : (T)0;
+  T hx1 = hx ? ldg_map<T>(A.p, g, i0 + TX + tx, j, k0, -1) : (T)0;
+  T hy0 = hy ? ldg_map<T>(A.p, g, i, j0 - 3 + ty, k0, -1) : (T)0;
+  T hy1 = hy ? ldg_map<T>(A.p, g, i, j0 + TY + ty, k0, -1) : (T)0;
   T mn[3], mx[3], am[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) { mn[a] = (T)INFINITY; mx[a] = (T)-INFINITY; am[a] = (T)0; }
@@ -297,17 +338,21 @@ __global__ void __launch_bounds__(TX * TY) k_correct25(CorrArgs<T, P> A, int kc)
   for (int k = k0; k < k1; ++k) {
 #pragma unroll
     for (int m = 0; m < 6; ++m) q[m] = q[m + 1];
-    q[6] = ldg_map<T>(A.p, g, ic, jc, k + 3, -1);
+    if (!zon) q[3] = ldg_map<T>(A.p, g, i, j, k, -1);
     sx[buf][ty][tx + 3] = q[3];
     sy[buf][ty + 3][tx] = q[3];
-    if (tx < 3) {
-      sx[buf][ty][tx] = ldg_map<T>(A.p, g, i0 - 3 + tx, jc, k, -1);
-      sx[buf][ty][TX + 3 + tx] = ldg_map<T>(A.p, g, i0 + TX + tx, jc, k, -1);
+    if (hx) { sx[buf][ty][tx] = hx0; sx[buf][ty][TX + 3 + tx] = hx1; }
+    if (hy) { sy[buf][ty][tx] = hy0; sy[buf][TY + 3 + ty][tx] = hy1; }
+    q[6] = ldg_map<T>(A.p, g, i, j, k + 3, -1);
+    const int kn = k + 1;
+    if (kn < k1) {
+      if (hx) { hx0 = ldg_map<T>(A.p, g, i0 - 3 + tx, j, kn, -1); hx1 = ldg_map<T>(A.p, g, i0 + TX + tx, j, kn, -1); }
+      if (hy) { hy0 = ldg_map<T>(A.p, g, i, j0 - 3 + ty, kn, -1); hy1 = ldg_map<T>(A.p, g, i, j0 + TY + ty, kn, -1); }
     }
-    if (ty < 3) {
-      sy[buf][ty][tx] = ldg_map<T>(A.p, g, ic, j0 - 3 + ty, k, -1);
-      sy[buf][TY + 3 + ty][tx] = ldg_map<T>(A.p, g, ic, j0 + TY + ty, k, -1);
-    }
+    const long long p = (long long)min(i, g.nx - 1) + g.sy() * min(j, g.ny - 1) + g.sz() * k;
+    T upv[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) upv[a] = __ldg(A.up[a] + p);
     __syncthreads();
     T v[7], gp[3];
 #pragma unroll
@@ -318,10 +363,9 @@ __global__ void __launch_bounds__(TX * TY) k_correct25(CorrArgs<T, P> A, int kc)
     gp[1] = d1(v, A.cf.ax[1]);
     gp[2] = zon ? d1(q, A.cf.ax[2]) : (T)0;
     if (valid) {
-      const long long p = (long long)i + g.sy() * j + g.sz() * k;
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
-        const T un = __ldg(A.up[a] + p) - A.dt * gp[a];
+        const T un = upv[a] - A.dt * gp[a];
         A.u[a][p] = un;
         if (un != un) nan = true;
         mn[a] = fmin(mn[a], un);
