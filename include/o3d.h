@@ -204,6 +204,27 @@ O3D_API int o3d_statistics_calc(o3d_ctx *ctx, double t, double out[17]);
  * reference (measurement hook). */
 O3D_API int o3d_time_kernel(o3d_ctx *ctx, int kernel, int reps, double *ms_per_launch);
 
+/* divergence(divf, fx, fy, fz, ..., odd) with function_stats of the result
+ * (src/differential_operators.f90:7-38, src/functions.f90:27-63) for callers
+ * that cannot allocate device memory.  No counterpart in the reference: it
+ * exists for hosts that give all device memory to their own allocator, time
+ * loops that must avoid the device-wide synchronisation of cudaMalloc and
+ * cudaFree, and code where allocation is forbidden.  It needs no context and
+ * calls no allocating routine.  d_fx, d_fy, d_fz and d_div are the caller's
+ * device buffers of nx*ny*nz doubles (d_div may be NULL); dx, dy, dz are the
+ * node spacings, bc* the O3D_BC_* code of each axis, odd selects the "i"
+ * closures; the work runs on `stream` (a cudaStream_t, NULL = default) and the
+ * call returns after stats = min, max, mean, imax, jmax, kmax (1-based) are in
+ * host memory.  Scratch: a fixed 512 KiB array in device memory, shared by
+ * every call: grids needing more than 16384 reduction blocks (beyond 512^3 or
+ * 768 x 384 x 384 points) are rejected with O3D_ERR_BADARG, and calls that
+ * overlap on the GPU race.  The first call on each device looks up the
+ * array's device address; make that first call before any stream capture. */
+O3D_API int o3d_divergence_stats_noalloc(const double *d_fx, const double *d_fy, const double *d_fz,
+                                         double *d_div, int nx, int ny, int nz, double dx, double dy,
+                                         double dz, int bcx, int bcy, int bcz, int odd, void *stream,
+                                         double stats[6]);
+
 /* Red-black SOR sweep(s) alone on device buffers: for tests of the kernel. */
 O3D_API int o3d_rbsor_sweeps_dev(o3d_ctx *ctx, double *d_pp, const double *d_rhs, double omega,
                          int nsweeps, double *dmax_last);

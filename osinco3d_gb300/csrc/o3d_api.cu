@@ -29,6 +29,16 @@ static void errf(const char* fmt, ...) {
   va_end(ap);
 }
 
+namespace o3d {
+// error text for o3d_last_error(), for the entry points of other files
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof g_err, fmt, ap);
+  va_end(ap);
+}
+}  // namespace o3d
+
 static double bits_to_double(unsigned long long k) {
   double d;
   memcpy(&d, &k, 8);

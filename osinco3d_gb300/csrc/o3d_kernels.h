@@ -48,6 +48,8 @@ struct ScalArgs {
   double* part;  // 3 doubles per block
 };
 
+void set_error(const char* fmt, ...);
+
 long long pt_blocks(const Grid& g);
 // blocks of the z-marching (2.5D) kernels: divergence and correction
 long long z_blocks(const Grid& g);

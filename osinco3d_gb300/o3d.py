@@ -125,6 +125,9 @@ def lib(build_if_missing: bool = True):
             "o3d_statistics_calc": (C.c_int, [vp, C.c_double, _dp]),
             "o3d_rbsor_sweeps_dev": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, _dp]),
             "o3d_time_kernel": (C.c_int, [vp, C.c_int, C.c_int, _dp]),
+            "o3d_divergence_stats_noalloc": (C.c_int, [vp, vp, vp, vp, C.c_int, C.c_int, C.c_int,
+                                                       C.c_double, C.c_double, C.c_double, C.c_int,
+                                                       C.c_int, C.c_int, C.c_int, vp, _dp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -294,6 +297,21 @@ class Context:
         self._check(self.L.o3d_rbsor_sweeps_dev(self.h, C.c_void_p(d_pp), C.c_void_p(d_rhs), omega,
                                                 nsweeps, C.byref(dm)))
         return dm.value
+
+
+def divergence_stats_noalloc(d_fx: int, d_fy: int, d_fz: int, d_div: int | None, shape, spacing, bcs,
+                             odd: int = 1, stream: int | None = None):
+    """o3d_divergence_stats_noalloc on the caller's device buffers (raw device
+    addresses); returns (status, stats[6]).  It allocates nothing."""
+    L = lib()
+    out = (C.c_double * 6)()
+    st = L.o3d_divergence_stats_noalloc(
+        C.c_void_p(d_fx), C.c_void_p(d_fy), C.c_void_p(d_fz), C.c_void_p(d_div or 0),
+        shape[0], shape[1], shape[2], spacing[0], spacing[1], spacing[2], bcs[0], bcs[1], bcs[2], odd,
+        C.c_void_p(stream or 0), out)
+    if st < 0:
+        raise O3DError(st, L.o3d_last_error().decode())
+    return st, np.array(out[:])
 
 
 def tgv_fields(params: Params):
