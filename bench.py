@@ -38,6 +38,10 @@ WORKLOAD = ("Taylor-Green vortex 256^3 periodic [0,2pi)^3 (xlx = 2pi*255/256), R
 # algorithmic bytes per grid point of one launch (float32 storage)
 PRED_BYTES_PER_PT = 15 * 4   # read u,v,w + 6 history, write 3 u* + 3 fluxes
 
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from the
+# ncu capture summarised in profiles/; None until measured
+TRAFFIC_PER_LAUNCH: dict = {}
+
 
 # ---------------------------------------------------------------------------
 # distributed plumbing (replicas only)
@@ -143,11 +147,21 @@ def pinned_field(shape):
     return t.numpy().reshape(shape, order="F")
 
 
-def run_variant(o3d, name: str, steps: int, warmup: int, world: int, **kw) -> dict:
-    import numpy as np
-
+def make_context(o3d, weights=None, **kw):
+    """Context of the 256^3 workload; with the learned guess, the trained
+    network is loaded and attached (owned by the context)."""
     p = o3d.tgv_params(N, eps=EPS, **kw)
     ctx = o3d.Context(p)
+    if kw.get("guess") == o3d.GUESS_LEARNED:
+        from osinco3d_gb300 import learn
+
+        ctx._net_owned = learn.load(weights, ctx.guess_grid())
+        ctx.attach_unet(ctx._net_owned)
+    return p, ctx
+
+
+def run_variant(o3d, name: str, steps: int, warmup: int, world: int, weights=None, **kw) -> dict:
+    p, ctx = make_context(o3d, weights, **kw)
     ux, uy, uz, pp = o3d.tgv_fields(p)
     for nm, f in zip(("ux", "uy", "uz", "pp"), (ux, uy, uz, pp)):
         ctx.upload(nm, f)
@@ -180,20 +194,19 @@ def run_variant(o3d, name: str, steps: int, warmup: int, world: int, **kw) -> di
         "vcycles_per_step": sum(cyc) / steps,
         "poisson_res_inf_last": res[-1],
         "gpu_launches": launches,
-        "omega": ctx.omega,
     }
     return out, ctx, it
 
 
-def measure_e2e(o3d, steps: int, warmup: int, world: int, **kw) -> dict:
+def measure_e2e(o3d, steps: int, warmup: int, world: int, weights=None, **kw) -> dict:
     """Same steps through o3d_step_host: the driver's host arrays (page-locked)
     are copied in before and out after every step."""
-    p = o3d.tgv_params(N, eps=EPS, **kw)
+    p, ctx = make_context(o3d, weights, **kw)
     ux0, uy0, uz0, pp0 = o3d.tgv_fields(p)
     bufs = [pinned_field(ux0.shape) for _ in range(4)]
     for b, f in zip(bufs, (ux0, uy0, uz0, pp0)):
         b[...] = f
-    with o3d.Context(p) as ctx:
+    with ctx:
         it = 0
         for _ in range(warmup):
             it += 1
@@ -210,14 +223,28 @@ def measure_e2e(o3d, steps: int, warmup: int, world: int, **kw) -> dict:
             "ms_per_step": 1e3 * wall / steps}
 
 
-def predictor_roofline(o3d, ctx, peaks: dict) -> dict:
-    """Device time of the fused predictor kernel on the live state, CUDA events
-    on the context's stream, averaged over repeated launches."""
-    t = ctx.time_kernel("predict", 20)
-    achieved = PRED_BYTES_PER_PT * N ** 3 / (t * 1e-3) / 1e9
+# algorithmic bytes per grid point of the hot kernels (float32 storage)
+KERNEL_BYTES = {
+    "predict": (PRED_BYTES_PER_PT, "k_predict25<float>"),
+    "mg_smooth": (8, "k_smooth<float> (one red-black colour pass, finest level)"),  # half-grid e, r in/out
+    "rhs": (16, "k_div25<float>"),
+    "correct": (4 * 6 + 8, "k_correct25<float,double>"),
+}
+
+
+def kernel_roofline(o3d, ctx, peaks: dict) -> dict:
+    """Device time per launch of the hot kernels on the live state (CUDA events
+    on the context's stream, averaged over repeated launches) and their
+    achieved algorithmic bandwidth.  The roofline entry is the finest-level
+    smoother, the kernel with the largest share of the step."""
     peak = peaks.get("hbm_gbs")
-    return {"kernel": "k_predict<float>", "ms": t, "achieved": achieved, "peak": peak,
-            "frac": achieved / peak if peak else None}
+    out = {}
+    for name, (bpp, label) in KERNEL_BYTES.items():
+        t = ctx.time_kernel(name, 20)
+        gbs = bpp * N ** 3 / (t * 1e-3) / 1e9
+        out[name] = {"kernel": label, "ms": t, "bytes_per_point": bpp, "achieved": gbs,
+                     "frac": gbs / peak if peak else None}
+    return out
 
 
 def cpu_baseline_oracle(seconds_budget: float = 20.0, omp: bool = False, sweeps: int = 30) -> dict:
@@ -244,6 +271,10 @@ def cpu_baseline_oracle(seconds_budget: float = 20.0, omp: bool = False, sweeps:
             "seconds": dt}
 
 
+GUESS_DESC = {"mixed_mg_learned": "learned (U-Net correction of the previous pressure)",
+              "mixed_mg": "previous pressure"}
+
+
 def load_peaks() -> dict:
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -254,30 +285,43 @@ def load_peaks() -> dict:
 
 
 def gpu_arm(args, rank, world, local):
-    from osinco3d_gb300 import o3d
+    from osinco3d_gb300 import learn, o3d
 
     o3d.lib()
     peaks = load_peaks()
     variants = {}
+    weights = learn.WEIGHTS if os.path.exists(learn.WEIGHTS) else None
+    mixed = dict(precision=o3d.PREC_MIXED, solver=o3d.SOLVER_MG, kmax=100)
+    if weights:
+        head_name, head_kw = "mixed_mg_learned", dict(mixed, guess=o3d.GUESS_LEARNED)
+    else:
+        head_name, head_kw = "mixed_mg", mixed
     with ClockSampler(local) as clk:
-        head, ctx, _ = run_variant(o3d, "mixed_mg", args.steps, args.warmup, world,
-                                   precision=o3d.PREC_MIXED, solver=o3d.SOLVER_MG, kmax=100)
+        head, ctx, _ = run_variant(o3d, head_name, args.steps, args.warmup, world, weights=weights, **head_kw)
     clocks = clk.summary()
-    roof = predictor_roofline(o3d, ctx, peaks)
+    roof = kernel_roofline(o3d, ctx, peaks)
     ctx.close()
-    variants["mixed_mg"] = head
+    variants[head_name] = head
     if not args.quick:
-        v, c2, _ = run_variant(o3d, "fp64_mg", args.steps, args.warmup, world,
-                               precision=o3d.PREC_FP64, solver=o3d.SOLVER_MG, kmax=100)
-        c2.close()
-        variants["fp64_mg"] = v
+        fp64 = dict(precision=o3d.PREC_FP64, solver=o3d.SOLVER_MG, kmax=100)
+        for name, kw in (("mixed_mg", mixed), ("mixed_mg_extrapolated", dict(mixed, guess=o3d.GUESS_EXTRAPOLATED)),
+                         ("mixed_mg_zero", dict(mixed, guess=o3d.GUESS_ZERO)),
+                         # the plain method: FP64 V(2,2) Gauss-Seidel from the previous pressure
+                         ("fp64_mg", fp64),
+                         # FP64 with the mixed method's smoother settings and extrapolated guess
+                         ("fp64_mg_v21_om1.15_extrapolated",
+                          dict(fp64, mg_post=1, mg_omega=1.15, guess=o3d.GUESS_EXTRAPOLATED))):
+            if name in variants:
+                continue
+            v, cx, _ = run_variant(o3d, name, args.steps, args.warmup, world, **kw)
+            cx.close()
+            variants[name] = v
         sor_steps = max(2, args.steps // 4)
         v, c3, _ = run_variant(o3d, "fp64_rbsor", sor_steps, min(args.warmup, 3), world,
                                precision=o3d.PREC_FP64, solver=o3d.SOLVER_SOR, kmax=20000)
         c3.close()
         variants["fp64_rbsor"] = v
-    e2e = None if args.no_e2e else measure_e2e(o3d, max(3, args.steps // 2), 3, world,
-                                                precision=o3d.PREC_MIXED, solver=o3d.SOLVER_MG, kmax=100)
+    e2e = None if args.no_e2e else measure_e2e(o3d, max(3, args.steps // 2), 3, world, weights=weights, **head_kw)
     line = {
         "metric": METRIC,
         "value": head["mpts_per_s"],
@@ -291,20 +335,23 @@ def gpu_arm(args, rank, world, local):
         "vs_baseline": None,
         "dtype": "fp32 stencils/V-cycles + fp64 defect correction",
         "data": "synthetic (analytic Taylor-Green initial state)",
-        "config": {"workload": WORKLOAD, "grid": [N, N, N], "poisson": "multigrid V(2,2) in FP64 defect correction",
+        "config": {"workload": WORKLOAD, "grid": [N, N, N], "poisson": ("FP32 multigrid V(2,1), red-black smoother omega=1.15, one V-cycle per FP64 residual "
+                               "(defect correction); initial guess: " + GUESS_DESC[head_name]),
                    "parallelism": f"replicas x{world}", "l2": "no flush: every step streams > 1 GB, far above the 129 MB L2"},
         "e2e": e2e,
         "gpu_launches": head["gpu_launches"],
         "clocks": clocks,
         "variants": variants,
     }
-    line["roofline"] = {"bound": "hbm", "achieved": roof["achieved"], "peak": roof["peak"], "unit": "GB/s",
-                        "frac": roof["frac"], "traffic": None, "kernel": roof["kernel"],
-                        "bytes_per_point": PRED_BYTES_PER_PT, "ms": roof["ms"],
-                        "peak_source": peaks.get("source")}
+    top = roof["mg_smooth"]
+    line["roofline"] = {"bound": "hbm", "achieved": top["achieved"], "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                        "frac": top["frac"], "traffic": TRAFFIC_PER_LAUNCH.get("mg_smooth"), "kernel": top["kernel"],
+                        "bytes_per_point": top["bytes_per_point"], "ms": top["ms"],
+                        "peak_source": peaks.get("source"), "others": {k: v for k, v in roof.items() if k != "mg_smooth"}}
     if "fp64_mg" in variants:
         line["speedup_mixed_vs_fp64_mg"] = variants["fp64_mg"]["ms_per_step"] / head["ms_per_step"]
         line["speedup_mixed_vs_fp64_rbsor"] = variants["fp64_rbsor"]["ms_per_step"] / head["ms_per_step"]
+        line["poisson_s_per_step"] = {k: v["poisson_s_per_step"] for k, v in variants.items()}
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_oracle()
     return line

@@ -65,7 +65,8 @@ enum {
 enum {
   O3D_GUESS_PREVIOUS = 0, /* previous step's pressure (the reference: pp persists) */
   O3D_GUESS_ZERO = 1,
-  O3D_GUESS_LEARNED = 2   /* 3D U-Net prediction from (div u*, previous p) */
+  O3D_GUESS_LEARNED = 2,  /* 3D U-Net prediction from (div u*, previous p) */
+  O3D_GUESS_EXTRAPOLATED = 3 /* 2 p(n) - p(n-1): linear extrapolation in time */
 };
 
 /* field identifiers for o3d_upload / o3d_download */
@@ -106,9 +107,12 @@ typedef struct o3d_params {
   int precision;          /* O3D_PREC_* */
   int solver;             /* O3D_SOLVER_* */
   int mg_levels;          /* 0 = as many as the grid allows */
-  int mg_pre, mg_post;    /* smoothing sweeps; 0 -> 2 */
+  int mg_pre, mg_post;    /* smoothing sweeps; 0 -> V(2,2) in FP64, V(2,1) mixed */
   int guess;              /* O3D_GUESS_* */
   int diagnostics;        /* 1: per-step div/CFL/min-max reductions as the driver prints them */
+  int mg_cycles;          /* V-cycles per FP64 residual; 0 -> 1 */
+  double mg_omega;        /* relaxation of the red-black smoother; 0 -> 1 (Gauss-Seidel)
+                             in FP64, 1.15 mixed */
 } o3d_params;
 
 /* Fills *p with the defaults of the reference's namelists (periodic 64^3). */
@@ -193,6 +197,43 @@ O3D_API int o3d_step_host(o3d_ctx *ctx, int itime, double *ux, double *uy, doubl
 /* statistics_calc(...), src/utils.f90:243-375: out[17] = t, E_k, eps, eps2,
  * dzeta, <u^2>, <v^2>, <w^2>, nine <(du_i/dx_j)^2>, FP64 reductions. */
 O3D_API int o3d_statistics_calc(o3d_ctx *ctx, double t, double out[17]);
+
+/* ---- learned Poisson warm start ------------------------------------------
+ * A 3D U-Net (BF16 tensor-core convolutions, FP32 accumulation) predicts the
+ * pressure increment of the next solve from the residual of the previous
+ * pressure, r = rhs - A p(n), and the last increment p(n) - p(n-1), both on
+ * the grid two multigrid coarsenings below the pressure grid and scaled by
+ * S = rms of that increment.  The guess is p(n) + S * prolong(prolong(y));
+ * the solver then iterates to eps as usual.  No counterpart in the
+ * reference. */
+typedef struct o3d_unet o3d_unet;
+/* nx, ny, nz: the network grid (that of o3d_guess_grid); periodic[a] = 1
+ * wraps axis a in the convolutions; base_channels (16) doubles per level. */
+O3D_API int o3d_unet_create(int nx, int ny, int nz, const int periodic[3], int base_channels, int levels,
+                            int in_channels, unsigned long long seed, o3d_unet **out);
+O3D_API int o3d_unet_destroy(o3d_unet *net);
+O3D_API long long o3d_unet_num_params(const o3d_unet *net);
+/* FP32 master parameters (host buffers of o3d_unet_num_params floats) */
+O3D_API int o3d_unet_get_params(o3d_unet *net, float *host);
+O3D_API int o3d_unet_set_params(o3d_unet *net, const float *host);
+/* d_in: in_channels x nvox FP32 device buffer (channel-major, x fastest);
+ * d_out: nvox FP32; `wait` is a cudaStream_t ordered before and after. */
+O3D_API int o3d_unet_forward_dev(o3d_unet *net, const float *d_in, float *d_out, void *wait);
+/* MSE loss and parameter gradients of one sample (host_grad may be NULL) */
+O3D_API int o3d_unet_gradients(o3d_unet *net, const float *d_in, const float *d_target, float *loss,
+                               float *host_grad);
+/* one Adam step (beta 0.9 / 0.999) on one sample */
+O3D_API int o3d_unet_train_step(o3d_unet *net, const float *d_in, const float *d_target, float lr, float *loss);
+/* the grid of the guess features for this context (dims[3]) */
+O3D_API int o3d_guess_grid(o3d_ctx *ctx, int dims[3]);
+/* use `net` for O3D_GUESS_LEARNED (NULL detaches); the caller keeps ownership */
+O3D_API int o3d_attach_unet(o3d_ctx *ctx, o3d_unet *net);
+/* Training data: with device buffers set (features 2 x n, target n on the
+ * guess grid), every solve that has a previous pressure writes its features
+ * before and its target, restrict(restrict(p(n+1) - p(n))) / S, after. */
+O3D_API int o3d_set_sample_buffers(o3d_ctx *ctx, float *d_feat, float *d_tgt);
+/* 1 when the last solve wrote a sample */
+O3D_API int o3d_sample_ready(const o3d_ctx *ctx);
 
 /* Device time of one launch of a hot kernel on the live state, averaged over
  * `reps` back-to-back launches timed with CUDA events on the context's stream.

@@ -87,11 +87,7 @@ __global__ void k_sor_control(SolveCtrl* c) {
 
 static dim3 rb_grid(const Grid& g) { return dim3((unsigned)((g.nx + 1) / 2 + 31) / 32, (g.ny + 7) / 8, g.nz); }
 
-void launch_sor_sweep_ctrl(double* p, const double* rhs, const Grid& g, const PoiCoef<double>& c,
-                           SolveCtrl* ctrl, cudaStream_t s) {
-  k_sor_rb<<<rb_grid(g), dim3(32, 8), 0, s>>>(p, rhs, g, c, 0, ctrl, 0.0, 1);
-  k_sor_rb<<<rb_grid(g), dim3(32, 8), 0, s>>>(p, rhs, g, c, 1, ctrl, 0.0, 1);
-}
+
 void launch_sor_control(SolveCtrl* ctrl, cudaStream_t s) { k_sor_control<<<1, 1, 0, s>>>(ctrl); }
 void launch_sor_fixed(double* p, const double* rhs, const Grid& g, const PoiCoef<double>& c,
                       double omega, SolveCtrl* ctrl, cudaStream_t s) {
@@ -238,6 +234,27 @@ __global__ void __launch_bounds__(256) k_smooth_zero(T* __restrict__ e, const T*
   e[q] = ((i + j + k) & 1) == 0 ? om * (r[q] * c.invA) : (T)0;
 }
 
+// first sweep from e = 0 in one pass: red points get omega*r/A, black points
+// the relaxed Gauss-Seidel value from those red neighbours,
+// omega*(r - omega*lap_nb(r)/A)/A (lap_nb: the off-diagonal part of A)
+template <class T>
+__global__ void __launch_bounds__(256) k_smooth_first(T* __restrict__ e, const T* __restrict__ r, Grid g,
+                                                      PoiCoef<T> c, T om, const SolveCtrl* ctrl) {
+  if (ctrl->done) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= g.nx || j >= g.ny) return;
+  const long long q = (long long)i + g.sy() * j + g.sz() * k;
+  const T rq = __ldg(r + q);
+  if (((i + j + k) & 1) == 0) {
+    e[q] = om * (rq * c.invA);
+  } else {
+    const T sr = lap_nb<T>(r, g, i, j, k, c);
+    e[q] = om * ((rq - om * (sr * c.invA)) * c.invA);
+  }
+}
+
 template <class T>
 __global__ void __launch_bounds__(256) k_smooth(T* __restrict__ e, const T* __restrict__ r, Grid g,
                                                 PoiCoef<T> c, int color, T om, const SolveCtrl* ctrl) {
@@ -253,6 +270,23 @@ __global__ void __launch_bounds__(256) k_smooth(T* __restrict__ e, const T* __re
   const T ec = e[q];
   const T en = (r[q] - s) * c.invA;
   e[q] = ec + om * (en - ec);
+}
+
+void launch_sor_sweep_ctrl(double* p, const double* rhs, const Grid& g, const PoiCoef<double>& c,
+                           SolveCtrl* ctrl, cudaStream_t s) {
+  k_sor_rb<<<rb_grid(g), dim3(32, 8), 0, s>>>(p, rhs, g, c, 0, ctrl, 0.0, 1);
+  k_sor_rb<<<rb_grid(g), dim3(32, 8), 0, s>>>(p, rhs, g, c, 1, ctrl, 0.0, 1);
+}
+
+// `n` red-black sweeps of A e = r with relaxation om, in place on e
+template <class T>
+static void smooth_sweeps(const MGLevel& L, T* e, const T* r, const PoiCoef<T>& c, T om, int n,
+                          const SolveCtrl* ctrl, cudaStream_t s, long long* nl) {
+  for (int q = 0; q < n; ++q)
+    for (int color = 0; color < 2; ++color)
+      k_smooth<T><<<dim3((unsigned)(((L.g.nx + 1) / 2 + 31) / 32), (L.g.ny + 7) / 8, L.g.nz), dim3(32, 8), 0, s>>>(
+          e, r, L.g, c, color, om, ctrl);
+  *nl += 2 * n;
 }
 
 template <class T>
@@ -339,6 +373,45 @@ __global__ void __launch_bounds__(256) k_prolong(T* __restrict__ ef, const T* __
   ef[(long long)i + gf.sy() * j + gf.sz() * k] += v;
 }
 
+// Prolongation + add with one thread per coarse cell (I, J, K): its 8 coarse
+// corners are read once and the 2 x 2 x 2 fine points (2I+a, 2J+b, 2K+c)
+// are updated; used when all three axes are coarsened.
+__device__ __forceinline__ int prol_hi(int I, int nc, int bc) {
+  return I + 1 < nc ? I + 1 : (bc == AX_PERIODIC ? 0 : nc - 1);
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_prolong_cell(T* __restrict__ ef, const T* __restrict__ ec, Grid gf,
+                                                      Grid gc, const SolveCtrl* ctrl) {
+  if (ctrl->done) return;
+  const int I = blockIdx.x * blockDim.x + threadIdx.x;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y;
+  const int K = blockIdx.z;
+  if (I >= gc.nx || J >= gc.ny) return;
+  const int I1 = prol_hi(I, gc.nx, gf.bc[0]), J1 = prol_hi(J, gc.ny, gf.bc[1]), K1 = prol_hi(K, gc.nz, gf.bc[2]);
+  auto at = [&](int a, int b, int c) { return __ldg(ec + (long long)a + gc.sy() * b + gc.sz() * c); };
+  const T c000 = at(I, J, K), c100 = at(I1, J, K), c010 = at(I, J1, K), c110 = at(I1, J1, K);
+  const T c001 = at(I, J, K1), c101 = at(I1, J, K1), c011 = at(I, J1, K1), c111 = at(I1, J1, K1);
+  const T h = (T)0.5;
+  // values on the 2 x 2 x 2 fine points, x fastest
+  const T x00 = h * (c000 + c100), x10 = h * (c010 + c110), x01 = h * (c001 + c101), x11 = h * (c011 + c111);
+  const T v[2][2][2] = {{{c000, x00}, {h * (c000 + c010), h * (x00 + x10)}},
+                        {{h * (c000 + c001), h * (x00 + x01)},
+                         {h * (h * (c000 + c010) + h * (c001 + c011)), h * (h * (x00 + x10) + h * (x01 + x11))}}};
+  for (int dc = 0; dc < 2; ++dc) {
+    const int kf = 2 * K + dc;
+    if (kf >= gf.nz) break;
+    for (int db = 0; db < 2; ++db) {
+      const int jf = 2 * J + db;
+      if (jf >= gf.ny) break;
+      const long long row = gf.sy() * jf + gf.sz() * kf;
+      const int i0f = 2 * I;
+      ef[row + i0f] += v[dc][db][0];
+      if (i0f + 1 < gf.nx) ef[row + i0f + 1] += v[dc][db][1];
+    }
+  }
+}
+
 // Coarsest level: one block, shared memory, weighted mean of r removed,
 // `sweeps` red-black Gauss-Seidel sweeps from e = 0.
 template <class T>
@@ -419,7 +492,7 @@ __global__ void k_mg_control(SolveCtrl* c) {
   const double dmax = __longlong_as_double((long long)c->dmax_key);
   c->dmax_key = 0ull;
   c->iter += 1;
-  c->cycles += 1;
+  c->cycles += c->cycles_per_iter;
   c->dmax = dmax;
   // max |r| of this iteration's residual (before its correction was added)
   c->res_inf = __longlong_as_double((long long)c->res_key);
@@ -433,9 +506,11 @@ __global__ void k_mg_control(SolveCtrl* c) {
 static inline dim3 g3(const Grid& g) { return dim3((g.nx + 31) / 32, (g.ny + 7) / 8, g.nz); }
 static inline dim3 g3rb(const Grid& g) { return dim3((unsigned)(((g.nx + 1) / 2 + 31) / 32), (g.ny + 7) / 8, g.nz); }
 
+// One V-cycle on level l for A e = r, from e = 0 (zero_init: the first
+// sweep in one pass from r) or from the current e.
 template <class T>
-static void vcycle(MGLevel* lv, int l, int nlev, int pre, int post, int coarse_sweeps, T om,
-                   SolveCtrl* ctrl, cudaStream_t s, long long* nl) {
+static void vcycle(MGLevel* lv, int l, int nlev, int pre, int post, int coarse_sweeps, T om, SolveCtrl* ctrl,
+                   cudaStream_t s, long long* nl, bool zero_init) {
   const MGLevel& L = lv[l];
   T* e = (T*)L.e;
   T* r = (T*)L.r;
@@ -446,46 +521,203 @@ static void vcycle(MGLevel* lv, int l, int nlev, int pre, int post, int coarse_s
       k_coarse<T><<<1, 1024, 0, s>>>(e, r, L.g, c, coarse_sweeps, ctrl);
       *nl += 1;
     } else {
-      k_smooth_zero<T><<<g3(L.g), b, 0, s>>>(e, r, L.g, c, (T)1, ctrl);
-      k_smooth<T><<<g3rb(L.g), b, 0, s>>>(e, r, L.g, c, 1, (T)1, ctrl);
-      for (int q = 1; q < coarse_sweeps; ++q)
-        for (int color = 0; color < 2; ++color) k_smooth<T><<<g3rb(L.g), b, 0, s>>>(e, r, L.g, c, color, (T)1, ctrl);
-      *nl += 2 * coarse_sweeps;
+      k_smooth_first<T><<<g3(L.g), b, 0, s>>>(e, r, L.g, c, (T)1, ctrl);
+      *nl += 1;
+      smooth_sweeps<T>(L, e, r, c, (T)1, coarse_sweeps - 1, ctrl, s, nl);
     }
     return;
   }
-  k_smooth_zero<T><<<g3(L.g), b, 0, s>>>(e, r, L.g, c, om, ctrl);
-  k_smooth<T><<<g3rb(L.g), b, 0, s>>>(e, r, L.g, c, 1, om, ctrl);
-  for (int q = 1; q < pre; ++q)
-    for (int color = 0; color < 2; ++color) k_smooth<T><<<g3rb(L.g), b, 0, s>>>(e, r, L.g, c, color, om, ctrl);
+  int sweeps = pre;
+  if (zero_init) {
+    k_smooth_first<T><<<g3(L.g), b, 0, s>>>(e, r, L.g, c, om, ctrl);
+    *nl += 1;
+    sweeps -= 1;
+  }
+  smooth_sweeps<T>(L, e, r, c, om, sweeps, ctrl, s, nl);
   k_resid<T><<<g3(L.g), b, 0, s>>>(e, r, (T*)L.t, L.g, c, ctrl);
   const MGLevel& C = lv[l + 1];
   Coarsen cz;
   for (int a = 0; a < 3; ++a) cz.c[a] = L.coarsen[a];
   k_restrict<T><<<g3(C.g), b, 0, s>>>((const T*)L.t, (T*)C.r, L.g, C.g, cz, ctrl);
-  *nl += 2 + 2 * pre + 1;
-  vcycle<T>(lv, l + 1, nlev, pre, post, coarse_sweeps, om, ctrl, s, nl);
-  k_prolong<T><<<g3(L.g), b, 0, s>>>(e, (const T*)C.e, L.g, C.g, cz, ctrl);
-  for (int q = 0; q < post; ++q)
-    for (int color = 0; color < 2; ++color) k_smooth<T><<<g3rb(L.g), b, 0, s>>>(e, r, L.g, c, color, om, ctrl);
-  *nl += 1 + 2 * post;
+  *nl += 2;
+  vcycle<T>(lv, l + 1, nlev, pre, post, coarse_sweeps, om, ctrl, s, nl, true);
+  if (cz.c[0] && cz.c[1] && cz.c[2])
+    k_prolong_cell<T><<<g3(C.g), b, 0, s>>>(e, (const T*)C.e, L.g, C.g, ctrl);
+  else
+    k_prolong<T><<<g3(L.g), b, 0, s>>>(e, (const T*)C.e, L.g, C.g, cz, ctrl);
+  *nl += 1;
+  smooth_sweeps<T>(L, e, r, c, om, post, ctrl, s, nl);
 }
 
+// One outer iteration of the defect-correction loop: FP64 residual, `cycles`
+// V-cycles in T on A e = r (the first from e = 0, the next ones from the
+// current e), p += e in FP64, stop test.
 template <class T, class R>
 void launch_mg_outer(double* p, const R* rhs, MGLevel* lv, int nlev, int pre, int post,
-                     int coarse_sweeps, T smooth_omega, SolveCtrl* ctrl, double* wpart,
-                     cudaStream_t s, long long* nl) {
-  (void)wpart;
+                     int coarse_sweeps, T smooth_omega, int cycles, SolveCtrl* ctrl, cudaStream_t s,
+                     long long* nl) {
   const MGLevel& L0 = lv[0];
   PoiCoef<double> c64 = make_poi<double>(L0.h[0], L0.h[1], L0.h[2]);
   k_resid_top_max<T, R><<<g3(L0.g), dim3(32, 8), 0, s>>>(p, rhs, (T*)L0.r, L0.g, c64, ctrl);
   *nl += 1;
-  vcycle<T>(lv, 0, nlev, pre, post, coarse_sweeps, smooth_omega, ctrl, s, nl);
+  for (int q = 0; q < cycles; ++q) vcycle<T>(lv, 0, nlev, pre, post, coarse_sweeps, smooth_omega, ctrl, s, nl, q == 0);
   k_update<T><<<(unsigned)((L0.g.n + 256LL * UPD_PER - 1) / (256LL * UPD_PER)), 256, 0, s>>>(p, (const T*)L0.e,
                                                                                          L0.g.n, ctrl);
   k_mg_control<<<1, 1, 0, s>>>(ctrl);
   *nl += 2;
 }
+
+// p <- 2 p - p_prev, p_prev <- p (linear extrapolation of the pressure in time)
+__global__ void k_extrapolate(double* __restrict__ p, double* __restrict__ pprev, long long n) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const double pc = p[q];
+  p[q] = 2.0 * pc - pprev[q];
+  pprev[q] = pc;
+}
+void launch_extrapolate(double* p, double* pprev, long long n, cudaStream_t s) {
+  k_extrapolate<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p, pprev, n);
+}
+
+// ---------------------------------------------------------------------------
+// learned warm start plumbing: features and targets at the network grid
+// (the multigrid level two coarsenings below the pressure grid)
+// ---------------------------------------------------------------------------
+// d = p - pprev in T
+template <class T>
+__global__ void k_pdiff(const double* __restrict__ p, const double* __restrict__ pprev, T* __restrict__ d, long long n) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) d[q] = (T)(p[q] - pprev[q]);
+}
+
+// learn_scale = sqrt(mean(d^2)) over the coarse grid (one block)
+template <class T>
+__global__ void k_rms(const T* __restrict__ d, long long n, SolveCtrl* ctrl) {
+  __shared__ double sh[1024];
+  double a = 0.0;
+  for (long long q = threadIdx.x; q < n; q += blockDim.x) {
+    const double v = (double)d[q];
+    a += v * v;
+  }
+  sh[threadIdx.x] = a;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if ((int)threadIdx.x < st) sh[threadIdx.x] += sh[threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) ctrl->learn_scale = sqrt(sh[0] / (double)n) + 1e-30;
+}
+
+// network input: channel 0 = r * h^2 / S, channel 1 = d / S (FP32, channel-major)
+template <class T>
+__global__ void k_features(const T* __restrict__ r, const T* __restrict__ d, long long n, double h2,
+                           const SolveCtrl* ctrl, float* __restrict__ feat) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const double inv = 1.0 / ctrl->learn_scale;
+  feat[q] = (float)((double)r[q] * h2 * inv);
+  feat[n + q] = (float)((double)d[q] * inv);
+}
+
+// coarse correction e = S * y
+template <class T>
+__global__ void k_unscale(const float* __restrict__ y, long long n, const SolveCtrl* ctrl, T* __restrict__ e) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) e[q] = (T)((double)y[q] * ctrl->learn_scale);
+}
+
+// training target t = d / S (FP32)
+template <class T>
+__global__ void k_target(const T* __restrict__ d, long long n, const SolveCtrl* ctrl, float* __restrict__ t) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) t[q] = (float)((double)d[q] / ctrl->learn_scale);
+}
+
+// p += e
+template <class T>
+__global__ void k_padd(double* __restrict__ p, const T* __restrict__ e, long long n) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) p[q] += (double)e[q];
+}
+
+static inline unsigned b256(long long n) { return (unsigned)((n + 255) / 256); }
+
+// Restricts a level-0 field down to level ll through the levels' scratch
+// arrays `which` (0: e, 1: t); returns the level-ll array.
+template <class T>
+static T* restrict_to(MGLevel* lv, int ll, const T* f0, int which, SolveCtrl* ctrl, cudaStream_t s, long long* nl) {
+  const T* src = f0;
+  T* dst = nullptr;
+  for (int l = 0; l < ll; ++l) {
+    Coarsen cz;
+    for (int a = 0; a < 3; ++a) cz.c[a] = lv[l].coarsen[a];
+    dst = (T*)(which ? lv[l + 1].t : lv[l + 1].e);
+    k_restrict<T><<<g3(lv[l + 1].g), dim3(32, 8), 0, s>>>(src, dst, lv[l].g, lv[l + 1].g, cz, ctrl);
+    src = dst;
+    *nl += 1;
+  }
+  return dst;
+}
+
+// Features of the learned guess from the current pressure p (= p^n), the
+// previous pressure pprev and the rhs: r = rhs - mean - A p and d = p - pprev,
+// both restricted to level ll; S = rms(d).  Writes feat (2 x n_ll FP32).
+// Uses the scratch arrays of levels 0..ll; ctrl->done must be 0.
+template <class T, class R>
+void launch_learn_features(double* p, const double* pprev, const R* rhs, MGLevel* lv, int ll, SolveCtrl* ctrl,
+                           float* feat, cudaStream_t s, long long* nl) {
+  const MGLevel& L0 = lv[0];
+  PoiCoef<double> c64 = make_poi<double>(L0.h[0], L0.h[1], L0.h[2]);
+  k_resid_top<T, R><<<g3(L0.g), dim3(32, 8), 0, s>>>(p, rhs, (T*)L0.r, L0.g, c64, ctrl);
+  k_pdiff<T><<<b256(L0.g.n), 256, 0, s>>>(p, pprev, (T*)L0.t, L0.g.n);
+  const T* rc = restrict_to<T>(lv, ll, (const T*)L0.r, 0, ctrl, s, nl);
+  const T* dc = restrict_to<T>(lv, ll, (const T*)L0.t, 1, ctrl, s, nl);
+  const long long n2 = lv[ll].g.n;
+  k_rms<T><<<1, 1024, 0, s>>>(dc, n2, ctrl);
+  const double h2 = lv[ll].h[0] * lv[ll].h[0];
+  k_features<T><<<b256(n2), 256, 0, s>>>(rc, dc, n2, h2, ctrl, feat);
+  *nl += 4;
+}
+
+// p += prolong^ll(S * y) with y the network output on level ll.
+template <class T>
+void launch_learn_apply(double* p, const float* y, MGLevel* lv, int ll, SolveCtrl* ctrl, cudaStream_t s,
+                        long long* nl) {
+  const long long n2 = lv[ll].g.n;
+  k_unscale<T><<<b256(n2), 256, 0, s>>>(y, n2, ctrl, (T*)lv[ll].e);
+  for (int l = ll - 1; l >= 0; --l) {
+    cudaMemsetAsync(lv[l].e, 0, (size_t)lv[l].g.n * sizeof(T), s);
+    Coarsen cz;
+    for (int a = 0; a < 3; ++a) cz.c[a] = lv[l].coarsen[a];
+    k_prolong<T><<<g3(lv[l].g), dim3(32, 8), 0, s>>>((T*)lv[l].e, (const T*)lv[l + 1].e, lv[l].g, lv[l + 1].g, cz,
+                                                     ctrl);
+    *nl += 1;
+  }
+  k_padd<T><<<b256(lv[0].g.n), 256, 0, s>>>(p, (const T*)lv[0].e, lv[0].g.n);
+  *nl += 2;
+}
+
+// Training target of the last solve: restrict^ll(p - pprev) / S into tgt (FP32).
+template <class T>
+void launch_learn_target(const double* p, const double* pprev, MGLevel* lv, int ll, SolveCtrl* ctrl, float* tgt,
+                         cudaStream_t s, long long* nl) {
+  const MGLevel& L0 = lv[0];
+  k_pdiff<T><<<b256(L0.g.n), 256, 0, s>>>(p, pprev, (T*)L0.t, L0.g.n);
+  const T* dc = restrict_to<T>(lv, ll, (const T*)L0.t, 1, ctrl, s, nl);
+  k_target<T><<<b256(lv[ll].g.n), 256, 0, s>>>(dc, lv[ll].g.n, ctrl, tgt);
+  *nl += 2;
+}
+
+template void launch_learn_features<float, float>(double*, const double*, const float*, MGLevel*, int, SolveCtrl*,
+                                                  float*, cudaStream_t, long long*);
+template void launch_learn_features<double, double>(double*, const double*, const double*, MGLevel*, int, SolveCtrl*,
+                                                    float*, cudaStream_t, long long*);
+template void launch_learn_apply<float>(double*, const float*, MGLevel*, int, SolveCtrl*, cudaStream_t, long long*);
+template void launch_learn_apply<double>(double*, const float*, MGLevel*, int, SolveCtrl*, cudaStream_t, long long*);
+template void launch_learn_target<float>(const double*, const double*, MGLevel*, int, SolveCtrl*, float*, cudaStream_t,
+                                         long long*);
+template void launch_learn_target<double>(const double*, const double*, MGLevel*, int, SolveCtrl*, float*,
+                                          cudaStream_t, long long*);
 
 template <class R>
 void launch_rhs_wmean(const R* rhs, const Grid& g, double* part, SolveCtrl* ctrl, cudaStream_t s,
@@ -522,9 +754,9 @@ template void launch_level_kernel<double, double>(int, double*, const double*, c
                                                   cudaStream_t);
 
 template void launch_mg_outer<double, double>(double*, const double*, MGLevel*, int, int, int, int,
-                                              double, SolveCtrl*, double*, cudaStream_t, long long*);
+                                              double, int, SolveCtrl*, cudaStream_t, long long*);
 template void launch_mg_outer<float, float>(double*, const float*, MGLevel*, int, int, int, int,
-                                            float, SolveCtrl*, double*, cudaStream_t, long long*);
+                                            float, int, SolveCtrl*, cudaStream_t, long long*);
 template void launch_rhs_wmean<double>(const double*, const Grid&, double*, SolveCtrl*, cudaStream_t, long long*);
 template void launch_rhs_wmean<float>(const float*, const Grid&, double*, SolveCtrl*, cudaStream_t, long long*);
 template void launch_residual_inf<double>(const double*, const double*, const Grid&, const PoiCoef<double>&,

@@ -87,6 +87,15 @@ struct o3d_ctx {
   void* fphi[3];
   void* rhs;
   double* pp;
+  double* pp_prev;   // previous step's pressure (extrapolated and learned guesses, lazy)
+  int pp_prev_valid;
+  o3d_unet* unet;    // network of the learned guess (not owned)
+  float* feat;       // its input on the network grid (2 channels)
+  float* ynet;       // its output
+  float* sample_feat;  // caller's buffers for training samples (features, target)
+  float* sample_tgt;
+  int sample_ready;
+  int learn_level;     // multigrid level of the network grid
   double* stage[4];  // FP64 staging buffers for host transfers (lazy)
 
   double* part;      // per-block reduction records
@@ -366,6 +375,11 @@ int build_mg(o3d_ctx* c) {
   return O3D_OK;
 }
 
+int mg_cycles_of(const o3d_ctx* c) {
+  if (c->P.solver != O3D_SOLVER_MG) return 0;
+  return c->P.mg_cycles > 0 ? c->P.mg_cycles : 1;
+}
+
 int reset_ctrl(o3d_ctx* c, double omega, double eps, int kmax, int idyn) {
   SolveCtrl* h = c->ctrl_h;
   memset(h, 0, sizeof *h);
@@ -377,6 +391,7 @@ int reset_ctrl(o3d_ctx* c, double omega, double eps, int kmax, int idyn) {
   h->factor = (c->gp.bc[0] == AX_PERIODIC && c->gp.bc[1] == AX_MIRROR) ? 1.01 : 1.05;
   h->kmax = kmax;
   h->idyn = idyn;
+  h->cycles_per_iter = mg_cycles_of(c);
   CK(cudaMemcpyAsync(c->ctrl, h, sizeof *h, cudaMemcpyHostToDevice, c->s));
   return O3D_OK;
 }
@@ -405,9 +420,16 @@ int capture_sor(o3d_ctx* c) {
 }
 
 int mg_smooth_cfg(const o3d_ctx* c, int* pre, int* post) {
+  // the plain FP64 method is the V(2,2) Gauss-Seidel cycle; the mixed one
+  // defaults to V(2,1) over-relaxed (fewer FP32 sweeps per FP64 residual)
   *pre = c->P.mg_pre > 0 ? c->P.mg_pre : 2;
-  *post = c->P.mg_post > 0 ? c->P.mg_post : 2;
+  *post = c->P.mg_post > 0 ? c->P.mg_post : (c->mixed ? 1 : 2);
   return 0;
+}
+
+double mg_omega_of(const o3d_ctx* c) {
+  if (c->P.mg_omega > 0.0) return c->P.mg_omega;
+  return c->mixed ? 1.15 : 1.0;
 }
 
 int capture_mg(o3d_ctx* c) {
@@ -424,12 +446,14 @@ int capture_mg(o3d_ctx* c) {
   cudaGraph_t graph;
   CK(cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal));
   for (int q = 0; q < c->mg_batch; ++q) {
+    const int cyc = mg_cycles_of(c);
+    const double om = mg_omega_of(c);
     if (c->mixed)
       launch_mg_outer<float, float>(c->pp, (const float*)c->rhs, c->mg.data(), (int)c->mg.size(), pre,
-                                    post, coarse_sweeps, 1.0f, c->ctrl, c->part, c->s, &nl);
+                                    post, coarse_sweeps, (float)om, cyc, c->ctrl, c->s, &nl);
     else
       launch_mg_outer<double, double>(c->pp, (const double*)c->rhs, c->mg.data(), (int)c->mg.size(),
-                                      pre, post, coarse_sweeps, 1.0, c->ctrl, c->part, c->s, &nl);
+                                      pre, post, coarse_sweeps, om, cyc, c->ctrl, c->s, &nl);
   }
   CK(cudaStreamEndCapture(c->s, &graph));
   CK(cudaGraphInstantiate(&c->mg_exec, graph, 0));
@@ -438,22 +462,109 @@ int capture_mg(o3d_ctx* c) {
   return O3D_OK;
 }
 
+// Sets up the learned-guess machinery: multigrid scratch levels, the level
+// the network works on, and its buffers.  The level is the deepest one
+// reached by coarsening every axis each time, with at most three
+// coarsenings and at least 16 points on every axis (256^3 -> 32^3,
+// 128^3 -> 16^3, 32^3 -> 16^3).
+int learn_ready(o3d_ctx* c) {
+  if (!c->mg_ok) {
+    int st = build_mg(c);
+    if (st) return st;
+  }
+  int ll = 0;
+  while (ll < 3 && ll + 1 < (int)c->mg.size()) {
+    const MGLevel& L = c->mg[ll];
+    if (!(L.coarsen[0] && L.coarsen[1] && L.coarsen[2])) break;
+    const Grid& g = c->mg[ll + 1].g;
+    if (g.nx < 16 || g.ny < 16 || g.nz < 16) break;
+    ++ll;
+  }
+  if (ll < 1) {
+    errf("the learned warm start needs a grid that coarsens at least once on every axis to 16+ points");
+    return O3D_ERR_BADARG;
+  }
+  c->learn_level = ll;
+  const long long n2 = c->mg[ll].g.n;
+  if (!c->feat) {
+    int st = dalloc(c->s, (void**)&c->feat, (size_t)n2 * 2 * sizeof(float));
+    if (!st) st = dalloc(c->s, (void**)&c->ynet, (size_t)n2 * sizeof(float));
+    if (st) return st;
+  }
+  return O3D_OK;
+}
+
 // Solves A pp = rhs with the context's solver; pp holds the initial guess.
 int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step_info* info) {
-  if (c->P.guess == O3D_GUESS_ZERO) CK(cudaMemsetAsync(c->pp, 0, (size_t)c->g.n * 8, c->s));
-  if (c->P.guess == O3D_GUESS_LEARNED) {
-    snprintf(g_err, sizeof g_err, "learned initial guess is not available in this build");
+  const int guess = c->P.guess;
+  const bool learned = guess == O3D_GUESS_LEARNED;
+  const bool sampling = c->sample_feat != nullptr;
+  const bool need_hist = guess == O3D_GUESS_EXTRAPOLATED || learned || sampling;
+  if (learned && !c->unet) {
+    errf("the learned initial guess needs a network (o3d_attach_unet)");
     return O3D_ERR_NOT_BUILT;
   }
+  if (need_hist && !c->pp_prev) {
+    int st0 = dalloc(c->s, (void**)&c->pp_prev, (size_t)c->g.n * 8);
+    if (st0) return st0;
+  }
+  if ((learned || sampling)) {
+    int st0 = learn_ready(c);
+    if (st0) return st0;
+  }
+  if (guess == O3D_GUESS_ZERO) CK(cudaMemsetAsync(c->pp, 0, (size_t)c->g.n * 8, c->s));
   int st = reset_ctrl(c, *omega_io, eps, kmax, idyn);
   if (st) return st;
   CK(cudaEventRecord(c->ev[2], c->s));
   const bool use_mg = c->P.solver == O3D_SOLVER_MG;
-  if (use_mg) {
-    if ((st = capture_mg(c))) return st;
+  if (use_mg || learned || sampling) {
     if (c->mixed) launch_rhs_wmean<float>((const float*)c->rhs, c->gp, c->part, c->ctrl, c->s, &c->launches);
     else launch_rhs_wmean<double>((const double*)c->rhs, c->gp, c->part, c->ctrl, c->s, &c->launches);
     CKL();
+  }
+  c->sample_ready = 0;
+  if (need_hist) {
+    if (c->pp_prev_valid && (learned || sampling)) {
+      // features from p(n), p(n-1) and the rhs; then p(n-1) <- p(n)
+      if (c->mixed)
+        launch_learn_features<float, float>(c->pp, c->pp_prev, (const float*)c->rhs, c->mg.data(), c->learn_level,
+                                            c->ctrl, c->feat, c->s, &c->launches);
+      else
+        launch_learn_features<double, double>(c->pp, c->pp_prev, (const double*)c->rhs, c->mg.data(),
+                                              c->learn_level, c->ctrl, c->feat, c->s, &c->launches);
+      CKL();
+      if (guess == O3D_GUESS_EXTRAPOLATED) {
+        launch_extrapolate(c->pp, c->pp_prev, c->g.n, c->s);  // also sets p(n-1) <- p(n)
+        c->launches++;
+        CKL();
+      } else {
+        CK(cudaMemcpyAsync(c->pp_prev, c->pp, (size_t)c->g.n * 8, cudaMemcpyDeviceToDevice, c->s));
+      }
+      if (sampling) {
+        CK(cudaMemcpyAsync(c->sample_feat, c->feat, (size_t)c->mg[c->learn_level].g.n * 2 * sizeof(float),
+                           cudaMemcpyDeviceToDevice, c->s));
+        c->sample_ready = 1;
+      }
+      if (learned) {
+        if ((st = unet_forward(c->unet, c->feat, c->ynet, c->s))) return st;
+        if (c->mixed)
+          launch_learn_apply<float>(c->pp, c->ynet, c->mg.data(), c->learn_level, c->ctrl, c->s, &c->launches);
+        else
+          launch_learn_apply<double>(c->pp, c->ynet, c->mg.data(), c->learn_level, c->ctrl, c->s, &c->launches);
+        CKL();
+      }
+    } else if (c->pp_prev_valid && guess == O3D_GUESS_EXTRAPOLATED) {
+      launch_extrapolate(c->pp, c->pp_prev, c->g.n, c->s);
+      c->launches++;
+      CKL();
+    } else {
+      // first solve: no history yet, start from the previous pressure
+      CK(cudaMemcpyAsync(c->pp_prev, c->pp, (size_t)c->g.n * 8, cudaMemcpyDeviceToDevice, c->s));
+      c->pp_prev_valid = 1;
+    }
+  }
+  if (use_mg) {
+    if ((st = capture_mg(c))) return st;
   } else {
     if ((st = capture_sor(c))) return st;
   }
@@ -467,6 +578,17 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
     }
     if ((st = read_ctrl(c))) return st;
     if (c->ctrl_h->done) break;
+  }
+  if (c->sample_ready && c->sample_tgt) {
+    CK(cudaMemsetAsync(&c->ctrl->done, 0, sizeof(int), c->s));
+    if (c->mixed)
+      launch_learn_target<float>(c->pp, c->pp_prev, c->mg.data(), c->learn_level, c->ctrl, c->sample_tgt, c->s,
+                                 &c->launches);
+    else
+      launch_learn_target<double>(c->pp, c->pp_prev, c->mg.data(), c->learn_level, c->ctrl, c->sample_tgt, c->s,
+                                  &c->launches);
+    CKL();
+    CK(cudaMemsetAsync(&c->ctrl->done, 0xff, sizeof(int), c->s));
   }
   // SOR: max |rhs - A p| of the final pressure; multigrid: max |r| of the
   // last outer iteration's residual, recorded by the loop itself (a second
@@ -517,6 +639,10 @@ int check_params(const o3d_params* p) {
   if (p->itscheme < 1 || p->itscheme > 3) { errf("itscheme %d unrecognized", p->itscheme); return O3D_ERR_BADARG; }
   if (p->precision != O3D_PREC_FP64 && p->precision != O3D_PREC_MIXED) { errf("precision %d unknown", p->precision); return O3D_ERR_BADARG; }
   if (p->solver != O3D_SOLVER_SOR && p->solver != O3D_SOLVER_MG) { errf("solver %d unknown", p->solver); return O3D_ERR_BADARG; }
+  if (p->mg_omega < 0.0 || p->mg_omega >= 2.0 || p->mg_pre < 0 || p->mg_post < 0 || p->mg_cycles < 0) {
+    errf("multigrid options out of range (mg_omega in [0, 2), sweep and cycle counts >= 0)");
+    return O3D_ERR_BADARG;
+  }
   if (!(p->dt > 0.0) || !(p->re > 0.0) || !(p->xlx > 0.0) || !(p->yly > 0.0) || !(p->zlz > 0.0)) {
     errf("dt, re and the domain lengths must be positive");
     return O3D_ERR_BADARG;
@@ -641,7 +767,8 @@ int o3d_destroy(o3d_ctx* c) {
     for (int h = 0; h < 3; ++h) cudaFree(c->fu[q][h]);
     cudaFree(c->fphi[q]);
   }
-  cudaFree(c->nu_t); cudaFree(c->rhs); cudaFree(c->pp);
+  cudaFree(c->nu_t); cudaFree(c->rhs); cudaFree(c->pp); cudaFree(c->pp_prev);
+  cudaFree(c->feat); cudaFree(c->ynet);
   cudaFree(c->phi); cudaFree(c->phi2); cudaFree(c->src);
   for (int q = 0; q < 4; ++q) cudaFree(c->stage[q]);
   cudaFree(c->part); cudaFree(c->spart); cudaFree(c->diag); cudaFree(c->ctrl);
@@ -907,6 +1034,54 @@ int o3d_rbsor_sweeps_dev(o3d_ctx* c, double* d_pp, const double* d_rhs, double o
   if (dmax_last) *dmax_last = bits_to_double(c->ctrl_h->dmax_key);
   return O3D_OK;
 }
+
+int o3d_attach_unet(o3d_ctx* c, o3d_unet* net) {
+  if (!c) return O3D_ERR_BADARG;
+  c->unet = net;
+  if (!net) return O3D_OK;
+  int st = learn_ready(c);
+  if (st) return st;
+  int nx, ny, nz, nin;
+  unet_grid(net, &nx, &ny, &nz, &nin);
+  const Grid& g2 = c->mg[c->learn_level].g;
+  if (nx != g2.nx || ny != g2.ny || nz != g2.nz || nin != 2) {
+    c->unet = nullptr;
+    errf("network grid %d x %d x %d (%d inputs) differs from the guess grid %d x %d x %d (2 inputs)", nx, ny, nz, nin,
+         g2.nx, g2.ny, g2.nz);
+    return O3D_ERR_BADARG;
+  }
+  CK(cudaStreamSynchronize(c->s));
+  return O3D_OK;
+}
+
+int o3d_guess_grid(o3d_ctx* c, int dims[3]) {
+  if (!c || !dims) return O3D_ERR_BADARG;
+  int st = learn_ready(c);
+  if (st) return st;
+  dims[0] = c->mg[c->learn_level].g.nx;
+  dims[1] = c->mg[c->learn_level].g.ny;
+  dims[2] = c->mg[c->learn_level].g.nz;
+  CK(cudaStreamSynchronize(c->s));
+  return O3D_OK;
+}
+
+int o3d_set_sample_buffers(o3d_ctx* c, float* d_feat, float* d_tgt) {
+  if (!c) return O3D_ERR_BADARG;
+  if ((d_feat == nullptr) != (d_tgt == nullptr)) {
+    errf("sample buffers: give both the feature and the target buffer, or neither");
+    return O3D_ERR_BADARG;
+  }
+  if (d_feat) {
+    int st = learn_ready(c);
+    if (st) return st;
+  }
+  c->sample_feat = d_feat;
+  c->sample_tgt = d_tgt;
+  c->sample_ready = 0;
+  return O3D_OK;
+}
+
+int o3d_sample_ready(const o3d_ctx* c) { return c ? c->sample_ready : 0; }
 
 int o3d_time_kernel(o3d_ctx* c, int kernel, int reps, double* ms_per_launch) {
   if (!c || reps < 1 || !ms_per_launch || kernel < 0 || kernel > 4) {

@@ -299,7 +299,9 @@ struct SolveCtrl {
   double rhs_mean;               // weighted mean removed from the rhs (multigrid)
   double res_inf;
   int iter, kmax, idyn, done, status;
-  int cycles;
+  int cycles;            // V-cycles run so far
+  int cycles_per_iter;   // V-cycles per outer iteration (multigrid)
+  double learn_scale;    // feature scale S of the learned warm start
 };
 
 }  // namespace o3d

@@ -4,7 +4,13 @@
 
 #include "o3d_internal.cuh"
 
+struct o3d_unet;
+
 namespace o3d {
+
+// the network of the learned guess (o3d_unet_host.cu)
+int unet_forward(o3d_unet* n, const float* d_in, float* d_out, cudaStream_t wait);
+int unet_grid(const o3d_unet* n, int* nx, int* ny, int* nz, int* in_ch);
 
 template <class T>
 struct PredArgs {
@@ -120,9 +126,22 @@ void launch_sor_fixed(double* p, const double* rhs, const Grid& g, const PoiCoef
 // Multigrid: T is the arithmetic of the cycles, R the type of the top rhs.
 template <class T, class R>
 void launch_mg_outer(double* p, const R* rhs, MGLevel* lv, int nlev, int pre, int post,
-                     int coarse_sweeps, T smooth_omega, SolveCtrl* ctrl, double* wpart,
-                     cudaStream_t s, long long* nl);
-// one finest-level kernel for timing: 0 smoother colour pass, 1 FP64 residual
+                     int coarse_sweeps, T smooth_omega, int cycles, SolveCtrl* ctrl, cudaStream_t s,
+                     long long* nl);
+void launch_extrapolate(double* p, double* pprev, long long n, cudaStream_t s);
+
+// learned warm start: the network works on multigrid level ll
+template <class T, class R>
+void launch_learn_features(double* p, const double* pprev, const R* rhs, MGLevel* lv, int ll, SolveCtrl* ctrl,
+                           float* feat, cudaStream_t s, long long* nl);
+template <class T>
+void launch_learn_apply(double* p, const float* y, MGLevel* lv, int ll, SolveCtrl* ctrl, cudaStream_t s,
+                        long long* nl);
+template <class T>
+void launch_learn_target(const double* p, const double* pprev, MGLevel* lv, int ll, SolveCtrl* ctrl, float* tgt,
+                         cudaStream_t s, long long* nl);
+
+// one finest-level kernel for timing: 0 smoother (one sweep), 1 FP64 residual
 template <class T, class R>
 void launch_level_kernel(int which, double* p, const R* rhs, const MGLevel& L, SolveCtrl* ctrl,
                          cudaStream_t s);

@@ -32,7 +32,7 @@ ERR_NOT_BUILT = -5
 
 PREC_FP64, PREC_MIXED = 0, 1
 SOLVER_SOR, SOLVER_MG = 0, 1
-GUESS_PREVIOUS, GUESS_ZERO, GUESS_LEARNED = 0, 1, 2
+GUESS_PREVIOUS, GUESS_ZERO, GUESS_LEARNED, GUESS_EXTRAPOLATED = 0, 1, 2, 3
 
 FIELD = {"ux": 0, "uy": 1, "uz": 2, "pp": 3, "ux_pred": 4, "uy_pred": 5, "uz_pred": 6,
          "phi": 7, "src": 8, "nu_t": 9, "rhs": 10}
@@ -61,6 +61,7 @@ class Params(C.Structure):
         ("iles", C.c_int), ("cs", C.c_double),
         ("precision", C.c_int), ("solver", C.c_int), ("mg_levels", C.c_int),
         ("mg_pre", C.c_int), ("mg_post", C.c_int), ("guess", C.c_int), ("diagnostics", C.c_int),
+        ("mg_cycles", C.c_int), ("mg_omega", C.c_double),
     ]
 
 
@@ -125,6 +126,19 @@ def lib(build_if_missing: bool = True):
             "o3d_statistics_calc": (C.c_int, [vp, C.c_double, _dp]),
             "o3d_rbsor_sweeps_dev": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, _dp]),
             "o3d_time_kernel": (C.c_int, [vp, C.c_int, C.c_int, _dp]),
+            "o3d_unet_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), C.c_int, C.c_int,
+                                          C.c_int, C.c_ulonglong, C.POINTER(vp)]),
+            "o3d_unet_destroy": (C.c_int, [vp]),
+            "o3d_unet_num_params": (C.c_longlong, [vp]),
+            "o3d_unet_get_params": (C.c_int, [vp, C.POINTER(C.c_float)]),
+            "o3d_unet_set_params": (C.c_int, [vp, C.POINTER(C.c_float)]),
+            "o3d_unet_forward_dev": (C.c_int, [vp, vp, vp, vp]),
+            "o3d_unet_gradients": (C.c_int, [vp, vp, vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+            "o3d_unet_train_step": (C.c_int, [vp, vp, vp, C.c_float, C.POINTER(C.c_float)]),
+            "o3d_guess_grid": (C.c_int, [vp, C.POINTER(C.c_int)]),
+            "o3d_attach_unet": (C.c_int, [vp, vp]),
+            "o3d_set_sample_buffers": (C.c_int, [vp, vp, vp]),
+            "o3d_sample_ready": (C.c_int, [vp]),
             "o3d_divergence_stats_noalloc": (C.c_int, [vp, vp, vp, vp, C.c_int, C.c_int, C.c_int,
                                                        C.c_double, C.c_double, C.c_double, C.c_int,
                                                        C.c_int, C.c_int, C.c_int, vp, _dp]),
@@ -284,6 +298,22 @@ class Context:
         self._check(self.L.o3d_statistics_calc(self.h, t, out))
         return np.array(out[:])
 
+    # -- learned warm start ----------------------------------------------------
+    def guess_grid(self):
+        dims = (C.c_int * 3)()
+        self._check(self.L.o3d_guess_grid(self.h, dims))
+        return tuple(dims)
+
+    def attach_unet(self, net: "UNet | None") -> None:
+        self._check(self.L.o3d_attach_unet(self.h, net.h if net else None))
+        self._net = net  # keep the network alive while attached
+
+    def set_sample_buffers(self, d_feat: int | None, d_tgt: int | None) -> None:
+        self._check(self.L.o3d_set_sample_buffers(self.h, C.c_void_p(d_feat or 0), C.c_void_p(d_tgt or 0)))
+
+    def sample_ready(self) -> bool:
+        return bool(self.L.o3d_sample_ready(self.h))
+
     KERNELS = {"predict": 0, "rhs": 1, "correct": 2, "mg_smooth": 3, "resid64": 4}
 
     def time_kernel(self, name: str, reps: int = 20) -> float:
@@ -297,6 +327,66 @@ class Context:
         self._check(self.L.o3d_rbsor_sweeps_dev(self.h, C.c_void_p(d_pp), C.c_void_p(d_rhs), omega,
                                                 nsweeps, C.byref(dm)))
         return dm.value
+
+
+class UNet:
+    """The 3D U-Net of the learned warm start (o3d_unet_*): BF16 tensor-core
+    convolutions, trained by the library's own forward/backward kernels."""
+
+    def __init__(self, dims, periodic=(1, 1, 1), base=16, levels=4, in_channels=2, seed=1234):
+        self.L = lib()
+        h = C.c_void_p()
+        per = (C.c_int * 3)(*periodic)
+        st = self.L.o3d_unet_create(dims[0], dims[1], dims[2], per, base, levels, in_channels, seed, C.byref(h))
+        if st < 0:
+            raise O3DError(st, self.L.o3d_last_error().decode())
+        self.h = h
+        self.dims, self.base, self.levels, self.in_channels = tuple(dims), base, levels, in_channels
+        self.periodic = tuple(periodic)
+
+    def _check(self, code: int) -> int:
+        if code < 0:
+            raise O3DError(code, self.L.o3d_last_error().decode())
+        return code
+
+    @property
+    def nparams(self) -> int:
+        return int(self.L.o3d_unet_num_params(self.h))
+
+    def get_params(self) -> np.ndarray:
+        out = np.zeros(self.nparams, dtype=np.float32)
+        self._check(self.L.o3d_unet_get_params(self.h, out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        self._check(self.L.o3d_unet_set_params(self.h, p.ctypes.data_as(C.POINTER(C.c_float))))
+
+    def forward(self, d_in: int, d_out: int, stream: int | None = None) -> None:
+        self._check(self.L.o3d_unet_forward_dev(self.h, C.c_void_p(d_in), C.c_void_p(d_out), C.c_void_p(stream or 0)))
+
+    def gradients(self, d_in: int, d_tgt: int):
+        loss = C.c_float(0)
+        g = np.zeros(self.nparams, dtype=np.float32)
+        self._check(self.L.o3d_unet_gradients(self.h, C.c_void_p(d_in), C.c_void_p(d_tgt), C.byref(loss),
+                                              g.ctypes.data_as(C.POINTER(C.c_float))))
+        return loss.value, g
+
+    def train_step(self, d_in: int, d_tgt: int, lr: float) -> float:
+        loss = C.c_float(0)
+        self._check(self.L.o3d_unet_train_step(self.h, C.c_void_p(d_in), C.c_void_p(d_tgt), lr, C.byref(loss)))
+        return loss.value
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.L.o3d_unet_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def divergence_stats_noalloc(d_fx: int, d_fy: int, d_fz: int, d_div: int | None, shape, spacing, bcs,
