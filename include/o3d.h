@@ -65,7 +65,7 @@ enum {
 enum {
   O3D_GUESS_PREVIOUS = 0, /* previous step's pressure (the reference: pp persists) */
   O3D_GUESS_ZERO = 1,
-  O3D_GUESS_LEARNED = 2,  /* 3D U-Net prediction from (div u*, previous p) */
+  O3D_GUESS_LEARNED = 2,  /* extrapolated pressure plus a 3D U-Net correction (below) */
   O3D_GUESS_EXTRAPOLATED = 3 /* 2 p(n) - p(n-1): linear extrapolation in time */
 };
 
@@ -199,13 +199,17 @@ O3D_API int o3d_step_host(o3d_ctx *ctx, int itime, double *ux, double *uy, doubl
 O3D_API int o3d_statistics_calc(o3d_ctx *ctx, double t, double out[17]);
 
 /* ---- learned Poisson warm start ------------------------------------------
- * A 3D U-Net (BF16 tensor-core convolutions, FP32 accumulation) predicts the
- * pressure increment of the next solve from the residual of the previous
- * pressure, r = rhs - A p(n), and the last increment p(n) - p(n-1), both on
- * the grid two multigrid coarsenings below the pressure grid and scaled by
- * S = rms of that increment.  The guess is p(n) + S * prolong(prolong(y));
- * the solver then iterates to eps as usual.  No counterpart in the
- * reference. */
+ * A 3D U-Net (BF16 tensor-core convolutions, FP32 accumulation) corrects the
+ * extrapolated pressure p_ex = 2 p(n) - p(n-1).  Its input, on the multigrid
+ * level ll of o3d_guess_grid (the pressure grid coarsened 1 to 3 times, at
+ * least 16 points per axis): the restricted FP64 residual of p_ex times
+ * h_ll^2, and the restricted last increment p(n) - p(n-1), both divided by
+ * S = rms of the restricted increment.  Its output y predicts
+ * restrict(p(n+1) - p_ex) / S.  The correction prolong(S y) starts the first
+ * V-cycle of the multigrid solve (the residual already computed is reused),
+ * or is added to p_ex before SOR; the solver then iterates to eps as
+ * usual, so the converged pressure does not depend on the network.  No
+ * counterpart in the reference. */
 typedef struct o3d_unet o3d_unet;
 /* nx, ny, nz: the network grid (that of o3d_guess_grid); periodic[a] = 1
  * wraps axis a in the convolutions; base_channels (16) doubles per level. */
@@ -229,8 +233,9 @@ O3D_API int o3d_guess_grid(o3d_ctx *ctx, int dims[3]);
 /* use `net` for O3D_GUESS_LEARNED (NULL detaches); the caller keeps ownership */
 O3D_API int o3d_attach_unet(o3d_ctx *ctx, o3d_unet *net);
 /* Training data: with device buffers set (features 2 x n, target n on the
- * guess grid), every solve that has a previous pressure writes its features
- * before and its target, restrict(restrict(p(n+1) - p(n))) / S, after. */
+ * guess grid), every multigrid solve with the extrapolated or learned guess
+ * that has a previous pressure writes the network input before and the
+ * target, restrict(p(n+1) - p_ex) / S, after (O3D_ERR_BADARG otherwise). */
 O3D_API int o3d_set_sample_buffers(o3d_ctx *ctx, float *d_feat, float *d_tgt);
 /* 1 when the last solve wrote a sample */
 O3D_API int o3d_sample_ready(const o3d_ctx *ctx);
@@ -244,6 +249,13 @@ O3D_API int o3d_sample_ready(const o3d_ctx *ctx);
  * recompute the velocity identically from u* and p.  No counterpart in the
  * reference (measurement hook). */
 O3D_API int o3d_time_kernel(o3d_ctx *ctx, int kernel, int reps, double *ms_per_launch);
+
+/* Self-check of the binary64 <-> binary32 conversions the kernels perform on
+ * the integer pipe (round to nearest even): converts n seeded pseudo-random
+ * bit patterns (normal, subnormal, zero, tie and out-of-range cases) both
+ * ways on the device and counts results that differ bit-wise from the FP64
+ * conversion instructions.  No counterpart in the reference. */
+O3D_API int o3d_check_conversions(long long n, unsigned long long seed, long long *mismatches);
 
 /* divergence(divf, fx, fy, fz, ..., odd) with function_stats of the result
  * (src/differential_operators.f90:7-38, src/functions.f90:27-63) for callers

@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(256) k_wmean_part(const R* __restrict__ rhs, G
     if (g.bc[1] == AX_MIRROR && (j == 0 || j == g.ny - 1)) wxy *= 0.5;
     double acc = 0.0, edge = 0.0;
     for (int k = 0; k < g.nz; ++k) {
-      const double v = (double)rhs[(long long)i + g.sy() * j + g.sz() * k];
+      const double v = to_t<double>(rhs[(long long)i + g.sy() * j + g.sz() * k]);
       if (k == 0 || k == g.nz - 1) edge += v; else acc += v;
     }
     const double wz = g.bc[2] == AX_MIRROR ? 0.5 : 1.0;
@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(256) k_resid_top(const double* __restrict__ p,
   if (i >= g.nx || j >= g.ny) return;
   const long long q = (long long)i + g.sy() * j + g.sz() * k;
   const double ap = lap_nb<double>(p, g, i, j, k, c) + c.A * p[q];
-  r0[q] = (T)(((double)rhs[q] - ctrl->rhs_mean) - ap);
+  r0[q] = to_t<T>((to_t<double>(rhs[q]) - ctrl->rhs_mean) - ap);
 }
 
 // same residual, plus max |r| of the block into ctrl->res_key
@@ -192,7 +192,7 @@ __global__ void __launch_bounds__(256) k_resid_top_max(const double* __restrict_
   if (i < g.nx && j < g.ny) {
     const long long q = (long long)i + g.sy() * j + g.sz() * k;
     const double ap = lap_nb<double>(p, g, i, j, k, c) + c.A * p[q];
-    const T rv = (T)(((double)rhs[q] - ctrl->rhs_mean) - ap);
+    const T rv = to_t<T>((to_t<double>(rhs[q]) - ctrl->rhs_mean) - ap);
     r0[q] = rv;
     m = fabsf((float)rv);
   }
@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(256) k_resid_inf(const double* __restrict__ p,
   if (i < g.nx && j < g.ny) {
     const long long q = (long long)i + g.sy() * j + g.sz() * k;
     const double ap = lap_nb<double>(p, g, i, j, k, c) + c.A * p[q];
-    d = fabs(((double)rhs[q] - (use_mean ? ctrl->rhs_mean : 0.0)) - ap);
+    d = fabs((to_t<double>(rhs[q]) - (use_mean ? ctrl->rhs_mean : 0.0)) - ap);
   }
   const double bm = block_max(d);
   if (threadIdx.x == 0 && threadIdx.y == 0 && bm > 0.0)
@@ -477,7 +477,7 @@ __global__ void __launch_bounds__(256) k_update(double* __restrict__ p, const T*
     const long long q = base + (long long)u * blockDim.x;
     if (q < n) {
       const T ev = e[q];
-      p[q] += (double)ev;
+      p[q] += to_t<double>(ev);
       m = fmax(m, fabs(ev));
     }
   }
@@ -549,22 +549,37 @@ static void vcycle(MGLevel* lv, int l, int nlev, int pre, int post, int coarse_s
   smooth_sweeps<T>(L, e, r, c, om, post, ctrl, s, nl);
 }
 
-// One outer iteration of the defect-correction loop: FP64 residual, `cycles`
-// V-cycles in T on A e = r (the first from e = 0, the next ones from the
-// current e), p += e in FP64, stop test.
+// One outer iteration of the defect-correction loop, in two parts.
+// launch_mg_resid: r0 = rhs - mean - A p in FP64 (stored in T) with max |r0|.
 template <class T, class R>
-void launch_mg_outer(double* p, const R* rhs, MGLevel* lv, int nlev, int pre, int post,
-                     int coarse_sweeps, T smooth_omega, int cycles, SolveCtrl* ctrl, cudaStream_t s,
-                     long long* nl) {
+void launch_mg_resid(double* p, const R* rhs, MGLevel* lv, SolveCtrl* ctrl, cudaStream_t s, long long* nl) {
   const MGLevel& L0 = lv[0];
   PoiCoef<double> c64 = make_poi<double>(L0.h[0], L0.h[1], L0.h[2]);
   k_resid_top_max<T, R><<<g3(L0.g), dim3(32, 8), 0, s>>>(p, rhs, (T*)L0.r, L0.g, c64, ctrl);
   *nl += 1;
-  for (int q = 0; q < cycles; ++q) vcycle<T>(lv, 0, nlev, pre, post, coarse_sweeps, smooth_omega, ctrl, s, nl, q == 0);
+}
+
+// launch_mg_cycles: `cycles` V-cycles in T on A e = r0 (the first from e = 0,
+// or from the correction already in the finest level's e when from_e), then
+// p += e in FP64 and the stop test.
+template <class T>
+void launch_mg_cycles(double* p, MGLevel* lv, int nlev, int pre, int post, int coarse_sweeps, T smooth_omega,
+                      int cycles, bool from_e, SolveCtrl* ctrl, cudaStream_t s, long long* nl) {
+  const MGLevel& L0 = lv[0];
+  for (int q = 0; q < cycles; ++q)
+    vcycle<T>(lv, 0, nlev, pre, post, coarse_sweeps, smooth_omega, ctrl, s, nl, q == 0 && !from_e);
   k_update<T><<<(unsigned)((L0.g.n + 256LL * UPD_PER - 1) / (256LL * UPD_PER)), 256, 0, s>>>(p, (const T*)L0.e,
                                                                                          L0.g.n, ctrl);
   k_mg_control<<<1, 1, 0, s>>>(ctrl);
   *nl += 2;
+}
+
+template <class T, class R>
+void launch_mg_outer(double* p, const R* rhs, MGLevel* lv, int nlev, int pre, int post,
+                     int coarse_sweeps, T smooth_omega, int cycles, SolveCtrl* ctrl, cudaStream_t s,
+                     long long* nl) {
+  launch_mg_resid<T, R>(p, rhs, lv, ctrl, s, nl);
+  launch_mg_cycles<T>(p, lv, nlev, pre, post, coarse_sweeps, smooth_omega, cycles, false, ctrl, s, nl);
 }
 
 // p <- 2 p - p_prev, p_prev <- p (linear extrapolation of the pressure in time)
@@ -579,17 +594,26 @@ void launch_extrapolate(double* p, double* pprev, long long n, cudaStream_t s) {
   k_extrapolate<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p, pprev, n);
 }
 
-// ---------------------------------------------------------------------------
-// learned warm start plumbing: features and targets at the network grid
-// (the multigrid level two coarsenings below the pressure grid)
-// ---------------------------------------------------------------------------
-// d = p - pprev in T
+// the same extrapolation, also writing the last increment d = p - p_prev in T
 template <class T>
-__global__ void k_pdiff(const double* __restrict__ p, const double* __restrict__ pprev, T* __restrict__ d, long long n) {
+__global__ void k_extrapolate_d(double* __restrict__ p, double* __restrict__ pprev, T* __restrict__ d, long long n) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q < n) d[q] = (T)(p[q] - pprev[q]);
+  if (q >= n) return;
+  const double pc = p[q], pv = pprev[q];
+  p[q] = 2.0 * pc - pv;
+  pprev[q] = pc;
+  d[q] = to_t<T>(pc - pv);
 }
 
+// ---------------------------------------------------------------------------
+// learned warm start plumbing.  The network works on multigrid level ll
+// (coarsened ll times on every axis).  Its input, for the extrapolated
+// pressure p_ex = 2 p^n - p^(n-1): channel 0 = restrict(rhs - mean - A p_ex)
+// h_ll^2 / S, channel 1 = restrict(p^n - p^(n-1)) / S, with S the rms of the
+// restricted increment; its output y predicts restrict(p^(n+1) - p_ex) / S.
+// The correction prolong(S y) starts the first V-cycle (multigrid) or is
+// added to p (SOR).
+// ---------------------------------------------------------------------------
 // learn_scale = sqrt(mean(d^2)) over the coarse grid (one block)
 template <class T>
 __global__ void k_rms(const T* __restrict__ d, long long n, SolveCtrl* ctrl) {
@@ -626,18 +650,28 @@ __global__ void k_unscale(const float* __restrict__ y, long long n, const SolveC
   if (q < n) e[q] = (T)((double)y[q] * ctrl->learn_scale);
 }
 
-// training target t = d / S (FP32)
+// training target t = dp / S - ch1 (dp = restrict(p^(n+1) - p^n), ch1 = the
+// increment channel of the input): restrict(p^(n+1) - p_ex) / S, restriction
+// being linear
 template <class T>
-__global__ void k_target(const T* __restrict__ d, long long n, const SolveCtrl* ctrl, float* __restrict__ t) {
+__global__ void k_target(const T* __restrict__ dp, long long n, const SolveCtrl* ctrl, const float* __restrict__ ch1,
+                         float* __restrict__ t) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q < n) t[q] = (float)((double)d[q] / ctrl->learn_scale);
+  if (q < n) t[q] = (float)((double)dp[q] / ctrl->learn_scale - (double)ch1[q]);
+}
+
+// d = p - pprev in T
+template <class T>
+__global__ void k_pdiff(const double* __restrict__ p, const double* __restrict__ pprev, T* __restrict__ d, long long n) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) d[q] = to_t<T>(p[q] - pprev[q]);
 }
 
 // p += e
 template <class T>
 __global__ void k_padd(double* __restrict__ p, const T* __restrict__ e, long long n) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q < n) p[q] += (double)e[q];
+  if (q < n) p[q] += to_t<double>(e[q]);
 }
 
 static inline unsigned b256(long long n) { return (unsigned)((n + 255) / 256); }
@@ -659,65 +693,77 @@ static T* restrict_to(MGLevel* lv, int ll, const T* f0, int which, SolveCtrl* ct
   return dst;
 }
 
-// Features of the learned guess from the current pressure p (= p^n), the
-// previous pressure pprev and the rhs: r = rhs - mean - A p and d = p - pprev,
-// both restricted to level ll; S = rms(d).  Writes feat (2 x n_ll FP32).
-// Uses the scratch arrays of levels 0..ll; ctrl->done must be 0.
-template <class T, class R>
-void launch_learn_features(double* p, const double* pprev, const R* rhs, MGLevel* lv, int ll, SolveCtrl* ctrl,
-                           float* feat, cudaStream_t s, long long* nl) {
-  const MGLevel& L0 = lv[0];
-  PoiCoef<double> c64 = make_poi<double>(L0.h[0], L0.h[1], L0.h[2]);
-  k_resid_top<T, R><<<g3(L0.g), dim3(32, 8), 0, s>>>(p, rhs, (T*)L0.r, L0.g, c64, ctrl);
-  k_pdiff<T><<<b256(L0.g.n), 256, 0, s>>>(p, pprev, (T*)L0.t, L0.g.n);
-  const T* rc = restrict_to<T>(lv, ll, (const T*)L0.r, 0, ctrl, s, nl);
-  const T* dc = restrict_to<T>(lv, ll, (const T*)L0.t, 1, ctrl, s, nl);
+// p <- p_ex, p_prev <- p, and the increment into the finest level's t
+template <class T>
+void launch_learn_extrapolate(double* p, double* pprev, MGLevel* lv, cudaStream_t s, long long* nl) {
+  k_extrapolate_d<T><<<b256(lv[0].g.n), 256, 0, s>>>(p, pprev, (T*)lv[0].t, lv[0].g.n);
+  *nl += 1;
+}
+
+// Network input from the residual of p_ex in the finest level's r (left
+// intact) and the increment in its t; uses the e and t arrays of levels
+// 1..ll.  ctrl->done must be 0.
+template <class T>
+void launch_learn_features(MGLevel* lv, int ll, SolveCtrl* ctrl, float* feat, cudaStream_t s, long long* nl) {
+  const T* rc = restrict_to<T>(lv, ll, (const T*)lv[0].r, 0, ctrl, s, nl);
+  const T* dc = restrict_to<T>(lv, ll, (const T*)lv[0].t, 1, ctrl, s, nl);
   const long long n2 = lv[ll].g.n;
   k_rms<T><<<1, 1024, 0, s>>>(dc, n2, ctrl);
   const double h2 = lv[ll].h[0] * lv[ll].h[0];
   k_features<T><<<b256(n2), 256, 0, s>>>(rc, dc, n2, h2, ctrl, feat);
-  *nl += 4;
+  *nl += 2;
 }
 
-// p += prolong^ll(S * y) with y the network output on level ll.
+// Finest level's e <- prolong^ll(S y) (y: network output on level ll); with
+// add_to_p, also p += e.
 template <class T>
-void launch_learn_apply(double* p, const float* y, MGLevel* lv, int ll, SolveCtrl* ctrl, cudaStream_t s,
-                        long long* nl) {
+void launch_learn_apply(double* p, const float* y, MGLevel* lv, int ll, bool add_to_p, SolveCtrl* ctrl,
+                        cudaStream_t s, long long* nl) {
   const long long n2 = lv[ll].g.n;
   k_unscale<T><<<b256(n2), 256, 0, s>>>(y, n2, ctrl, (T*)lv[ll].e);
+  *nl += 1;
   for (int l = ll - 1; l >= 0; --l) {
     cudaMemsetAsync(lv[l].e, 0, (size_t)lv[l].g.n * sizeof(T), s);
     Coarsen cz;
     for (int a = 0; a < 3; ++a) cz.c[a] = lv[l].coarsen[a];
-    k_prolong<T><<<g3(lv[l].g), dim3(32, 8), 0, s>>>((T*)lv[l].e, (const T*)lv[l + 1].e, lv[l].g, lv[l + 1].g, cz,
-                                                     ctrl);
+    if (cz.c[0] && cz.c[1] && cz.c[2])
+      k_prolong_cell<T><<<g3(lv[l + 1].g), dim3(32, 8), 0, s>>>((T*)lv[l].e, (const T*)lv[l + 1].e, lv[l].g,
+                                                                lv[l + 1].g, ctrl);
+    else
+      k_prolong<T><<<g3(lv[l].g), dim3(32, 8), 0, s>>>((T*)lv[l].e, (const T*)lv[l + 1].e, lv[l].g, lv[l + 1].g,
+                                                       cz, ctrl);
     *nl += 1;
   }
-  k_padd<T><<<b256(lv[0].g.n), 256, 0, s>>>(p, (const T*)lv[0].e, lv[0].g.n);
-  *nl += 2;
+  if (add_to_p) {
+    k_padd<T><<<b256(lv[0].g.n), 256, 0, s>>>(p, (const T*)lv[0].e, lv[0].g.n);
+    *nl += 1;
+  }
 }
 
-// Training target of the last solve: restrict^ll(p - pprev) / S into tgt (FP32).
+// Training target of the last solve into tgt (FP32); ch1 is the increment
+// channel of that solve's network input.
 template <class T>
-void launch_learn_target(const double* p, const double* pprev, MGLevel* lv, int ll, SolveCtrl* ctrl, float* tgt,
-                         cudaStream_t s, long long* nl) {
+void launch_learn_target(const double* p, const double* pprev, MGLevel* lv, int ll, SolveCtrl* ctrl,
+                         const float* ch1, float* tgt, cudaStream_t s, long long* nl) {
   const MGLevel& L0 = lv[0];
   k_pdiff<T><<<b256(L0.g.n), 256, 0, s>>>(p, pprev, (T*)L0.t, L0.g.n);
   const T* dc = restrict_to<T>(lv, ll, (const T*)L0.t, 1, ctrl, s, nl);
-  k_target<T><<<b256(lv[ll].g.n), 256, 0, s>>>(dc, lv[ll].g.n, ctrl, tgt);
+  k_target<T><<<b256(lv[ll].g.n), 256, 0, s>>>(dc, lv[ll].g.n, ctrl, ch1, tgt);
   *nl += 2;
 }
 
-template void launch_learn_features<float, float>(double*, const double*, const float*, MGLevel*, int, SolveCtrl*,
-                                                  float*, cudaStream_t, long long*);
-template void launch_learn_features<double, double>(double*, const double*, const double*, MGLevel*, int, SolveCtrl*,
-                                                    float*, cudaStream_t, long long*);
-template void launch_learn_apply<float>(double*, const float*, MGLevel*, int, SolveCtrl*, cudaStream_t, long long*);
-template void launch_learn_apply<double>(double*, const float*, MGLevel*, int, SolveCtrl*, cudaStream_t, long long*);
-template void launch_learn_target<float>(const double*, const double*, MGLevel*, int, SolveCtrl*, float*, cudaStream_t,
-                                         long long*);
-template void launch_learn_target<double>(const double*, const double*, MGLevel*, int, SolveCtrl*, float*,
-                                          cudaStream_t, long long*);
+#define O3D_LEARN_INST(T)                                                                                      \
+  template void launch_learn_extrapolate<T>(double*, double*, MGLevel*, cudaStream_t, long long*);             \
+  template void launch_learn_features<T>(MGLevel*, int, SolveCtrl*, float*, cudaStream_t, long long*);         \
+  template void launch_learn_apply<T>(double*, const float*, MGLevel*, int, bool, SolveCtrl*, cudaStream_t,    \
+                                      long long*);                                                             \
+  template void launch_learn_target<T>(const double*, const double*, MGLevel*, int, SolveCtrl*, const float*, \
+                                       float*, cudaStream_t, long long*);                                      \
+  template void launch_mg_resid<T, T>(double*, const T*, MGLevel*, SolveCtrl*, cudaStream_t, long long*);      \
+  template void launch_mg_cycles<T>(double*, MGLevel*, int, int, int, int, T, int, bool, SolveCtrl*,           \
+                                    cudaStream_t, long long*);
+O3D_LEARN_INST(float)
+O3D_LEARN_INST(double)
 
 template <class R>
 void launch_rhs_wmean(const R* rhs, const Grid& g, double* part, SolveCtrl* ctrl, cudaStream_t s,

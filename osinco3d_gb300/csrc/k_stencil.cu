@@ -1,8 +1,6 @@
-// k_stencil.cu -- stencil kernels of the step: single derivatives, the fused
-// momentum predictor (9 first + 9 second derivatives, Smagorinsky nu_t,
-// convection, diffusion and the Adams-Bashforth update in one pass), the
-// divergence/right-hand side, the velocity correction, the scalar transport
-// and the flow statistics.  Templated on the arithmetic type T (double for
+// k_stencil.cu -- stencil kernels of the step outside the 2.5D pipeline
+// (k_stencil25.cu): single derivatives, standalone nu_t, the scalar
+// transport and the flow statistics.  Templated on the arithmetic type T (double for
 // the plain method, float for the mixed method).
 #include "o3d_internal.cuh"
 #include "o3d_kernels.h"
@@ -27,361 +25,6 @@ __global__ void k_der(const T* __restrict__ f, T* __restrict__ df, Grid g, AxisC
   T v[7];
   load_line<3>(f, g, axis, i, j, k, odd != 0, v);
   df[q] = order == 1 ? d1(v, c) : d2(v, c);
-}
-
-// ---------------------------------------------------------------------------
-// fused predictor, predict_velocity + calculate_nu_t
-// (src/integration.f90:106-188, src/les_turbulence.f90:54-88)
-// ---------------------------------------------------------------------------
-template <class T>
-__global__ void __launch_bounds__(256) k_predict(PredArgs<T> A) {
-  const Grid& g = A.g;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
-  if (i >= g.nx || j >= g.ny) return;
-  const long long q = (long long)i + g.sy() * j + g.sz() * k;
-
-  T uc[3], g1[3][3], g2[3][3];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      if (g.bc[a] == AX_ZERO) {
-        g1[c][a] = (T)0;
-        g2[c][a] = (T)0;
-        continue;
-      }
-      T v[7];
-      // component c is odd along its own axis: derxi/derxxi for ux, deryi for uy, derzi for uz
-      load_line<3>(A.u[c], g, a, i, j, k, a == c, v);
-      g1[c][a] = d1(v, A.cf.ax[a]);
-      g2[c][a] = d2(v, A.cf.ax[a]);
-      if (a == 0) uc[c] = v[3];
-    }
-  }
-  T nut = (T)0;
-  if (A.les) {
-    const T s11 = g1[0][0], s22 = g1[1][1], s33 = g1[2][2];
-    const T s12 = (T)0.5 * (g1[0][1] + g1[1][0]);
-    const T s13 = (T)0.5 * (g1[0][2] + g1[2][0]);
-    const T s23 = (T)0.5 * (g1[1][2] + g1[2][1]);
-    const T smag = sqrt((T)2 * (s11 * s11 + s22 * s22 + s33 * s33 +
-                                (T)2 * (s12 * s12 + s13 * s13 + s23 * s23)));
-    nut = A.csd2 * smag;
-    A.nu_t[q] = nut;
-  }
-  const T nu_eff = A.onere + nut;
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    const T F = nu_eff * (g2[c][0] + g2[c][1] + g2[c][2]) -
-                (uc[0] * g1[c][0] + uc[1] * g1[c][1] + uc[2] * g1[c][2]);
-    T up = uc[c] + A.adu * F;
-    if (A.f2[c]) up = up + A.bdu * A.f2[c][q];
-    if (A.f3[c]) up = up + A.cdu * A.f3[c][q];
-    A.fnew[c][q] = F;
-    A.up[c][q] = up;
-  }
-}
-
-// ---------------------------------------------------------------------------
-// 2.5D fused predictor.  A block owns a TX x TY column of (x, y) points and
-// marches along z over a chunk of planes.  Each thread keeps the seven
-// z-neighbours of its point for the three components in a register queue;
-// the current plane's x- and y-lines (with 3-point halos, ghost-mapped at the
-// domain ends) are staged in double-buffered shared memory, so every value
-// is read from global memory once per plane plus the halos.
-// ---------------------------------------------------------------------------
-template <class T, class S>
-__device__ __forceinline__ T ldg_map(const S* __restrict__ f, const Grid& g, int i, int j, int k,
-                                     int odd_axis) {
-  bool fx, fy, fz;
-  const int ii = ghost(i, g.nx, g.bc[0], &fx);
-  const int jj = ghost(j, g.ny, g.bc[1], &fy);
-  const int kk = ghost(k, g.nz, g.bc[2] == AX_ZERO ? AX_PERIODIC : g.bc[2], &fz);
-  const T v = (T)__ldg(f + ii + g.sy() * jj + g.sz() * kk);
-  const bool neg = (fx && odd_axis == 0) || (fy && odd_axis == 1) || (fz && odd_axis == 2);
-  return neg ? -v : v;
-}
-
-template <class T, int TX, int TY>
-__global__ void __launch_bounds__(TX * TY, sizeof(T) == 4 ? 3 : 1) k_predict25(PredArgs<T> A, int kc) {
-  const Grid& g = A.g;
-  __shared__ T sx[2][3][TY][TX + 6];
-  __shared__ T sy[2][3][TY + 6][TX];
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
-  const int i = i0 + tx, j = j0 + ty;
-  // points past the grid end still stage ghost-mapped values: the lines of
-  // the last valid points read them
-  const bool valid = i < g.nx && j < g.ny;
-  const int k0 = blockIdx.z * kc;
-  const int k1 = min(k0 + kc, g.nz);
-  const bool zon = g.bc[2] != AX_ZERO;
-  const bool hx = tx < 3, hy = ty < 3;
-  const int hxi0 = i0 - 3 + tx, hxi1 = i0 + TX + tx;  // x-halo columns of this thread
-  const int hyj0 = j0 - 3 + ty, hyj1 = j0 + TY + ty;  // y-halo rows of this thread
-
-  // register queue: q[c][m] = u_c(i, j, k - 3 + m)
-  T q[3][7];
-#pragma unroll
-  for (int c = 0; c < 3; ++c)
-#pragma unroll
-    for (int m = 0; m < 6; ++m) q[c][m + 1] = zon || m == 2 ? ldg_map<T>(A.u[c], g, i, j, k0 - 3 + m, c) : (T)0;
-  // halos of the first plane
-  T hxv[3][2], hyv[3][2];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    hxv[c][0] = hx ? ldg_map<T>(A.u[c], g, hxi0, j, k0, c) : (T)0;
-    hxv[c][1] = hx ? ldg_map<T>(A.u[c], g, hxi1, j, k0, c) : (T)0;
-    hyv[c][0] = hy ? ldg_map<T>(A.u[c], g, i, hyj0, k0, c) : (T)0;
-    hyv[c][1] = hy ? ldg_map<T>(A.u[c], g, i, hyj1, k0, c) : (T)0;
-  }
-
-  int buf = 0;
-  for (int k = k0; k < k1; ++k) {
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-#pragma unroll
-      for (int m = 0; m < 6; ++m) q[c][m] = q[c][m + 1];
-      if (!zon) q[c][3] = ldg_map<T>(A.u[c], g, i, j, k, c);
-      // stage plane k
-      sx[buf][c][ty][tx + 3] = q[c][3];
-      sy[buf][c][ty + 3][tx] = q[c][3];
-      if (hx) {
-        sx[buf][c][ty][tx] = hxv[c][0];
-        sx[buf][c][ty][TX + 3 + tx] = hxv[c][1];
-      }
-      if (hy) {
-        sy[buf][c][ty][tx] = hyv[c][0];
-        sy[buf][c][TY + 3 + ty][tx] = hyv[c][1];
-      }
-    }
-    // issue the loads of the next plane (queue head and halos) before computing
-    const int kn = k + 1;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      q[c][6] = zon ? ldg_map<T>(A.u[c], g, i, j, k + 3, c) : (T)0;
-      if (kn < k1) {
-        if (hx) {
-          hxv[c][0] = ldg_map<T>(A.u[c], g, hxi0, j, kn, c);
-          hxv[c][1] = ldg_map<T>(A.u[c], g, hxi1, j, kn, c);
-        }
-        if (hy) {
-          hyv[c][0] = ldg_map<T>(A.u[c], g, i, hyj0, kn, c);
-          hyv[c][1] = ldg_map<T>(A.u[c], g, i, hyj1, kn, c);
-        }
-      }
-    }
-    const long long p = (long long)min(i, g.nx - 1) + g.sy() * min(j, g.ny - 1) + g.sz() * k;
-    T h2[3], h3[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      h2[c] = A.f2[c] ? __ldg(A.f2[c] + p) : (T)0;
-      h3[c] = A.f3[c] ? __ldg(A.f3[c] + p) : (T)0;
-    }
-    __syncthreads();
-    T g1[3][3], g2[3][3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      T v[7];
-#pragma unroll
-      for (int m = 0; m < 7; ++m) v[m] = sx[buf][c][ty][tx + m];
-      g1[c][0] = d1(v, A.cf.ax[0]);
-      g2[c][0] = d2(v, A.cf.ax[0]);
-#pragma unroll
-      for (int m = 0; m < 7; ++m) v[m] = sy[buf][c][ty + m][tx];
-      g1[c][1] = d1(v, A.cf.ax[1]);
-      g2[c][1] = d2(v, A.cf.ax[1]);
-      if (zon) {  // q[c][0..6] holds planes k-3 .. k+3
-        g1[c][2] = d1(q[c], A.cf.ax[2]);
-        g2[c][2] = d2(q[c], A.cf.ax[2]);
-      } else {
-        g1[c][2] = (T)0;
-        g2[c][2] = (T)0;
-      }
-    }
-    if (valid) {
-      T nut = (T)0;
-      if (A.les) {
-        const T s11 = g1[0][0], s22 = g1[1][1], s33 = g1[2][2];
-        const T s12 = (T)0.5 * (g1[0][1] + g1[1][0]);
-        const T s13 = (T)0.5 * (g1[0][2] + g1[2][0]);
-        const T s23 = (T)0.5 * (g1[1][2] + g1[2][1]);
-        const T smag = sqrt((T)2 * (s11 * s11 + s22 * s22 + s33 * s33 +
-                                    (T)2 * (s12 * s12 + s13 * s13 + s23 * s23)));
-        nut = A.csd2 * smag;
-        A.nu_t[p] = nut;
-      }
-      const T nu_eff = A.onere + nut;
-      const T uc0 = q[0][3], uc1 = q[1][3], uc2 = q[2][3];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const T F = nu_eff * (g2[c][0] + g2[c][1] + g2[c][2]) -
-                    (uc0 * g1[c][0] + uc1 * g1[c][1] + uc2 * g1[c][2]);
-        T up = q[c][3] + A.adu * F;
-        if (A.f2[c]) up = up + A.bdu * h2[c];
-        if (A.f3[c]) up = up + A.cdu * h3[c];
-        A.fnew[c][p] = F;
-        A.up[c][p] = up;
-      }
-    }
-    buf ^= 1;
-  }
-}
-
-// ---------------------------------------------------------------------------
-// 2.5D divergence (src/differential_operators.f90:25-35) -> optional output
-// div*scale, with function_stats (src/functions.f90:27-63) accumulated per
-// thread over its z-column and reduced once per block.
-// ---------------------------------------------------------------------------
-template <class T, class O, int TX, int TY>
-__global__ void __launch_bounds__(TX * TY) k_div25(const T* __restrict__ fx, const T* __restrict__ fy,
-                                                   const T* __restrict__ fz, O* __restrict__ out, Grid g,
-                                                   Coef3<T> cf, int odd, T dt, int divide, StatPart* part,
-                                                   int kc) {
-  __shared__ T sx[2][TY][TX + 6];
-  __shared__ T sy[2][TY + 6][TX];
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
-  const int i = i0 + tx, j = j0 + ty;
-  const bool valid = i < g.nx && j < g.ny;
-  const int k0 = blockIdx.z * kc;
-  const int k1 = min(k0 + kc, g.nz);
-  const bool zon = g.bc[2] != AX_ZERO;
-  const int ox = odd ? 0 : -1, oy = odd ? 1 : -1, oz = odd ? 2 : -1;
-  const bool hx = tx < 3, hy = ty < 3;
-  T q[7];
-#pragma unroll
-  for (int m = 0; m < 6; ++m) q[m + 1] = zon ? ldg_map<T>(fz, g, i, j, k0 - 3 + m, oz) : (T)0;
-  // values of the next plane to stage: x-line centre and halos, y-line centre and halos
-  T cx = ldg_map<T>(fx, g, i, j, k0, ox), cy = ldg_map<T>(fy, g, i, j, k0, oy);
-  T hx0 = hx ? ldg_map<T>(fx, g, i0 - 3 + tx, j, k0, ox) : (T)0;
-  T hx1 = hx ? ldg_map<T>(fx, g, i0 + TX + tx, j, k0, ox) : (T)0;
-  T hy0 = hy ? ldg_map<T>(fy, g, i, j0 - 3 + ty, k0, oy) : (T)0;
-  T hy1 = hy ? ldg_map<T>(fy, g, i, j0 + TY + ty, k0, oy) : (T)0;
-  T mn = (T)INFINITY, mx = (T)-INFINITY;
-  long long imx = 0x7fffffffffffffffll;
-  double sum = 0.0;
-  int buf = 0;
-  for (int k = k0; k < k1; ++k) {
-#pragma unroll
-    for (int m = 0; m < 6; ++m) q[m] = q[m + 1];
-    sx[buf][ty][tx + 3] = cx;
-    sy[buf][ty + 3][tx] = cy;
-    if (hx) { sx[buf][ty][tx] = hx0; sx[buf][ty][TX + 3 + tx] = hx1; }
-    if (hy) { sy[buf][ty][tx] = hy0; sy[buf][TY + 3 + ty][tx] = hy1; }
-    q[6] = zon ? ldg_map<T>(fz, g, i, j, k + 3, oz) : (T)0;
-    const int kn = k + 1;
-    if (kn < k1) {
-      cx = ldg_map<T>(fx, g, i, j, kn, ox);
-      cy = ldg_map<T>(fy, g, i, j, kn, oy);
-      if (hx) { hx0 = ldg_map<T>(fx, g, i0 - 3 + tx, j, kn, ox); hx1 = ldg_map<T>(fx, g, i0 + TX + tx, j, kn, ox); }
-      if (hy) { hy0 = ldg_map<T>(fy, g, i, j0 - 3 + ty, kn, oy); hy1 = ldg_map<T>(fy, g, i, j0 + TY + ty, kn, oy); }
-    }
-    __syncthreads();
-    T v[7];
-#pragma unroll
-    for (int m = 0; m < 7; ++m) v[m] = sx[buf][ty][tx + m];
-    const T ddx = d1(v, cf.ax[0]);
-#pragma unroll
-    for (int m = 0; m < 7; ++m) v[m] = sy[buf][ty + m][tx];
-    const T ddy = d1(v, cf.ax[1]);
-    const T ddz = zon ? d1(q, cf.ax[2]) : (T)0;
-    const T div = ddx + ddy + ddz;
-    if (valid) {
-      const long long p = (long long)i + g.sy() * j + g.sz() * k;
-      if (out) out[p] = (O)(divide ? div / dt : div);
-      sum += (double)div;
-      if (div < mn) mn = div;
-      if (div > mx) { mx = div; imx = p; }  // k ascends: the first max of the column is kept
-    }
-    buf ^= 1;
-  }
-  if (part) {
-    StatPart st;
-    st.mn = (double)mn; st.mx = (double)mx; st.sum = sum; st.imx = imx;
-    if (!(mx >= mn)) { st.mn = INFINITY; st.mx = -INFINITY; st.imx = 0x7fffffffffffffffll; }
-    block_stat(st, part, block_linear_id());
-  }
-}
-
-// ---------------------------------------------------------------------------
-// 2.5D correct_velocity (src/integration.f90:297-325) with the per-step
-// extrema of the corrected velocity accumulated per thread.
-// ---------------------------------------------------------------------------
-template <class T, class P, int TX, int TY>
-__global__ void __launch_bounds__(TX * TY) k_correct25(CorrArgs<T, P> A, int kc) {
-  const Grid& g = A.g;
-  __shared__ T sx[2][TY][TX + 6];
-  __shared__ T sy[2][TY + 6][TX];
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
-  const int i = i0 + tx, j = j0 + ty;
-  const bool valid = i < g.nx && j < g.ny;
-  const int k0 = blockIdx.z * kc;
-  const int k1 = min(k0 + kc, g.nz);
-  const bool zon = g.bc[2] != AX_ZERO;
-  const bool hx = tx < 3, hy = ty < 3;
-  T q[7];
-#pragma unroll
-  for (int m = 0; m < 6; ++m) q[m + 1] = ldg_map<T>(A.p, g, i, j, k0 - 3 + m, -1);
-  T hx0 = hx ? ldg_map<T>(A.p, g, i0 - 3 + tx, j, k0, -1) : (T)0;
-  T hx1 = hx ? ldg_map<T>(A.p, g, i0 + TX + tx, j, k0, -1) : (T)0;
-  T hy0 = hy ? ldg_map<T>(A.p, g, i, j0 - 3 + ty, k0, -1) : (T)0;
-  T hy1 = hy ? ldg_map<T>(A.p, g, i, j0 + TY + ty, k0, -1) : (T)0;
-  T mn[3], mx[3], am[3];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) { mn[a] = (T)INFINITY; mx[a] = (T)-INFINITY; am[a] = (T)0; }
-  bool nan = false;
-  int buf = 0;
-  for (int k = k0; k < k1; ++k) {
-#pragma unroll
-    for (int m = 0; m < 6; ++m) q[m] = q[m + 1];
-    if (!zon) q[3] = ldg_map<T>(A.p, g, i, j, k, -1);
-    sx[buf][ty][tx + 3] = q[3];
-    sy[buf][ty + 3][tx] = q[3];
-    if (hx) { sx[buf][ty][tx] = hx0; sx[buf][ty][TX + 3 + tx] = hx1; }
-    if (hy) { sy[buf][ty][tx] = hy0; sy[buf][TY + 3 + ty][tx] = hy1; }
-    q[6] = ldg_map<T>(A.p, g, i, j, k + 3, -1);
-    const int kn = k + 1;
-    if (kn < k1) {
-      if (hx) { hx0 = ldg_map<T>(A.p, g, i0 - 3 + tx, j, kn, -1); hx1 = ldg_map<T>(A.p, g, i0 + TX + tx, j, kn, -1); }
-      if (hy) { hy0 = ldg_map<T>(A.p, g, i, j0 - 3 + ty, kn, -1); hy1 = ldg_map<T>(A.p, g, i, j0 + TY + ty, kn, -1); }
-    }
-    const long long p = (long long)min(i, g.nx - 1) + g.sy() * min(j, g.ny - 1) + g.sz() * k;
-    T upv[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) upv[a] = __ldg(A.up[a] + p);
-    __syncthreads();
-    T v[7], gp[3];
-#pragma unroll
-    for (int m = 0; m < 7; ++m) v[m] = sx[buf][ty][tx + m];
-    gp[0] = d1(v, A.cf.ax[0]);
-#pragma unroll
-    for (int m = 0; m < 7; ++m) v[m] = sy[buf][ty + m][tx];
-    gp[1] = d1(v, A.cf.ax[1]);
-    gp[2] = zon ? d1(q, A.cf.ax[2]) : (T)0;
-    if (valid) {
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        const T un = upv[a] - A.dt * gp[a];
-        A.u[a][p] = un;
-        if (un != un) nan = true;
-        mn[a] = fmin(mn[a], un);
-        mx[a] = fmax(mx[a], un);
-        am[a] = fmax(am[a], fabs(un));
-      }
-    }
-    buf ^= 1;
-  }
-  double r[10];
-  const int ops[10] = {RED_MIN, RED_MIN, RED_MIN, RED_MAX, RED_MAX, RED_MAX,
-                       RED_MAX, RED_MAX, RED_MAX, RED_MAX};
-#pragma unroll
-  for (int a = 0; a < 3; ++a) { r[a] = (double)mn[a]; r[3 + a] = (double)mx[a]; r[6 + a] = (double)am[a]; }
-  r[9] = nan ? 1.0 : 0.0;
-  block_reduce_store<10>(r, ops, A.part, block_linear_id());
 }
 
 // standalone calculate_nu_t (src/les_turbulence.f90:54-88)
@@ -410,82 +53,6 @@ __global__ void k_nu_t(const T* __restrict__ ux, const T* __restrict__ uy, const
   const T s23 = (T)0.5 * (g1[1][2] + g1[2][1]);
   nu_t[q] = csd2 * sqrt((T)2 * (s11 * s11 + s22 * s22 + s33 * s33 +
                                 (T)2 * (s12 * s12 + s13 * s13 + s23 * s23)));
-}
-
-// ---------------------------------------------------------------------------
-// divergence (src/differential_operators.f90:25-35); out = div * scale
-// (scale = 1/dt gives the Poisson rhs of correct_pression,
-// src/integration.f90:235-239), with function_stats of div.
-// ---------------------------------------------------------------------------
-template <class T, class O>
-__global__ void __launch_bounds__(256) k_div(const T* __restrict__ fx, const T* __restrict__ fy,
-                                             const T* __restrict__ fz, O* __restrict__ out,
-                                             Grid g, Coef3<T> cf, int odd, T dt, int divide,
-                                             StatPart* part) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
-  const bool valid = i < g.nx && j < g.ny;
-  double dv = 0.0;
-  long long q = 0;
-  if (valid) {
-    q = (long long)i + g.sy() * j + g.sz() * k;
-    const T* f[3] = {fx, fy, fz};
-    T d[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      if (g.bc[a] == AX_ZERO) { d[a] = (T)0; continue; }
-      T v[7];
-      load_line<3>(f[a], g, a, i, j, k, odd != 0, v);
-      d[a] = d1(v, cf.ax[a]);
-    }
-    const T div = d[0] + d[1] + d[2];
-    dv = (double)div;
-    if (out) out[q] = (O)(divide ? div / dt : div);
-  }
-  if (part) block_stat(stat_of(dv, q, valid), part, block_linear_id());
-}
-
-// ---------------------------------------------------------------------------
-// correct_velocity (src/integration.f90:297-325): u = u* - dt dp/dx_i with
-// the even ("p") closures, plus the per-step extrema of the corrected field
-// (NaN / overflow check, print_velocity_values, compute_cfl).
-// ---------------------------------------------------------------------------
-template <class T, class P>
-__global__ void __launch_bounds__(256) k_correct(CorrArgs<T, P> A) {
-  const Grid& g = A.g;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
-  const bool valid = i < g.nx && j < g.ny;
-  double r[10];
-  const int ops[10] = {RED_MIN, RED_MIN, RED_MIN, RED_MAX, RED_MAX, RED_MAX,
-                       RED_MAX, RED_MAX, RED_MAX, RED_MAX};
-#pragma unroll
-  for (int q = 0; q < 3; ++q) { r[q] = INFINITY; r[3 + q] = -INFINITY; r[6 + q] = 0.0; }
-  r[9] = 0.0;
-  if (valid) {
-    const long long q = (long long)i + g.sy() * j + g.sz() * k;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      T gp = (T)0;
-      if (g.bc[a] != AX_ZERO) {
-        T v[7];
-        load_line<3>(A.p, g, a, i, j, k, false, v);
-        gp = d1(v, A.cf.ax[a]);
-      }
-      const T un = A.up[a][q] - A.dt * gp;
-      A.u[a][q] = un;
-      const double d = (double)un;
-      if (d != d) r[9] = 1.0;
-      else {
-        r[a] = d;
-        r[3 + a] = d;
-        r[6 + a] = fabs(d);
-      }
-    }
-  }
-  block_reduce_store<10>(r, ops, A.part, block_linear_id());
 }
 
 // ---------------------------------------------------------------------------
@@ -657,34 +224,10 @@ void launch_der(const T* f, T* df, const Grid& g, const AxisCoef<T>& c, int axis
                 int odd, cudaStream_t s) {
   k_der<T><<<pt_grid(g), pt_block(), 0, s>>>(f, df, g, c, axis, order, odd);
 }
-constexpr int PRED_TX = 32, PRED_TY = 8, PRED_KC = 32;
-
-template <class T>
-void launch_predict(const PredArgs<T>& a, cudaStream_t s) {
-  const Grid& g = a.g;
-  dim3 grid((g.nx + PRED_TX - 1) / PRED_TX, (g.ny + PRED_TY - 1) / PRED_TY, (g.nz + PRED_KC - 1) / PRED_KC);
-  k_predict25<T, PRED_TX, PRED_TY><<<grid, dim3(PRED_TX, PRED_TY), 0, s>>>(a, PRED_KC);
-}
 template <class T>
 void launch_nu_t(const T* ux, const T* uy, const T* uz, T* nu, const Grid& g, const Coef3<T>& cf,
                  T csd2, cudaStream_t s) {
   k_nu_t<T><<<pt_grid(g), pt_block(), 0, s>>>(ux, uy, uz, nu, g, cf, csd2);
-}
-constexpr int Z_TX = 32, Z_TY = 8, Z_KC = 32;
-static inline dim3 z_grid(const Grid& g) {
-  return dim3((g.nx + Z_TX - 1) / Z_TX, (g.ny + Z_TY - 1) / Z_TY, (g.nz + Z_KC - 1) / Z_KC);
-}
-long long z_blocks(const Grid& g) { dim3 b = z_grid(g); return (long long)b.x * b.y * b.z; }
-
-template <class T, class O>
-void launch_div(const T* fx, const T* fy, const T* fz, O* out, const Grid& g, const Coef3<T>& cf,
-                int odd, T dt, int divide, StatPart* part, cudaStream_t s) {
-  k_div25<T, O, Z_TX, Z_TY><<<z_grid(g), dim3(Z_TX, Z_TY), 0, s>>>(fx, fy, fz, out, g, cf, odd, dt, divide,
-                                                                     part, Z_KC);
-}
-template <class T, class P>
-void launch_correct(const CorrArgs<T, P>& a, cudaStream_t s) {
-  k_correct25<T, P, Z_TX, Z_TY><<<z_grid(a.g), dim3(Z_TX, Z_TY), 0, s>>>(a, Z_KC);
 }
 template <class T>
 void launch_stats(const T* ux, const T* uy, const T* uz, const Grid& g, const Coef3<T>& cf,
@@ -714,7 +257,6 @@ void launch_convert(const S* s_, D* d, long long n, cudaStream_t s) {
 #define O3D_INST(T)                                                                            \
   template void launch_der<T>(const T*, T*, const Grid&, const AxisCoef<T>&, int, int, int,     \
                               cudaStream_t);                                                   \
-  template void launch_predict<T>(const PredArgs<T>&, cudaStream_t);                            \
   template void launch_nu_t<T>(const T*, const T*, const T*, T*, const Grid&, const Coef3<T>&,  \
                                T, cudaStream_t);                                               \
   template void launch_stats<T>(const T*, const T*, const T*, const Grid&, const Coef3<T>&,     \
@@ -722,14 +264,6 @@ void launch_convert(const S* s_, D* d, long long n, cudaStream_t s) {
   template void launch_transeq<T>(const ScalArgs<T>&, const double*, cudaStream_t, long long*);
 O3D_INST(double)
 O3D_INST(float)
-template void launch_div<double, double>(const double*, const double*, const double*, double*,
-                                         const Grid&, const Coef3<double>&, int, double, int,
-                                         StatPart*, cudaStream_t);
-template void launch_div<float, float>(const float*, const float*, const float*, float*,
-                                       const Grid&, const Coef3<float>&, int, float, int,
-                                       StatPart*, cudaStream_t);
-template void launch_correct<double, double>(const CorrArgs<double, double>&, cudaStream_t);
-template void launch_correct<float, double>(const CorrArgs<float, double>&, cudaStream_t);
 template void launch_convert<double, float>(const double*, float*, long long, cudaStream_t);
 template void launch_convert<float, double>(const float*, double*, long long, cudaStream_t);
 

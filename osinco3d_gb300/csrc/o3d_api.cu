@@ -419,6 +419,10 @@ int capture_sor(o3d_ctx* c) {
   return O3D_OK;
 }
 
+// red-black sweeps of the coarsest multigrid level when it is too large
+// for the one-block shared-memory solve
+constexpr int MG_COARSE_SWEEPS = 40;
+
 int mg_smooth_cfg(const o3d_ctx* c, int* pre, int* post) {
   // the plain FP64 method is the V(2,2) Gauss-Seidel cycle; the mixed one
   // defaults to V(2,1) over-relaxed (fewer FP32 sweeps per FP64 residual)
@@ -441,7 +445,7 @@ int capture_mg(o3d_ctx* c) {
   c->mg_batch = 2;
   int pre, post;
   mg_smooth_cfg(c, &pre, &post);
-  const int coarse_sweeps = 40;
+  const int coarse_sweeps = MG_COARSE_SWEEPS;
   long long nl = 0;
   cudaGraph_t graph;
   CK(cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal));
@@ -508,6 +512,10 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
     int st0 = dalloc(c->s, (void**)&c->pp_prev, (size_t)c->g.n * 8);
     if (st0) return st0;
   }
+  if (sampling && (c->P.solver != O3D_SOLVER_MG || (guess != O3D_GUESS_EXTRAPOLATED && !learned))) {
+    errf("training samples come from multigrid solves with the extrapolated or learned guess");
+    return O3D_ERR_BADARG;
+  }
   if ((learned || sampling)) {
     int st0 = learn_ready(c);
     if (st0) return st0;
@@ -523,34 +531,53 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
     CKL();
   }
   c->sample_ready = 0;
+  int pre = 2, post = 2;
+  mg_smooth_cfg(c, &pre, &post);
+  if (use_mg) {
+    if ((st = capture_mg(c))) return st;
+  } else {
+    if ((st = capture_sor(c))) return st;
+  }
   if (need_hist) {
     if (c->pp_prev_valid && (learned || sampling)) {
-      // features from p(n), p(n-1) and the rhs; then p(n-1) <- p(n)
-      if (c->mixed)
-        launch_learn_features<float, float>(c->pp, c->pp_prev, (const float*)c->rhs, c->mg.data(), c->learn_level,
-                                            c->ctrl, c->feat, c->s, &c->launches);
-      else
-        launch_learn_features<double, double>(c->pp, c->pp_prev, (const double*)c->rhs, c->mg.data(),
-                                              c->learn_level, c->ctrl, c->feat, c->s, &c->launches);
-      CKL();
-      if (guess == O3D_GUESS_EXTRAPOLATED) {
-        launch_extrapolate(c->pp, c->pp_prev, c->g.n, c->s);  // also sets p(n-1) <- p(n)
-        c->launches++;
-        CKL();
+      // p <- p_ex = 2 p(n) - p(n-1), p(n-1) <- p(n), increment into the finest t;
+      // the FP64 residual of p_ex (the first outer iteration's, for multigrid)
+      // and the increment, restricted, are the network's input
+      const int ll = c->learn_level;
+      MGLevel* lv = c->mg.data();
+      if (c->mixed) launch_learn_extrapolate<float>(c->pp, c->pp_prev, lv, c->s, &c->launches);
+      else launch_learn_extrapolate<double>(c->pp, c->pp_prev, lv, c->s, &c->launches);
+      if (use_mg) {
+        if (c->mixed) launch_mg_resid<float, float>(c->pp, (const float*)c->rhs, lv, c->ctrl, c->s, &c->launches);
+        else launch_mg_resid<double, double>(c->pp, (const double*)c->rhs, lv, c->ctrl, c->s, &c->launches);
       } else {
-        CK(cudaMemcpyAsync(c->pp_prev, c->pp, (size_t)c->g.n * 8, cudaMemcpyDeviceToDevice, c->s));
+        if (c->mixed) launch_level_kernel<float, float>(1, c->pp, (const float*)c->rhs, lv[0], c->ctrl, c->s);
+        else launch_level_kernel<double, double>(1, c->pp, (const double*)c->rhs, lv[0], c->ctrl, c->s);
+        c->launches++;
       }
+      if (c->mixed) launch_learn_features<float>(lv, ll, c->ctrl, c->feat, c->s, &c->launches);
+      else launch_learn_features<double>(lv, ll, c->ctrl, c->feat, c->s, &c->launches);
+      CKL();
       if (sampling) {
-        CK(cudaMemcpyAsync(c->sample_feat, c->feat, (size_t)c->mg[c->learn_level].g.n * 2 * sizeof(float),
+        CK(cudaMemcpyAsync(c->sample_feat, c->feat, (size_t)c->mg[ll].g.n * 2 * sizeof(float),
                            cudaMemcpyDeviceToDevice, c->s));
         c->sample_ready = 1;
       }
       if (learned) {
         if ((st = unet_forward(c->unet, c->feat, c->ynet, c->s))) return st;
+        if (c->mixed) launch_learn_apply<float>(c->pp, c->ynet, lv, ll, !use_mg, c->ctrl, c->s, &c->launches);
+        else launch_learn_apply<double>(c->pp, c->ynet, lv, ll, !use_mg, c->ctrl, c->s, &c->launches);
+        CKL();
+      }
+      if (use_mg) {  // the rest of the first outer iteration, from the network's correction when learned
+        const int cyc = mg_cycles_of(c);
+        const double om = mg_omega_of(c);
         if (c->mixed)
-          launch_learn_apply<float>(c->pp, c->ynet, c->mg.data(), c->learn_level, c->ctrl, c->s, &c->launches);
+          launch_mg_cycles<float>(c->pp, lv, (int)c->mg.size(), pre, post, MG_COARSE_SWEEPS, (float)om, cyc, learned,
+                                  c->ctrl, c->s, &c->launches);
         else
-          launch_learn_apply<double>(c->pp, c->ynet, c->mg.data(), c->learn_level, c->ctrl, c->s, &c->launches);
+          launch_mg_cycles<double>(c->pp, lv, (int)c->mg.size(), pre, post, MG_COARSE_SWEEPS, om, cyc, learned,
+                                   c->ctrl, c->s, &c->launches);
         CKL();
       }
     } else if (c->pp_prev_valid && guess == O3D_GUESS_EXTRAPOLATED) {
@@ -562,11 +589,6 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
       CK(cudaMemcpyAsync(c->pp_prev, c->pp, (size_t)c->g.n * 8, cudaMemcpyDeviceToDevice, c->s));
       c->pp_prev_valid = 1;
     }
-  }
-  if (use_mg) {
-    if ((st = capture_mg(c))) return st;
-  } else {
-    if ((st = capture_sor(c))) return st;
   }
   for (;;) {
     if (use_mg) {
@@ -581,12 +603,13 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
   }
   if (c->sample_ready && c->sample_tgt) {
     CK(cudaMemsetAsync(&c->ctrl->done, 0, sizeof(int), c->s));
+    const long long n2 = c->mg[c->learn_level].g.n;
     if (c->mixed)
-      launch_learn_target<float>(c->pp, c->pp_prev, c->mg.data(), c->learn_level, c->ctrl, c->sample_tgt, c->s,
-                                 &c->launches);
+      launch_learn_target<float>(c->pp, c->pp_prev, c->mg.data(), c->learn_level, c->ctrl, c->feat + n2,
+                                 c->sample_tgt, c->s, &c->launches);
     else
-      launch_learn_target<double>(c->pp, c->pp_prev, c->mg.data(), c->learn_level, c->ctrl, c->sample_tgt, c->s,
-                                  &c->launches);
+      launch_learn_target<double>(c->pp, c->pp_prev, c->mg.data(), c->learn_level, c->ctrl, c->feat + n2,
+                                  c->sample_tgt, c->s, &c->launches);
     CKL();
     CK(cudaMemsetAsync(&c->ctrl->done, 0xff, sizeof(int), c->s));
   }

@@ -82,6 +82,47 @@ __device__ __forceinline__ int ghost(int m, int n, int bc, bool* flip) {
 template <class T>
 __device__ __forceinline__ T ld(const T* __restrict__ p, long long i) { return __ldg(p + i); }
 
+// ---- binary64 <-> binary32 conversions on the integer pipe ---------------
+// GB300 executes FP64 instructions (conversions included) at 2 lanes per
+// clock per SM, so a kernel that converts every point is bound by them.
+// These convert by the IEEE 754 binary formats themselves: rebias the
+// exponent (1023 <-> 127) and move the fraction, rounding the 29 dropped
+// fraction bits to nearest, ties to even (roundTiesToEven, IEEE 754-2008
+// 4.3.1).  Zeros and normal numbers take the integer path; subnormal,
+// infinite, NaN and out-of-range values fall back to the FP64 instruction.
+// Results are bit-identical to __double2float_rn and to the exact widening.
+__device__ __forceinline__ float f64_to_f32(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const unsigned e = (hi >> 20) & 0x7ffu;          // biased binary64 exponent
+  const unsigned sign = hi & 0x80000000u;
+  if (e - 897u <= 253u) {                          // binary32 exponent 1..254
+    unsigned f = ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const unsigned rem = lo & 0x1fffffffu;         // the 29 dropped fraction bits
+    f += (rem > 0x10000000u || (rem == 0x10000000u && (f & 1u))) ? 1u : 0u;  // carries into the exponent
+    return __uint_as_float(sign | f);
+  }
+  if (((hi << 1) | lo) == 0u) return __uint_as_float(sign);  // +-0
+  return __double2float_rn(x);
+}
+
+__device__ __forceinline__ double f32_to_f64(float x) {
+  const unsigned u = __float_as_uint(x);
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e - 1u <= 253u)                              // normal: exact widening
+    return __hiloint2double((int)((u & 0x80000000u) | ((e + 896u) << 20) | ((u >> 3) & 0xfffffu)), (int)(u << 29));
+  if ((u << 1) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);  // +-0
+  return (double)x;
+}
+
+// conversion of a loaded value to the compute type
+template <class T, class S>
+__device__ __forceinline__ T to_t(S v) { return (T)v; }
+template <>
+__device__ __forceinline__ float to_t<float, double>(double v) { return f64_to_f32(v); }
+template <>
+__device__ __forceinline__ double to_t<double, float>(float v) { return f32_to_f64(v); }
+
 // Loads f at offsets -R..R along axis `a` of point (i,j,k) into v[0..2R].
 // Interior points take the fast path; points within R of an end use ghost().
 template <int R, class T, class S>

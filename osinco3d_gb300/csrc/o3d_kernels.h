@@ -124,22 +124,30 @@ void launch_sor_fixed(double* p, const double* rhs, const Grid& g, const PoiCoef
                       double omega, SolveCtrl* ctrl, cudaStream_t s);
 
 // Multigrid: T is the arithmetic of the cycles, R the type of the top rhs.
+// One outer iteration = launch_mg_resid (FP64 residual into the finest
+// level's r) + launch_mg_cycles (V-cycles, p += e, stop test).
 template <class T, class R>
 void launch_mg_outer(double* p, const R* rhs, MGLevel* lv, int nlev, int pre, int post,
                      int coarse_sweeps, T smooth_omega, int cycles, SolveCtrl* ctrl, cudaStream_t s,
                      long long* nl);
+template <class T, class R>
+void launch_mg_resid(double* p, const R* rhs, MGLevel* lv, SolveCtrl* ctrl, cudaStream_t s, long long* nl);
+template <class T>
+void launch_mg_cycles(double* p, MGLevel* lv, int nlev, int pre, int post, int coarse_sweeps, T smooth_omega,
+                      int cycles, bool from_e, SolveCtrl* ctrl, cudaStream_t s, long long* nl);
 void launch_extrapolate(double* p, double* pprev, long long n, cudaStream_t s);
 
 // learned warm start: the network works on multigrid level ll
-template <class T, class R>
-void launch_learn_features(double* p, const double* pprev, const R* rhs, MGLevel* lv, int ll, SolveCtrl* ctrl,
-                           float* feat, cudaStream_t s, long long* nl);
 template <class T>
-void launch_learn_apply(double* p, const float* y, MGLevel* lv, int ll, SolveCtrl* ctrl, cudaStream_t s,
-                        long long* nl);
+void launch_learn_extrapolate(double* p, double* pprev, MGLevel* lv, cudaStream_t s, long long* nl);
 template <class T>
-void launch_learn_target(const double* p, const double* pprev, MGLevel* lv, int ll, SolveCtrl* ctrl, float* tgt,
-                         cudaStream_t s, long long* nl);
+void launch_learn_features(MGLevel* lv, int ll, SolveCtrl* ctrl, float* feat, cudaStream_t s, long long* nl);
+template <class T>
+void launch_learn_apply(double* p, const float* y, MGLevel* lv, int ll, bool add_to_p, SolveCtrl* ctrl,
+                        cudaStream_t s, long long* nl);
+template <class T>
+void launch_learn_target(const double* p, const double* pprev, MGLevel* lv, int ll, SolveCtrl* ctrl,
+                         const float* ch1, float* tgt, cudaStream_t s, long long* nl);
 
 // one finest-level kernel for timing: 0 smoother (one sweep), 1 FP64 residual
 template <class T, class R>

@@ -54,6 +54,8 @@ struct UNet {
   float* ws = nullptr;                // split-K partials of the convolutions
   long long ws_cap = 0;
   cudaStream_t s = nullptr;
+  cudaEvent_t ev = nullptr;           // orders the forward pass after / before a caller's stream
+  cudaGraphExec_t fwd_exec = nullptr; // the forward pass as one graph (inference)
   std::vector<void*> allocs;
 };
 
@@ -171,6 +173,25 @@ static void forward(UNet& u) {
     conv(u, u.dec_b[l], u.da[l], u.d[l], true);
   }
   launch_head(u.d[0].p, u.d[0].cs, ch(u, 0), nvox(u.vol[0]), u.w + u.head_w, u.w + u.head_b, u.out, u.s);
+}
+
+// the forward pass replayed from a graph captured on first use (the
+// buffers and weights keep their addresses; o3d_unet_set_params repacks in
+// place), which removes the launch gaps between its ~30 small kernels
+static int forward_graph(UNet& u) {
+  if (!u.fwd_exec) {
+    cudaGraph_t g;
+    if (cudaStreamBeginCapture(u.s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return O3D_ERR_CUDA;
+    forward(u);
+    if (cudaStreamEndCapture(u.s, &g) != cudaSuccess) return O3D_ERR_CUDA;
+    const cudaError_t e = cudaGraphInstantiate(&u.fwd_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      u.fwd_exec = nullptr;
+      return O3D_ERR_CUDA;
+    }
+  }
+  return cudaGraphLaunch(u.fwd_exec, u.s) == cudaSuccess ? O3D_OK : O3D_ERR_CUDA;
 }
 
 // gradients of the loss in u.dout with respect to every parameter, into u.g
@@ -362,9 +383,11 @@ int o3d_unet_create(int nx, int ny, int nz, const int periodic[3], int base_chan
   }
   o3d_unet* n = new (std::nothrow) o3d_unet();
   if (!n) return O3D_ERR_NOMEM;
-  if (cudaStreamCreateWithFlags(&n->u.s, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaStreamCreateWithFlags(&n->u.s, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&n->u.ev, cudaEventDisableTiming) != cudaSuccess) {
+    if (n->u.s) cudaStreamDestroy(n->u.s);
     delete n;
-    set_error("U-Net: cudaStreamCreate failed");
+    set_error("U-Net: stream or event creation failed");
     return O3D_ERR_CUDA;
   }
   int st = o3d::build(n->u, nx, ny, nz, periodic, base_channels, levels, in_channels, seed);
@@ -380,6 +403,8 @@ int o3d_unet_create(int nx, int ny, int nz, const int periodic[3], int base_chan
 int o3d_unet_destroy(o3d_unet* n) {
   if (!n) return O3D_OK;
   if (n->u.s) cudaStreamSynchronize(n->u.s);
+  if (n->u.fwd_exec) cudaGraphExecDestroy(n->u.fwd_exec);
+  if (n->u.ev) cudaEventDestroy(n->u.ev);
   for (void* p : n->u.allocs) cudaFree(p);
   if (n->u.s) cudaStreamDestroy(n->u.s);
   delete n;
@@ -411,19 +436,20 @@ int o3d_unet_set_params(o3d_unet* n, const float* host) {
 int o3d_unet_forward_dev(o3d_unet* n, const float* d_in, float* d_out, void* wait) {
   if (!n || !d_in || !d_out) return O3D_ERR_BADARG;
   UNet& u = n->u;
-  cudaEvent_t ev = nullptr;
   if (wait) {
-    cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
-    cudaEventRecord(ev, (cudaStream_t)wait);
-    cudaStreamWaitEvent(u.s, ev, 0);
+    cudaEventRecord(u.ev, (cudaStream_t)wait);
+    cudaStreamWaitEvent(u.s, u.ev, 0);
   }
   launch_pack_input(d_in, u.in_ch, nvox(u.vol[0]), u.xin.p, 16, u.s);
-  forward(u);
+  int st = forward_graph(u);
+  if (st) {
+    set_error("U-Net forward graph: %s", cudaGetErrorString(cudaGetLastError()));
+    return st;
+  }
   cudaMemcpyAsync(d_out, u.out, nvox(u.vol[0]) * 4, cudaMemcpyDeviceToDevice, u.s);
   if (wait) {
-    cudaEventRecord(ev, u.s);
-    cudaStreamWaitEvent((cudaStream_t)wait, ev, 0);
-    cudaEventDestroy(ev);
+    cudaEventRecord(u.ev, u.s);
+    cudaStreamWaitEvent((cudaStream_t)wait, u.ev, 0);
   }
   return check_last("U-Net forward");
 }

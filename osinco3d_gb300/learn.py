@@ -1,10 +1,11 @@
 """Training data, training and evaluation of the learned Poisson warm start.
 
-The network maps the restricted residual of the previous pressure and the
-last pressure increment to the next increment (see o3d.h, "learned Poisson
-warm start").  Samples come from the solver itself: a context with sample
-buffers writes (features, target) for every solve that has a previous
-pressure.  Training runs the library's own BF16 forward/backward kernels and
+The network maps the restricted FP64 residual of the extrapolated pressure
+p_ex = 2 p^n - p^(n-1) and the last pressure increment to the coarse part of
+the remaining correction p^(n+1) - p_ex (see o3d.h, "learned Poisson warm
+start").  Samples come from the solver itself: a multigrid context with the
+extrapolated (or learned) guess and sample buffers writes (features,
+target) for every solve that has a previous pressure.  Training runs the library's own BF16 forward/backward kernels and
 Adam (o3d_unet_train_step); PyTorch only holds the device buffers.
 
   python -m osinco3d_gb300.learn train --n 128 --runs 8 --steps 150 --epochs 6 --out weights.npz
@@ -53,7 +54,8 @@ def generate(n: int, runs: int, steps: int, seed: int = 0, re_range=(800.0, 3000
     for r in range(runs):
         re = float(rng.uniform(*re_range))
         amp = float(rng.uniform(*noise))
-        p = o3d.tgv_params(n, re=re, precision=o3d.PREC_MIXED, solver=o3d.SOLVER_MG, eps=1e-8, kmax=100)
+        p = o3d.tgv_params(n, re=re, precision=o3d.PREC_MIXED, solver=o3d.SOLVER_MG, eps=1e-8, kmax=100,
+                           guess=o3d.GUESS_EXTRAPOLATED)
         with o3d.Context(p) as ctx:
             dims = ctx.guess_grid()
             n2 = dims[0] * dims[1] * dims[2]

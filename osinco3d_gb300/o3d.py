@@ -126,6 +126,7 @@ def lib(build_if_missing: bool = True):
             "o3d_statistics_calc": (C.c_int, [vp, C.c_double, _dp]),
             "o3d_rbsor_sweeps_dev": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, _dp]),
             "o3d_time_kernel": (C.c_int, [vp, C.c_int, C.c_int, _dp]),
+            "o3d_check_conversions": (C.c_int, [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)]),
             "o3d_unet_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), C.c_int, C.c_int,
                                           C.c_int, C.c_ulonglong, C.POINTER(vp)]),
             "o3d_unet_destroy": (C.c_int, [vp]),
@@ -387,6 +388,17 @@ class UNet:
             self.close()
         except Exception:
             pass
+
+
+def check_conversions(n: int = 1 << 24, seed: int = 1) -> int:
+    """Mismatches of the integer-pipe FP64 <-> FP32 conversions against the
+    conversion instructions over n seeded bit patterns (0 expected)."""
+    L = lib()
+    bad = C.c_longlong(-1)
+    st = L.o3d_check_conversions(n, seed, C.byref(bad))
+    if st < 0:
+        raise O3DError(st, L.o3d_last_error().decode())
+    return bad.value
 
 
 def divergence_stats_noalloc(d_fx: int, d_fy: int, d_fz: int, d_div: int | None, shape, spacing, bcs,

@@ -131,3 +131,11 @@ def test_golden_row0_on_gpu(oracle, o3d):
         got = ctx.statistics_calc(0.0)
     nz = gold != 0
     assert (np.abs(got[nz] - gold[nz]) / np.abs(gold[nz])).max() < 2e-12
+
+
+def test_integer_pipe_conversions_are_bit_exact(o3d):
+    """The FP64 <-> FP32 conversions the kernels do with integer arithmetic
+    (round to nearest even) equal the conversion instructions bit for bit,
+    over raw patterns, widened-and-nudged binary32 values, exact ties and the
+    edges of the binary32 normal range."""
+    assert o3d.check_conversions(1 << 24, seed=7) == 0
