@@ -203,13 +203,14 @@ O3D_API int o3d_statistics_calc(o3d_ctx *ctx, double t, double out[17]);
  * extrapolated pressure p_ex = 2 p(n) - p(n-1).  Its input, on the multigrid
  * level ll of o3d_guess_grid (the pressure grid coarsened 1 to 3 times, at
  * least 16 points per axis): the restricted FP64 residual of p_ex times
- * h_ll^2, and the restricted last increment p(n) - p(n-1), both divided by
- * S = rms of the restricted increment.  Its output y predicts
- * restrict(p(n+1) - p_ex) / S.  The correction prolong(S y) starts the first
- * V-cycle of the multigrid solve (the residual already computed is reused),
- * or is added to p_ex before SOR; the solver then iterates to eps as
- * usual, so the converged pressure does not depend on the network.  No
- * counterpart in the reference. */
+ * h_ll^2, divided by its rms S_r, and the restricted last increment
+ * p(n) - p(n-1), divided by its rms.  Its output y predicts
+ * restrict(p(n+1) - p_ex) / S_r, mean removed (the solver leaves the
+ * constant of the singular operator free).  The correction prolong(S_r y)
+ * starts the first V-cycle of the multigrid solve (the residual already
+ * computed is reused), or is added to p_ex before SOR; the solver then
+ * iterates to eps as usual, so the converged pressure does not depend on
+ * the network.  No counterpart in the reference. */
 typedef struct o3d_unet o3d_unet;
 /* nx, ny, nz: the network grid (that of o3d_guess_grid); periodic[a] = 1
  * wraps axis a in the convolutions; base_channels (16) doubles per level. */
@@ -235,7 +236,8 @@ O3D_API int o3d_attach_unet(o3d_ctx *ctx, o3d_unet *net);
 /* Training data: with device buffers set (features 2 x n, target n on the
  * guess grid), every multigrid solve with the extrapolated or learned guess
  * that has a previous pressure writes the network input before and the
- * target, restrict(p(n+1) - p_ex) / S, after (O3D_ERR_BADARG otherwise). */
+ * target, restrict(p(n+1) - p_ex) / S_r with its mean removed, after
+ * (O3D_ERR_BADARG otherwise). */
 O3D_API int o3d_set_sample_buffers(o3d_ctx *ctx, float *d_feat, float *d_tgt);
 /* 1 when the last solve wrote a sample */
 O3D_API int o3d_sample_ready(const o3d_ctx *ctx);

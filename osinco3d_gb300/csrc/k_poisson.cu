@@ -609,55 +609,75 @@ __global__ void k_extrapolate_d(double* __restrict__ p, double* __restrict__ ppr
 // learned warm start plumbing.  The network works on multigrid level ll
 // (coarsened ll times on every axis).  Its input, for the extrapolated
 // pressure p_ex = 2 p^n - p^(n-1): channel 0 = restrict(rhs - mean - A p_ex)
-// h_ll^2 / S, channel 1 = restrict(p^n - p^(n-1)) / S, with S the rms of the
-// restricted increment; its output y predicts restrict(p^(n+1) - p_ex) / S.
-// The correction prolong(S y) starts the first V-cycle (multigrid) or is
-// added to p (SOR).
+// h_ll^2 / S_r, channel 1 = restrict(p^n - p^(n-1)) / S_d, each scaled by
+// its own rms; its output y predicts restrict(p^(n+1) - p_ex) / S_r with
+// the mean removed (a constant is in the null space of the periodic and
+// mirror operators: the solver leaves it arbitrary).  The correction
+// prolong(S_r y) starts the first V-cycle (multigrid) or is added to p
+// (SOR).
 // ---------------------------------------------------------------------------
-// learn_scale = sqrt(mean(d^2)) over the coarse grid (one block)
+// S_r = rms(r h^2), S_d = rms(d) over the coarse grid (one block)
 template <class T>
-__global__ void k_rms(const T* __restrict__ d, long long n, SolveCtrl* ctrl) {
-  __shared__ double sh[1024];
-  double a = 0.0;
+__global__ void k_rms(const T* __restrict__ r, const T* __restrict__ d, long long n, double h2, SolveCtrl* ctrl) {
+  __shared__ double sh[2][1024];
+  double a = 0.0, b = 0.0;
   for (long long q = threadIdx.x; q < n; q += blockDim.x) {
-    const double v = (double)d[q];
-    a += v * v;
+    const double rv = (double)r[q] * h2, dv = (double)d[q];
+    a += rv * rv;
+    b += dv * dv;
   }
-  sh[threadIdx.x] = a;
+  sh[0][threadIdx.x] = a;
+  sh[1][threadIdx.x] = b;
   __syncthreads();
   for (int st = blockDim.x / 2; st > 0; st >>= 1) {
-    if ((int)threadIdx.x < st) sh[threadIdx.x] += sh[threadIdx.x + st];
+    if ((int)threadIdx.x < st) {
+      sh[0][threadIdx.x] += sh[0][threadIdx.x + st];
+      sh[1][threadIdx.x] += sh[1][threadIdx.x + st];
+    }
     __syncthreads();
   }
-  if (threadIdx.x == 0) ctrl->learn_scale = sqrt(sh[0] / (double)n) + 1e-30;
+  if (threadIdx.x == 0) {
+    ctrl->learn_scale = sqrt(sh[0][0] / (double)n) + 1e-300;
+    ctrl->learn_scale_d = sqrt(sh[1][0] / (double)n) + 1e-300;
+  }
 }
 
-// network input: channel 0 = r * h^2 / S, channel 1 = d / S (FP32, channel-major)
+// network input: channel 0 = r h^2 / S_r, channel 1 = d / S_d (FP32, channel-major)
 template <class T>
 __global__ void k_features(const T* __restrict__ r, const T* __restrict__ d, long long n, double h2,
                            const SolveCtrl* ctrl, float* __restrict__ feat) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
-  const double inv = 1.0 / ctrl->learn_scale;
-  feat[q] = (float)((double)r[q] * h2 * inv);
-  feat[n + q] = (float)((double)d[q] * inv);
+  feat[q] = (float)((double)r[q] * h2 / ctrl->learn_scale);
+  feat[n + q] = (float)((double)d[q] / ctrl->learn_scale_d);
 }
 
-// coarse correction e = S * y
+// coarse correction e = S_r * y
 template <class T>
 __global__ void k_unscale(const float* __restrict__ y, long long n, const SolveCtrl* ctrl, T* __restrict__ e) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q < n) e[q] = (T)((double)y[q] * ctrl->learn_scale);
 }
 
-// training target t = dp / S - ch1 (dp = restrict(p^(n+1) - p^n), ch1 = the
-// increment channel of the input): restrict(p^(n+1) - p_ex) / S, restriction
-// being linear
+// training target (one block): w = dp - S_d ch1 = restrict(p^(n+1) - p_ex)
+// (dp = restrict(p^(n+1) - p^n), ch1 = the increment channel of the input,
+// restriction being linear), t = (w - mean w) / S_r
 template <class T>
 __global__ void k_target(const T* __restrict__ dp, long long n, const SolveCtrl* ctrl, const float* __restrict__ ch1,
                          float* __restrict__ t) {
-  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q < n) t[q] = (float)((double)dp[q] / ctrl->learn_scale - (double)ch1[q]);
+  __shared__ double sh[1024];
+  const double sd = ctrl->learn_scale_d;
+  double a = 0.0;
+  for (long long q = threadIdx.x; q < n; q += blockDim.x) a += (double)dp[q] - sd * (double)ch1[q];
+  sh[threadIdx.x] = a;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if ((int)threadIdx.x < st) sh[threadIdx.x] += sh[threadIdx.x + st];
+    __syncthreads();
+  }
+  const double mean = sh[0] / (double)n, inv = 1.0 / ctrl->learn_scale;
+  for (long long q = threadIdx.x; q < n; q += blockDim.x)
+    t[q] = (float)(((double)dp[q] - sd * (double)ch1[q] - mean) * inv);
 }
 
 // d = p - pprev in T
@@ -708,8 +728,8 @@ void launch_learn_features(MGLevel* lv, int ll, SolveCtrl* ctrl, float* feat, cu
   const T* rc = restrict_to<T>(lv, ll, (const T*)lv[0].r, 0, ctrl, s, nl);
   const T* dc = restrict_to<T>(lv, ll, (const T*)lv[0].t, 1, ctrl, s, nl);
   const long long n2 = lv[ll].g.n;
-  k_rms<T><<<1, 1024, 0, s>>>(dc, n2, ctrl);
   const double h2 = lv[ll].h[0] * lv[ll].h[0];
+  k_rms<T><<<1, 1024, 0, s>>>(rc, dc, n2, h2, ctrl);
   k_features<T><<<b256(n2), 256, 0, s>>>(rc, dc, n2, h2, ctrl, feat);
   *nl += 2;
 }
@@ -748,7 +768,7 @@ void launch_learn_target(const double* p, const double* pprev, MGLevel* lv, int 
   const MGLevel& L0 = lv[0];
   k_pdiff<T><<<b256(L0.g.n), 256, 0, s>>>(p, pprev, (T*)L0.t, L0.g.n);
   const T* dc = restrict_to<T>(lv, ll, (const T*)L0.t, 1, ctrl, s, nl);
-  k_target<T><<<b256(lv[ll].g.n), 256, 0, s>>>(dc, lv[ll].g.n, ctrl, ch1, tgt);
+  k_target<T><<<1, 1024, 0, s>>>(dc, lv[ll].g.n, ctrl, ch1, tgt);
   *nl += 2;
 }
 

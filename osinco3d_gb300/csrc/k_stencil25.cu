@@ -163,7 +163,7 @@ struct PredRing {
   T hist[PD + 1][6][NC];  // f2 of u, v, w then f3 of u, v, w at the centre cells
 };
 
-template <class T, int TX, int TY, bool LES>
+template <class T, int TX, int TY, bool LES, bool ZON>
 __global__ void __launch_bounds__(TX * TY, sizeof(T) == 4 ? 3 : 1) k_predict25(PredArgs<T> A, int kc) {
   using Ring = PredRing<T, TX, TY>;
   constexpr int SW = Ring::SW;
@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(TX * TY, sizeof(T) == 4 ? 3 : 1) k_predict25(P
   const bool valid = i < g.nx && j < g.ny;
   const int k0 = blockIdx.z * kc;
   const int np = min(kc, g.nz - k0);
-  const bool zon = g.bc[2] != AX_ZERO;
+  constexpr bool zon = ZON;  // z derivatives (false: 2D, derz_2dsim)
   const bool may_flip = g.bc[0] == AX_MIRROR || g.bc[1] == AX_MIRROR || g.bc[2] == AX_MIRROR;
   const XYCell cc = xy_cell(g, i, j);
   const Halo<TX, TY> h = halo_cell<TX, TY>(g, i0, j0, t);
@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(TX * TY, sizeof(T) == 4 ? 3 : 1) k_predict25(P
     for (int m = 0; m < ZQ; ++m) q[c][m] = (T)0;
 #pragma unroll
   for (int lp = 0; lp < PD + 3; ++lp) issue(lp, lp);
-  if (zon) {  // planes -3..-1 through the registers into slots 0..2
+  if constexpr (zon) {  // planes -3..-1 through the registers into slots 0..2
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
       const ZPlane z = z_plane(g, k0 - 3 + m);
@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(TX * TY, sizeof(T) == 4 ? 3 : 1) k_predict25(P
         fix(lp + 3, (u + 3) % ZQ);
         __syncthreads();
         issue(lp + 3 + PD, (u + 3 + PD) % ZQ);
-        if (zon) {
+        if constexpr (zon) {
 #pragma unroll
           for (int c = 0; c < 3; ++c) q[c][(u + 6) % ZQ] = sm.tile[(u + 3) % ZQ][c][sc];
         }
@@ -343,7 +343,7 @@ struct DivRing {
   T sz[ZQ][NC];
 };
 
-template <class T, class O, int TX, int TY>
+template <class T, class O, int TX, int TY, bool ZON>
 __global__ void __launch_bounds__(TX * TY) k_div25(const T* __restrict__ fx, const T* __restrict__ fy,
                                                    const T* __restrict__ fz, O* __restrict__ out, Grid g,
                                                    Coef3<T> cf, int odd, T dt, int divide, StatPart* part,
@@ -358,7 +358,7 @@ __global__ void __launch_bounds__(TX * TY) k_div25(const T* __restrict__ fx, con
   const bool valid = i < g.nx && j < g.ny;
   const int k0 = blockIdx.z * kc;
   const int np = min(kc, g.nz - k0);
-  const bool zon = g.bc[2] != AX_ZERO;
+  constexpr bool zon = ZON;  // z derivatives (false: 2D, derz_2dsim)
   const bool may_flip = odd && (g.bc[0] == AX_MIRROR || g.bc[1] == AX_MIRROR || g.bc[2] == AX_MIRROR);
   const int ox = odd ? 0 : -1, oy = odd ? 1 : -1, oz = odd ? 2 : -1;
   const XYCell cc = xy_cell(g, i, j);
@@ -398,7 +398,7 @@ __global__ void __launch_bounds__(TX * TY) k_div25(const T* __restrict__ fx, con
   for (int m = 0; m < ZQ; ++m) q[m] = (T)0;
 #pragma unroll
   for (int lp = 0; lp < PD + 3; ++lp) issue(lp, lp);
-  if (zon) {
+  if constexpr (zon) {
 #pragma unroll
     for (int m = 0; m < 3; ++m) q[m] = ldc<T>(fz, cc, z_plane(g, k0 - 3 + m), oz);
   }
@@ -468,7 +468,7 @@ struct CorrRing {
   T up[PD + 1][3][NC];
 };
 
-template <class T, class S, int TX, int TY>
+template <class T, class S, int TX, int TY, bool ZON>
 __global__ void __launch_bounds__(TX * TY) k_correct25(CorrArgs<T, S> A, int kc) {
   using Ring = CorrRing<T, S, TX, TY>;
   constexpr int SW = Ring::SW;
@@ -482,7 +482,7 @@ __global__ void __launch_bounds__(TX * TY) k_correct25(CorrArgs<T, S> A, int kc)
   const bool valid = i < g.nx && j < g.ny;
   const int k0 = blockIdx.z * kc;
   const int np = min(kc, g.nz - k0);
-  const bool zon = g.bc[2] != AX_ZERO;
+  constexpr bool zon = ZON;  // z derivatives (false: 2D, derz_2dsim)
   const XYCell cc = xy_cell(g, i, j);
   const Halo<TX, TY> h = halo_cell<TX, TY>(g, i0, j0, t);
   const int sc = (ty + 3) * SW + tx + 3;
@@ -522,7 +522,7 @@ __global__ void __launch_bounds__(TX * TY) k_correct25(CorrArgs<T, S> A, int kc)
   for (int m = 0; m < ZQ; ++m) q[m] = (T)0;
 #pragma unroll
   for (int lp = 0; lp < PD + 3; ++lp) issue(lp, lp);
-  if (zon) {
+  if constexpr (zon) {
 #pragma unroll
     for (int m = 0; m < 3; ++m) q[m] = ldc<T>(A.p, cc, z_plane(g, k0 - 3 + m), -1);
   }
@@ -589,35 +589,52 @@ __global__ void __launch_bounds__(TX * TY) k_correct25(CorrArgs<T, S> A, int kc)
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
-template <class T, bool LES>
+template <class T, bool LES, bool ZON>
 static void predict_launch(const PredArgs<T>& a, cudaStream_t s) {
   constexpr size_t bytes = sizeof(PredRing<T, TX25, TY25>);
-  static const bool attr = (allow_smem(k_predict25<T, TX25, TY25, LES>, bytes), true);
+  static const bool attr = (allow_smem(k_predict25<T, TX25, TY25, LES, ZON>, bytes), true);
   (void)attr;
-  k_predict25<T, TX25, TY25, LES><<<grid25(a.g), dim3(TX25, TY25), bytes, s>>>(a, KC25);
+  k_predict25<T, TX25, TY25, LES, ZON><<<grid25(a.g), dim3(TX25, TY25), bytes, s>>>(a, KC25);
 }
 template <class T>
 void launch_predict(const PredArgs<T>& a, cudaStream_t s) {
-  if (a.les) predict_launch<T, true>(a, s);
-  else predict_launch<T, false>(a, s);
+  const bool zon = a.g.bc[2] != AX_ZERO;
+  if (a.les) {
+    if (zon) predict_launch<T, true, true>(a, s);
+    else predict_launch<T, true, false>(a, s);
+  } else {
+    if (zon) predict_launch<T, false, true>(a, s);
+    else predict_launch<T, false, false>(a, s);
+  }
 }
 
+template <class T, class O, bool ZON>
+static void div_launch(const T* fx, const T* fy, const T* fz, O* out, const Grid& g, const Coef3<T>& cf, int odd,
+                       T dt, int divide, StatPart* part, cudaStream_t s) {
+  constexpr size_t bytes = sizeof(DivRing<T, TX25, TY25>);
+  static const bool attr = (allow_smem(k_div25<T, O, TX25, TY25, ZON>, bytes), true);
+  (void)attr;
+  k_div25<T, O, TX25, TY25, ZON><<<grid25(g), dim3(TX25, TY25), bytes, s>>>(fx, fy, fz, out, g, cf, odd, dt,
+                                                                              divide, part, KC25);
+}
 template <class T, class O>
 void launch_div(const T* fx, const T* fy, const T* fz, O* out, const Grid& g, const Coef3<T>& cf,
                 int odd, T dt, int divide, StatPart* part, cudaStream_t s) {
-  constexpr size_t bytes = sizeof(DivRing<T, TX25, TY25>);
-  static const bool attr = (allow_smem(k_div25<T, O, TX25, TY25>, bytes), true);
-  (void)attr;
-  k_div25<T, O, TX25, TY25><<<grid25(g), dim3(TX25, TY25), bytes, s>>>(fx, fy, fz, out, g, cf, odd, dt, divide,
-                                                                         part, KC25);
+  if (g.bc[2] != AX_ZERO) div_launch<T, O, true>(fx, fy, fz, out, g, cf, odd, dt, divide, part, s);
+  else div_launch<T, O, false>(fx, fy, fz, out, g, cf, odd, dt, divide, part, s);
 }
 
+template <class T, class S, bool ZON>
+static void correct_launch(const CorrArgs<T, S>& a, cudaStream_t s) {
+  constexpr size_t bytes = sizeof(CorrRing<T, S, TX25, TY25>);
+  static const bool attr = (allow_smem(k_correct25<T, S, TX25, TY25, ZON>, bytes), true);
+  (void)attr;
+  k_correct25<T, S, TX25, TY25, ZON><<<grid25(a.g), dim3(TX25, TY25), bytes, s>>>(a, KC25);
+}
 template <class T, class S>
 void launch_correct(const CorrArgs<T, S>& a, cudaStream_t s) {
-  constexpr size_t bytes = sizeof(CorrRing<T, S, TX25, TY25>);
-  static const bool attr = (allow_smem(k_correct25<T, S, TX25, TY25>, bytes), true);
-  (void)attr;
-  k_correct25<T, S, TX25, TY25><<<grid25(a.g), dim3(TX25, TY25), bytes, s>>>(a, KC25);
+  if (a.g.bc[2] != AX_ZERO) correct_launch<T, S, true>(a, s);
+  else correct_launch<T, S, false>(a, s);
 }
 
 template void launch_predict<double>(const PredArgs<double>&, cudaStream_t);

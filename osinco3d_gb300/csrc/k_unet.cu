@@ -448,7 +448,7 @@ int conv_splits(long long nvox, int K, int N) {
   return S < 1 ? 1 : (int)S;
 }
 
-void launch_conv3(const ConvArgs& a, cudaStream_t s) {
+int launch_conv3(const ConvArgs& a, cudaStream_t s) {
   const long long nvox = (long long)a.v.nx * a.v.ny * a.v.nz;
   const unsigned gx = (unsigned)((nvox + 63) / 64);
   int S = a.ws ? conv_splits(nvox, a.K, a.N) : 1;
@@ -459,6 +459,7 @@ void launch_conv3(const ConvArgs& a, cudaStream_t s) {
     k_conv3<4><<<dim3(gx, (a.N + 31) / 32, S), 128, 0, s>>>(a);
   }
   if (S > 1) k_conv3_reduce<<<(unsigned)((nvox * (a.N / 2) + 255) / 256), 256, 0, s>>>(a, S);
+  return S > 1 ? 2 : 1;
 }
 
 void launch_wgrad(const WgradArgs& a0, cudaStream_t s) {

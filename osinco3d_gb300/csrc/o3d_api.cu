@@ -113,6 +113,8 @@ struct o3d_ctx {
   cudaGraphExec_t mg_exec;
   int mg_batch;
   long long mg_nodes;
+  cudaGraphExec_t learn_exec;  // first outer iteration with the learned guess (multigrid)
+  long long learn_nodes;
 
   cudaEvent_t ev[4];
   long long launches;
@@ -498,6 +500,58 @@ int learn_ready(o3d_ctx* c) {
   return O3D_OK;
 }
 
+// The start of a solve with the learned guess (or with training samples):
+// p <- p_ex = 2 p(n) - p(n-1), p(n-1) <- p(n), the increment into the finest
+// level's t; the FP64 residual of p_ex (the first outer iteration's, for
+// multigrid) and the increment, restricted, form the network's input; the
+// network's correction starts the first V-cycle (multigrid) or is added to p
+// (SOR).  Everything is enqueued on the context's stream.
+int enqueue_learned_first(o3d_ctx* c, bool learned, bool sampling, bool use_mg, int pre, int post,
+                          long long* nl) {
+  const int ll = c->learn_level;
+  MGLevel* lv = c->mg.data();
+  if (c->mixed) launch_learn_extrapolate<float>(c->pp, c->pp_prev, lv, c->s, nl);
+  else launch_learn_extrapolate<double>(c->pp, c->pp_prev, lv, c->s, nl);
+  if (use_mg) {
+    if (c->mixed) launch_mg_resid<float, float>(c->pp, (const float*)c->rhs, lv, c->ctrl, c->s, nl);
+    else launch_mg_resid<double, double>(c->pp, (const double*)c->rhs, lv, c->ctrl, c->s, nl);
+  } else {
+    if (c->mixed) launch_level_kernel<float, float>(1, c->pp, (const float*)c->rhs, lv[0], c->ctrl, c->s);
+    else launch_level_kernel<double, double>(1, c->pp, (const double*)c->rhs, lv[0], c->ctrl, c->s);
+    *nl += 1;
+  }
+  if (c->mixed) launch_learn_features<float>(lv, ll, c->ctrl, c->feat, c->s, nl);
+  else launch_learn_features<double>(lv, ll, c->ctrl, c->feat, c->s, nl);
+  CKL();
+  if (sampling) {
+    CK(cudaMemcpyAsync(c->sample_feat, c->feat, (size_t)c->mg[ll].g.n * 2 * sizeof(float), cudaMemcpyDeviceToDevice,
+                       c->s));
+    c->sample_ready = 1;
+  }
+  if (learned) {
+    int st = unet_enqueue_forward(c->unet, c->feat, c->ynet, c->s, nl);
+    if (st) {
+      errf("U-Net forward: %s", cudaGetErrorString(cudaGetLastError()));
+      return st;
+    }
+    if (c->mixed) launch_learn_apply<float>(c->pp, c->ynet, lv, ll, !use_mg, c->ctrl, c->s, nl);
+    else launch_learn_apply<double>(c->pp, c->ynet, lv, ll, !use_mg, c->ctrl, c->s, nl);
+    CKL();
+  }
+  if (use_mg) {  // the rest of the first outer iteration, from the network's correction when learned
+    const int cyc = mg_cycles_of(c);
+    const double om = mg_omega_of(c);
+    if (c->mixed)
+      launch_mg_cycles<float>(c->pp, lv, (int)c->mg.size(), pre, post, MG_COARSE_SWEEPS, (float)om, cyc, learned,
+                              c->ctrl, c->s, nl);
+    else
+      launch_mg_cycles<double>(c->pp, lv, (int)c->mg.size(), pre, post, MG_COARSE_SWEEPS, om, cyc, learned, c->ctrl,
+                               c->s, nl);
+    CKL();
+  }
+  return O3D_OK;
+}
+
 // Solves A pp = rhs with the context's solver; pp holds the initial guess.
 int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step_info* info) {
   const int guess = c->P.guess;
@@ -540,45 +594,28 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
   }
   if (need_hist) {
     if (c->pp_prev_valid && (learned || sampling)) {
-      // p <- p_ex = 2 p(n) - p(n-1), p(n-1) <- p(n), increment into the finest t;
-      // the FP64 residual of p_ex (the first outer iteration's, for multigrid)
-      // and the increment, restricted, are the network's input
-      const int ll = c->learn_level;
-      MGLevel* lv = c->mg.data();
-      if (c->mixed) launch_learn_extrapolate<float>(c->pp, c->pp_prev, lv, c->s, &c->launches);
-      else launch_learn_extrapolate<double>(c->pp, c->pp_prev, lv, c->s, &c->launches);
-      if (use_mg) {
-        if (c->mixed) launch_mg_resid<float, float>(c->pp, (const float*)c->rhs, lv, c->ctrl, c->s, &c->launches);
-        else launch_mg_resid<double, double>(c->pp, (const double*)c->rhs, lv, c->ctrl, c->s, &c->launches);
+      if (learned && use_mg && !sampling) {
+        // replayed from a graph captured on first use
+        if (!c->learn_exec) {
+          long long nl = 0;
+          cudaGraph_t graph;
+          CK(cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal));
+          const int st1 = enqueue_learned_first(c, true, false, true, pre, post, &nl);
+          const cudaError_t e1 = cudaStreamEndCapture(c->s, &graph);
+          if (st1) {
+            if (e1 == cudaSuccess) cudaGraphDestroy(graph);
+            return st1;
+          }
+          CK(e1);
+          const cudaError_t e2 = cudaGraphInstantiate(&c->learn_exec, graph, 0);
+          cudaGraphDestroy(graph);
+          CK(e2);
+          c->learn_nodes = nl;
+        }
+        CK(cudaGraphLaunch(c->learn_exec, c->s));
+        c->launches += c->learn_nodes;
       } else {
-        if (c->mixed) launch_level_kernel<float, float>(1, c->pp, (const float*)c->rhs, lv[0], c->ctrl, c->s);
-        else launch_level_kernel<double, double>(1, c->pp, (const double*)c->rhs, lv[0], c->ctrl, c->s);
-        c->launches++;
-      }
-      if (c->mixed) launch_learn_features<float>(lv, ll, c->ctrl, c->feat, c->s, &c->launches);
-      else launch_learn_features<double>(lv, ll, c->ctrl, c->feat, c->s, &c->launches);
-      CKL();
-      if (sampling) {
-        CK(cudaMemcpyAsync(c->sample_feat, c->feat, (size_t)c->mg[ll].g.n * 2 * sizeof(float),
-                           cudaMemcpyDeviceToDevice, c->s));
-        c->sample_ready = 1;
-      }
-      if (learned) {
-        if ((st = unet_forward(c->unet, c->feat, c->ynet, c->s))) return st;
-        if (c->mixed) launch_learn_apply<float>(c->pp, c->ynet, lv, ll, !use_mg, c->ctrl, c->s, &c->launches);
-        else launch_learn_apply<double>(c->pp, c->ynet, lv, ll, !use_mg, c->ctrl, c->s, &c->launches);
-        CKL();
-      }
-      if (use_mg) {  // the rest of the first outer iteration, from the network's correction when learned
-        const int cyc = mg_cycles_of(c);
-        const double om = mg_omega_of(c);
-        if (c->mixed)
-          launch_mg_cycles<float>(c->pp, lv, (int)c->mg.size(), pre, post, MG_COARSE_SWEEPS, (float)om, cyc, learned,
-                                  c->ctrl, c->s, &c->launches);
-        else
-          launch_mg_cycles<double>(c->pp, lv, (int)c->mg.size(), pre, post, MG_COARSE_SWEEPS, om, cyc, learned,
-                                   c->ctrl, c->s, &c->launches);
-        CKL();
+        if ((st = enqueue_learned_first(c, learned, sampling, use_mg, pre, post, &c->launches))) return st;
       }
     } else if (c->pp_prev_valid && guess == O3D_GUESS_EXTRAPOLATED) {
       launch_extrapolate(c->pp, c->pp_prev, c->g.n, c->s);
@@ -800,6 +837,7 @@ int o3d_destroy(o3d_ctx* c) {
   for (auto& L : c->mg) { cudaFree(L.e); cudaFree(L.r); cudaFree(L.t); }
   if (c->sor_exec) cudaGraphExecDestroy(c->sor_exec);
   if (c->mg_exec) cudaGraphExecDestroy(c->mg_exec);
+  if (c->learn_exec) cudaGraphExecDestroy(c->learn_exec);
   for (int q = 0; q < 4; ++q) if (c->ev[q]) cudaEventDestroy(c->ev[q]);
   if (c->s) cudaStreamDestroy(c->s);
   delete c;
@@ -1060,8 +1098,17 @@ int o3d_rbsor_sweeps_dev(o3d_ctx* c, double* d_pp, const double* d_rhs, double o
 
 int o3d_attach_unet(o3d_ctx* c, o3d_unet* net) {
   if (!c) return O3D_ERR_BADARG;
+  if (c->learn_exec) {
+    CK(cudaStreamSynchronize(c->s));
+    cudaGraphExecDestroy(c->learn_exec);
+    c->learn_exec = nullptr;
+  }
   c->unet = net;
   if (!net) return O3D_OK;
+  if (unet_sync(net)) {
+    errf("the network's queued work failed");
+    return O3D_ERR_CUDA;
+  }
   int st = learn_ready(c);
   if (st) return st;
   int nx, ny, nz, nin;

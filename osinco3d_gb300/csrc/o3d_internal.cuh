@@ -342,7 +342,8 @@ struct SolveCtrl {
   int iter, kmax, idyn, done, status;
   int cycles;            // V-cycles run so far
   int cycles_per_iter;   // V-cycles per outer iteration (multigrid)
-  double learn_scale;    // feature scale S of the learned warm start
+  double learn_scale;    // learned warm start: rms of the restricted residual x h^2 (input 0 and output scale)
+  double learn_scale_d;  // learned warm start: rms of the restricted increment (input 1 scale)
 };
 
 }  // namespace o3d

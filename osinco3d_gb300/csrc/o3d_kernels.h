@@ -9,7 +9,8 @@ struct o3d_unet;
 namespace o3d {
 
 // the network of the learned guess (o3d_unet_host.cu)
-int unet_forward(o3d_unet* n, const float* d_in, float* d_out, cudaStream_t wait);
+int unet_enqueue_forward(o3d_unet* n, const float* d_in, float* d_out, cudaStream_t s, long long* nl);
+int unet_sync(o3d_unet* n);
 int unet_grid(const o3d_unet* n, int* nx, int* ny, int* nz, int* in_ch);
 
 template <class T>

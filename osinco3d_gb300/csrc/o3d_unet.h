@@ -44,7 +44,7 @@ struct WgradArgs {
 // voxels with K inputs and N outputs is split into: 1 on grids that fill the
 // GPU, up to 27 * K / 64 on the small grids of the deep levels.
 int conv_splits(long long nvox, int K, int N);
-void launch_conv3(const ConvArgs& a, cudaStream_t s);
+int launch_conv3(const ConvArgs& a, cudaStream_t s);  // returns the kernels launched
 void launch_wgrad(const WgradArgs& a, cudaStream_t s);
 void launch_bias_grad(const __nv_bfloat16* dy, int dycs, int dyc0, long long nvox, int N, float* db, cudaStream_t s);
 void launch_pool(const __nv_bfloat16* x, int xcs, int xc0, const Vol& vf, __nv_bfloat16* y, int ycs, int yc0,

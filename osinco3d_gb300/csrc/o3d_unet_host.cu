@@ -56,6 +56,7 @@ struct UNet {
   cudaStream_t s = nullptr;
   cudaEvent_t ev = nullptr;           // orders the forward pass after / before a caller's stream
   cudaGraphExec_t fwd_exec = nullptr; // the forward pass as one graph (inference)
+  long long launches = 0;             // kernels launched by forward/backward so far
   std::vector<void*> allocs;
 };
 
@@ -114,7 +115,7 @@ static void conv(UNet& u, const ConvLayer& L, const Tensor& x, const Tensor& y, 
   a.accumulate = 0;
   a.ws = u.ws;
   a.ws_cap = u.ws_cap;
-  launch_conv3(a, u.s);
+  u.launches += launch_conv3(a, u.s);
 }
 
 // dX = conv(dY, mirrored W^T), masked by (mask > 0) when given
@@ -133,7 +134,7 @@ static void conv_dgrad(UNet& u, const ConvLayer& L, const Tensor& dy, const Tens
   a.accumulate = 0;
   a.ws = u.ws;
   a.ws_cap = u.ws_cap;
-  launch_conv3(a, u.s);
+  u.launches += launch_conv3(a, u.s);
 }
 
 static void conv_wgrad(UNet& u, const ConvLayer& L, const Tensor& x, const Tensor& dy) {
@@ -162,17 +163,22 @@ static void forward(UNet& u) {
     conv(u, u.enc_a[l], in, u.ea[l], true);
     const Tensor skip = l < Lv - 1 ? slice(u.cat[l], 2 * ch(u, l), ch(u, l)) : u.dbot[0];
     conv(u, u.enc_b[l], u.ea[l], skip, true);
-    if (l < Lv - 1) launch_pool(skip.p, skip.cs, skip.c0, skip.v, u.pool[l + 1].p, u.pool[l + 1].cs, 0,
-                                u.vol[l + 1], ch(u, l), u.s);
+    if (l < Lv - 1) {
+      launch_pool(skip.p, skip.cs, skip.c0, skip.v, u.pool[l + 1].p, u.pool[l + 1].cs, 0, u.vol[l + 1], ch(u, l),
+                  u.s);
+      u.launches += 1;
+    }
   }
   for (int l = Lv - 2; l >= 0; --l) {
     const Tensor& below = l == Lv - 2 ? u.dbot[0] : u.d[l + 1];
     launch_upsample(below.p, below.cs, below.c0, u.vol[l + 1], u.cat[l].p, u.cat[l].cs, 0, u.vol[l], ch(u, l + 1),
                     u.s);
+    u.launches += 1;
     conv(u, u.dec_a[l], u.cat[l], u.da[l], true);
     conv(u, u.dec_b[l], u.da[l], u.d[l], true);
   }
   launch_head(u.d[0].p, u.d[0].cs, ch(u, 0), nvox(u.vol[0]), u.w + u.head_w, u.w + u.head_b, u.out, u.s);
+  u.launches += 1;
 }
 
 // the forward pass replayed from a graph captured on first use (the
@@ -490,9 +496,23 @@ int o3d_unet_train_step(o3d_unet* n, const float* d_in, const float* d_target, f
 
 // used by the solver context (o3d_api.cu)
 namespace o3d {
-int unet_forward(o3d_unet* n, const float* d_in, float* d_out, cudaStream_t wait) {
-  return o3d_unet_forward_dev(n, d_in, d_out, (void*)wait);
+// The forward pass enqueued on the caller's stream s (so that a solver can
+// capture it in its own CUDA graph); the network's buffers are shared, so
+// the network must not run elsewhere meanwhile.
+int unet_enqueue_forward(o3d_unet* n, const float* d_in, float* d_out, cudaStream_t s, long long* nl) {
+  UNet& u = n->u;
+  const cudaStream_t own = u.s;
+  u.s = s;
+  const long long l0 = u.launches;
+  launch_pack_input(d_in, u.in_ch, nvox(u.vol[0]), u.xin.p, 16, u.s);
+  forward(u);
+  *nl += 1 + (u.launches - l0);
+  const cudaError_t e = cudaMemcpyAsync(d_out, u.out, nvox(u.vol[0]) * 4, cudaMemcpyDeviceToDevice, u.s);
+  u.s = own;
+  return e == cudaSuccess ? O3D_OK : O3D_ERR_CUDA;
 }
+// waits for the network's own queued work (weight packing after training)
+int unet_sync(o3d_unet* n) { return cudaStreamSynchronize(n->u.s) == cudaSuccess ? O3D_OK : O3D_ERR_CUDA; }
 int unet_grid(const o3d_unet* n, int* nx, int* ny, int* nz, int* in_ch) {
   *nx = n->u.vol[0].nx;
   *ny = n->u.vol[0].ny;

@@ -83,6 +83,8 @@ def train(net: "o3d.UNet", feat, tgt, epochs: int, lr: float = 1e-3, seed: int =
 
     rng = np.random.default_rng(seed)
     hist = []
+    if log:
+        log(f"zero-prediction loss {float((tgt.double() ** 2).mean()):.4e}")
     for ep in range(epochs):
         order = rng.permutation(feat.shape[0])
         tot = 0.0

@@ -9,6 +9,8 @@ FP32 accumulation order and the rounding boundaries it moves: output within
 BF16 oracle's norm plus the BF16 noise of that layer (the distance between
 the BF16 oracle and the same oracle in exact arithmetic, which reaches
 4-20 % on small grids); a wrong tap, padding or layout gives O(1) errors."""
+import os
+
 import numpy as np
 import pytest
 
@@ -111,3 +113,51 @@ def test_learned_guess_in_the_step(oracle, o3d):
         ctx.set_sample_buffers(None, None)
         ctx.attach_unet(None)
         net.close()
+
+
+def _cycles(o3d, guess, n, steps, warmup, weights=None):
+    """Mean V-cycles per step (steps after warm-up) and the final velocity of
+    the n^3 Taylor-Green run, Poisson eps = 1e-8, mixed precision."""
+    from osinco3d_gb300 import learn
+
+    p = o3d.tgv_params(n, re=1600.0, precision=o3d.PREC_MIXED, solver=o3d.SOLVER_MG, eps=1e-8, kmax=100,
+                       guess=guess)
+    with o3d.Context(p) as ctx:
+        net = None
+        if weights:
+            net = learn.load(weights, ctx.guess_grid())
+            ctx.attach_unet(net)
+        for nm, f in zip(("ux", "uy", "uz", "pp"), o3d.tgv_fields(p)):
+            ctx.upload(nm, f)
+        cyc = []
+        for it in range(1, warmup + steps + 1):
+            info = ctx.step(it)
+            assert info.poisson_status == 0
+            if it > warmup:
+                cyc.append(info.poisson_cycles)
+        u = ctx.download("ux")
+        if net:
+            ctx.attach_unet(None)
+            net.close()
+    return float(np.mean(cyc)), u
+
+
+@pytest.mark.slow
+def test_trained_network_saves_v_cycles(o3d):
+    """The committed network (trained on 128^3 solver samples) against the
+    same solver without it, at 256^3: the extrapolated guess alone, and the
+    previous step's pressure (the reference's start).  Every run iterates to
+    the same eps, so the velocity agrees; the network must save V-cycles."""
+    from osinco3d_gb300 import learn
+
+    if not os.path.exists(learn.WEIGHTS):
+        pytest.skip("no trained weights")
+    n, steps, warmup = 256, 6, 3
+    c_prev, u_prev = _cycles(o3d, o3d.GUESS_PREVIOUS, n, steps, warmup)
+    c_ex, u_ex = _cycles(o3d, o3d.GUESS_EXTRAPOLATED, n, steps, warmup)
+    c_nn, u_nn = _cycles(o3d, o3d.GUESS_LEARNED, n, steps, warmup, weights=learn.WEIGHTS)
+    print(f"V-cycles per step at {n}^3: previous {c_prev:.2f}, extrapolated {c_ex:.2f}, learned {c_nn:.2f}")
+    assert c_nn < c_ex <= c_prev
+    scale = np.abs(u_ex).max()
+    assert np.abs(u_nn - u_ex).max() < 1e-6 * scale
+    assert np.abs(u_prev - u_ex).max() < 1e-6 * scale
