@@ -229,14 +229,19 @@ KERNEL_BYTES = {
     "mg_smooth": (8, "k_smooth<float> (one red-black colour pass, finest level)"),  # half-grid e, r in/out
     "rhs": (16, "k_div25<float>"),
     "correct": (4 * 6 + 8, "k_correct25<float,double>"),
+    "resid64": (8 + 4 + 4, "k_resid25<float,float> (FP64 residual, finest level)"),  # read p, rhs; write r
 }
+# FP64 operations per point of the FP64 residual (its bound is the FP64 pipe)
+RESID64_FP64_OPS = 7
+# the kernel the roofline entry describes: the fused predictor, the largest
+# single HBM-bound kernel of the step
+ROOF_KERNEL = "predict"
 
 
 def kernel_roofline(o3d, ctx, peaks: dict) -> dict:
     """Device time per launch of the hot kernels on the live state (CUDA events
     on the context's stream, averaged over repeated launches) and their
-    achieved algorithmic bandwidth.  The roofline entry is the finest-level
-    smoother, the kernel with the largest share of the step."""
+    achieved algorithmic bandwidth."""
     peak = peaks.get("hbm_gbs")
     out = {}
     for name, (bpp, label) in KERNEL_BYTES.items():
@@ -244,6 +249,8 @@ def kernel_roofline(o3d, ctx, peaks: dict) -> dict:
         gbs = bpp * N ** 3 / (t * 1e-3) / 1e9
         out[name] = {"kernel": label, "ms": t, "bytes_per_point": bpp, "achieved": gbs,
                      "frac": gbs / peak if peak else None}
+    r = out["resid64"]
+    r["fp64_gops"] = RESID64_FP64_OPS * N ** 3 / (r["ms"] * 1e-3) / 1e9
     return out
 
 
@@ -299,7 +306,7 @@ def gpu_arm(args, rank, world, local):
     with ClockSampler(local) as clk:
         head, ctx, _ = run_variant(o3d, head_name, args.steps, args.warmup, world, weights=weights, **head_kw)
     clocks = clk.summary()
-    roof = kernel_roofline(o3d, ctx, peaks)
+    roof = None if args.no_roofline else kernel_roofline(o3d, ctx, peaks)
     ctx.close()
     variants[head_name] = head
     if not args.quick:
@@ -343,11 +350,13 @@ def gpu_arm(args, rank, world, local):
         "clocks": clocks,
         "variants": variants,
     }
-    top = roof["mg_smooth"]
-    line["roofline"] = {"bound": "hbm", "achieved": top["achieved"], "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
-                        "frac": top["frac"], "traffic": TRAFFIC_PER_LAUNCH.get("mg_smooth"), "kernel": top["kernel"],
-                        "bytes_per_point": top["bytes_per_point"], "ms": top["ms"],
-                        "peak_source": peaks.get("source"), "others": {k: v for k, v in roof.items() if k != "mg_smooth"}}
+    if roof:
+        top = roof[ROOF_KERNEL]
+        line["roofline"] = {"bound": "hbm", "achieved": top["achieved"], "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                            "frac": top["frac"], "traffic": TRAFFIC_PER_LAUNCH.get(ROOF_KERNEL),
+                            "kernel": top["kernel"], "bytes_per_point": top["bytes_per_point"], "ms": top["ms"],
+                            "peak_source": peaks.get("source"),
+                            "others": {k: v for k, v in roof.items() if k != ROOF_KERNEL}}
     if "fp64_mg" in variants:
         line["speedup_mixed_vs_fp64_mg"] = variants["fp64_mg"]["ms_per_step"] / head["ms_per_step"]
         line["speedup_mixed_vs_fp64_rbsor"] = variants["fp64_rbsor"]["ms_per_step"] / head["ms_per_step"]
@@ -388,6 +397,8 @@ def main():
     ap.add_argument("--quick", action="store_true", help="headline variant only")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end run")
+    ap.add_argument("--no-roofline", action="store_true",
+                    help="skip the per-kernel timing launches (for a launch list of the steps alone)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

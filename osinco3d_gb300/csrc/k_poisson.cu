@@ -10,8 +10,9 @@
 //  * Geometric multigrid V(pre,post) cycles (red-black Gauss-Seidel
 //    smoother, full-weighting restriction, trilinear prolongation,
 //    shared-memory coarse solve) as the inner solver of an FP64 defect-
-//    correction loop: r = rhs - A p in FP64, A e = r by one cycle in T,
-//    p += e, stop when max |e| < eps.  Replaces the unusable single V-cycle
+//    correction loop: r = rhs - A p in FP64 (the rhs's weighted mean
+//    removed once per solve), A e = r by V-cycles in T, p += e, stop when
+//    max |e| < eps.  Replaces the unusable single V-cycle
 //    of src/poisson_multigrid.f90:10-190.
 #include "o3d_internal.cuh"
 #include "o3d_kernels.h"
@@ -23,6 +24,31 @@ enum { ST_CONVERGED = 0, ST_STAGNATED = 1, ST_MAXIT = 2 };
 // neighbour index of the Poisson remap on one axis
 __device__ __forceinline__ int nb_lo(int i, int n, int bc) { return i > 0 ? i - 1 : (bc == AX_PERIODIC ? n - 1 : 1); }
 __device__ __forceinline__ int nb_hi(int i, int n, int bc) { return i < n - 1 ? i + 1 : (bc == AX_PERIODIC ? 0 : n - 2); }
+
+// Offsets of the six neighbours of point (i, j, k) with the Poisson remap at
+// the ends, in 32-bit arithmetic (a grid holds at most 2^31 points).
+struct Nb6 {
+  int xm, xp, ym, yp, zm, zp;
+};
+__device__ __forceinline__ Nb6 nb6(const Grid& g, int i, int j, int k) {
+  const int sy = g.nx, sz = g.nx * g.ny;
+  Nb6 o;
+  o.xm = i > 0 ? -1 : (g.bc[0] == AX_PERIODIC ? g.nx - 1 : 1);
+  o.xp = i < g.nx - 1 ? 1 : (g.bc[0] == AX_PERIODIC ? 1 - g.nx : -1);
+  o.ym = j > 0 ? -sy : (g.bc[1] == AX_PERIODIC ? (g.ny - 1) * sy : sy);
+  o.yp = j < g.ny - 1 ? sy : (g.bc[1] == AX_PERIODIC ? (1 - g.ny) * sy : -sy);
+  o.zm = k > 0 ? -sz : (g.bc[2] == AX_PERIODIC ? (g.nz - 1) * sz : sz);
+  o.zp = k < g.nz - 1 ? sz : (g.bc[2] == AX_PERIODIC ? (1 - g.nz) * sz : -sz);
+  return o;
+}
+__device__ __forceinline__ int idx3(const Grid& g, int i, int j, int k) { return i + g.nx * (j + g.ny * k); }
+
+// off-diagonal part of A at q: ox (w + e) + oy (s + n) + oz (b + t)
+template <class T, class S>
+__device__ __forceinline__ T lap6(const S* __restrict__ p, int q, const Nb6& o, const PoiCoef<T>& c) {
+  return c.ox * ((T)p[q + o.xm] + (T)p[q + o.xp]) + c.oy * ((T)p[q + o.ym] + (T)p[q + o.yp]) +
+         c.oz * ((T)p[q + o.zm] + (T)p[q + o.zp]);
+}
 
 template <class T, class S>
 __device__ __forceinline__ T lap_nb(const S* __restrict__ p, const Grid& g, int i, int j, int k,
@@ -53,8 +79,8 @@ __global__ void __launch_bounds__(256) k_sor_rb(double* __restrict__ p, const do
   if (j < g.ny) {
     const int i = 2 * ih + ((j + k + color) & 1);
     if (i < g.nx) {
-      const long long q = (long long)i + g.sy() * j + g.sz() * k;
-      const double s = lap_nb<double>(p, g, i, j, k, c);
+      const int q = idx3(g, i, j, k);
+      const double s = lap6<double>(p, q, nb6(g, i, j, k), c);
       const double pc = p[q];
       const double pnew = (rhs[q] - s) * c.invA;
       d = fabs(pnew - pc);
@@ -129,24 +155,30 @@ __device__ __forceinline__ double wnode(const Grid& g, int i, int j, int k) {
   return w;
 }
 
-// sum of w*rhs with the trapezoid weights; one thread per (i, j) column
+// sum of w*rhs with the trapezoid weights; a thread sums its (i, j) column
+// over a chunk of WM_KC planes, a block reduces its 32 x 8 columns
+constexpr int WM_KC = 32;
 template <class R>
 __global__ void __launch_bounds__(256) k_wmean_part(const R* __restrict__ rhs, Grid g, double* part) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k0 = blockIdx.z * WM_KC, k1 = min(k0 + WM_KC, g.nz);
   double r[1] = {0.0};
   const int ops[1] = {RED_SUM};
   if (i < g.nx && j < g.ny) {
     double wxy = 1.0;
     if (g.bc[0] == AX_MIRROR && (i == 0 || i == g.nx - 1)) wxy *= 0.5;
     if (g.bc[1] == AX_MIRROR && (j == 0 || j == g.ny - 1)) wxy *= 0.5;
-    double acc = 0.0, edge = 0.0;
-    for (int k = 0; k < g.nz; ++k) {
-      const double v = to_t<double>(rhs[(long long)i + g.sy() * j + g.sz() * k]);
+    // the column chunk is summed in the rhs type (at most WM_KC terms), the
+    // chunks and blocks in FP64
+    R acc = (R)0, edge = (R)0;
+    const R* col = rhs + (long long)i + g.sy() * j;
+    for (int k = k0; k < k1; ++k) {
+      const R v = __ldg(col + g.sz() * k);
       if (k == 0 || k == g.nz - 1) edge += v; else acc += v;
     }
     const double wz = g.bc[2] == AX_MIRROR ? 0.5 : 1.0;
-    r[0] = wxy * (acc + wz * edge);
+    r[0] = wxy * (to_t<double>(acc) + wz * to_t<double>(edge));
   }
   block_reduce_store<1>(r, ops, part, block_linear_id());
 }
@@ -164,49 +196,105 @@ __global__ void k_wmean_final(const double* __restrict__ part, long long nblk, d
   if (threadIdx.x == 0) ctrl->rhs_mean = s0[0] / wsum;
 }
 
-// r0 = (rhs - mean) - A p, FP64 arithmetic, stored in T
-template <class T, class R>
-__global__ void __launch_bounds__(256) k_resid_top(const double* __restrict__ p, const R* __restrict__ rhs,
-                                                   T* __restrict__ r0, Grid g, PoiCoef<double> c,
-                                                   SolveCtrl* ctrl) {
-  if (ctrl->done) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
-  if (i >= g.nx || j >= g.ny) return;
-  const long long q = (long long)i + g.sy() * j + g.sz() * k;
-  const double ap = lap_nb<double>(p, g, i, j, k, c) + c.A * p[q];
-  r0[q] = to_t<T>((to_t<double>(rhs[q]) - ctrl->rhs_mean) - ap);
+// rhs <- rhs - mean (the trapezoid-weighted mean of k_wmean_final), in
+// place, once per multigrid solve: the residual kernels then read a
+// compatible rhs and skip the subtraction.
+template <class R>
+__global__ void k_rhs_shift(R* __restrict__ rhs, long long n, const SolveCtrl* ctrl) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const R mean = to_t<R>(ctrl->rhs_mean);  // subtracted in the rhs type
+  if (q < n) rhs[q] = rhs[q] - mean;
 }
 
-// same residual, plus max |r| of the block into ctrl->res_key
-template <class T, class R>
-__global__ void __launch_bounds__(256) k_resid_top_max(const double* __restrict__ p, const R* __restrict__ rhs,
-                                                       T* __restrict__ r0, Grid g, PoiCoef<double> c,
-                                                       SolveCtrl* ctrl) {
+// ---------------------------------------------------------------------------
+// FP64 residual of the defect-correction loop, r0 = rhs - A p, stored in T
+// (with MAX, max |r0| of the block into ctrl->res_key).  2.5D: a block owns
+// a 32 x 8 column and marches along z over RZ_KC planes; each thread keeps
+// p at k-1, k, k+1 of its point in registers, the plane's x/y neighbours
+// come from a double-buffered shared tile with a 1-point halo (the halo
+// cell of a thread and the next queue head are loaded one plane ahead).
+// The operator is evaluated as one FMA chain,
+//   r = fma(-oz, pb+pt, fma(-oy, ps+pn, fma(-ox, pw+pe, fma(-A, pc, rhs)))),
+// 7 FP64 operations per point (GB300 runs 2 FP64 lanes per clock per SM:
+// this kernel is bound by them); the neighbour remap is that of
+// src/poisson.f90:57-92 (periodic wrap, or mirror about the end node).
+// ---------------------------------------------------------------------------
+constexpr int RZ_TX = 32, RZ_TY = 8, RZ_KC = 32;
+static inline dim3 rz_grid(const Grid& g) {
+  return dim3((g.nx + RZ_TX - 1) / RZ_TX, (g.ny + RZ_TY - 1) / RZ_TY, (g.nz + RZ_KC - 1) / RZ_KC);
+}
+
+template <class T, class R, bool MAX>
+__global__ void __launch_bounds__(RZ_TX * RZ_TY) k_resid25(const double* __restrict__ p, const R* __restrict__ rhs,
+                                                           T* __restrict__ r0, Grid g, PoiCoef<double> c,
+                                                           SolveCtrl* ctrl) {
   if (ctrl->done) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
+  constexpr int TX = RZ_TX, TY = RZ_TY, SW = TX + 2;
+  __shared__ double tile[2][(TY + 2) * SW];
+  const int tx = threadIdx.x, ty = threadIdx.y, t = ty * TX + tx;
+  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+  const int i = i0 + tx, j = j0 + ty;
+  const bool valid = i < g.nx && j < g.ny;
+  const int k0 = blockIdx.z * RZ_KC, k1 = min(k0 + RZ_KC, g.nz);
+  const long long sz = g.sz();
+  bool f;
+  const int cxy = ghost(i, g.nx, g.bc[0], &f) + g.nx * ghost(j, g.ny, g.bc[1], &f);
+  // halo cell of this thread (t < 2 (TX + TY)): left, right, below, above
+  const bool hon = t < 2 * (TX + TY);
+  int hi, hj, hidx;
+  if (t < TY) { hi = i0 - 1; hj = j0 + t; hidx = (t + 1) * SW; }
+  else if (t < 2 * TY) { hi = i0 + TX; hj = j0 + t - TY; hidx = (t - TY + 1) * SW + TX + 1; }
+  else if (t < 2 * TY + TX) { hi = i0 + t - 2 * TY; hj = j0 - 1; hidx = t - 2 * TY + 1; }
+  else { const int u = min(t - 2 * TY - TX, TX - 1); hi = i0 + u; hj = j0 + TY; hidx = (TY + 1) * SW + u + 1; }
+  const int hxy = ghost(hi, g.nx, g.bc[0], &f) + g.nx * ghost(hj, g.ny, g.bc[1], &f);
+  const int sc = (ty + 1) * SW + tx + 1;
+  auto zoff = [&](int k) { return sz * ghost(k, g.nz, g.bc[2], &f); };
+  const long long out0 = valid ? (long long)i + (long long)g.nx * j : 0;
+
+  double pb = __ldg(p + zoff(k0 - 1) + cxy), pc = __ldg(p + zoff(k0) + cxy), pt = __ldg(p + zoff(k0 + 1) + cxy);
+  double hv = hon ? __ldg(p + zoff(k0) + hxy) : 0.0;
   float m = 0.f;
-  if (i < g.nx && j < g.ny) {
-    const long long q = (long long)i + g.sy() * j + g.sz() * k;
-    const double ap = lap_nb<double>(p, g, i, j, k, c) + c.A * p[q];
-    const T rv = to_t<T>((to_t<double>(rhs[q]) - ctrl->rhs_mean) - ap);
-    r0[q] = rv;
-    m = fabsf((float)rv);
+  int buf = 0;
+  for (int k = k0; k < k1; ++k) {
+    tile[buf][sc] = pc;
+    if (hon) tile[buf][hidx] = hv;
+    double npt = 0.0;
+    if (k + 1 < k1) {
+      npt = __ldg(p + zoff(k + 2) + cxy);
+      if (hon) hv = __ldg(p + zoff(k + 1) + hxy);
+    }
+    const long long q = out0 + sz * k;
+    const double rh = valid ? to_t<double>(__ldg(rhs + q)) : 0.0;
+    __syncthreads();
+    if (valid) {
+      const double pw = tile[buf][sc - 1], pe = tile[buf][sc + 1];
+      const double ps = tile[buf][sc - SW], pn = tile[buf][sc + SW];
+      double r = fma(-c.A, pc, rh);
+      r = fma(-c.ox, pw + pe, r);
+      r = fma(-c.oy, ps + pn, r);
+      r = fma(-c.oz, pb + pt, r);
+      const T rv = to_t<T>(r);
+      r0[q] = rv;
+      if (MAX) m = fmaxf(m, fabsf((float)rv));
+    }
+    pb = pc;
+    pc = pt;
+    pt = npt;
+    buf ^= 1;
   }
-  const float bm = block_max_f(m);
-  if (threadIdx.x == 0 && threadIdx.y == 0 && bm > 0.f) {
-    // float max as double bits: the max of nonnegative doubles orders like their bits
-    atomicMax(&ctrl->res_key, (unsigned long long)__double_as_longlong((double)bm));
+  if (MAX) {
+    const float bm = block_max_f(m);
+    if (threadIdx.x == 0 && threadIdx.y == 0 && bm > 0.f) {
+      // float max as double bits: the max of nonnegative doubles orders like their bits
+      atomicMax(&ctrl->res_key, (unsigned long long)__double_as_longlong((double)bm));
+    }
   }
 }
 
-// max |rhs - mean - A p| after a solve
+// max |rhs - A p| after a solve (the multigrid rhs is already mean-free)
 template <class R>
 __global__ void __launch_bounds__(256) k_resid_inf(const double* __restrict__ p, const R* __restrict__ rhs,
-                                                   Grid g, PoiCoef<double> c, int use_mean, SolveCtrl* ctrl) {
+                                                   Grid g, PoiCoef<double> c, SolveCtrl* ctrl) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
@@ -214,7 +302,7 @@ __global__ void __launch_bounds__(256) k_resid_inf(const double* __restrict__ p,
   if (i < g.nx && j < g.ny) {
     const long long q = (long long)i + g.sy() * j + g.sz() * k;
     const double ap = lap_nb<double>(p, g, i, j, k, c) + c.A * p[q];
-    d = fabs((to_t<double>(rhs[q]) - (use_mean ? ctrl->rhs_mean : 0.0)) - ap);
+    d = fabs(to_t<double>(rhs[q]) - ap);
   }
   const double bm = block_max(d);
   if (threadIdx.x == 0 && threadIdx.y == 0 && bm > 0.0)
@@ -245,12 +333,12 @@ __global__ void __launch_bounds__(256) k_smooth_first(T* __restrict__ e, const T
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
   if (i >= g.nx || j >= g.ny) return;
-  const long long q = (long long)i + g.sy() * j + g.sz() * k;
+  const int q = idx3(g, i, j, k);
   const T rq = __ldg(r + q);
   if (((i + j + k) & 1) == 0) {
     e[q] = om * (rq * c.invA);
   } else {
-    const T sr = lap_nb<T>(r, g, i, j, k, c);
+    const T sr = lap6<T>(r, q, nb6(g, i, j, k), c);
     e[q] = om * ((rq - om * (sr * c.invA)) * c.invA);
   }
 }
@@ -265,8 +353,8 @@ __global__ void __launch_bounds__(256) k_smooth(T* __restrict__ e, const T* __re
   if (j >= g.ny) return;
   const int i = 2 * ih + ((j + k + color) & 1);
   if (i >= g.nx) return;
-  const long long q = (long long)i + g.sy() * j + g.sz() * k;
-  const T s = lap_nb<T>(e, g, i, j, k, c);
+  const int q = idx3(g, i, j, k);
+  const T s = lap6<T>(e, q, nb6(g, i, j, k), c);
   const T ec = e[q];
   const T en = (r[q] - s) * c.invA;
   e[q] = ec + om * (en - ec);
@@ -298,8 +386,8 @@ __global__ void __launch_bounds__(256) k_resid(const T* __restrict__ e, const T*
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
   if (i >= g.nx || j >= g.ny) return;
-  const long long q = (long long)i + g.sy() * j + g.sz() * k;
-  t[q] = r[q] - (lap_nb<T>(e, g, i, j, k, c) + c.A * e[q]);
+  const int q = idx3(g, i, j, k);
+  t[q] = r[q] - (lap6<T>(e, q, nb6(g, i, j, k), c) + c.A * e[q]);
 }
 
 struct Coarsen {
@@ -340,6 +428,36 @@ __global__ void __launch_bounds__(256) k_restrict(const T* __restrict__ tf, T* _
     }
   }
   rc[(long long)I + gc.sy() * J + gc.sz() * K] = acc;
+}
+
+// full weighting when every axis is coarsened: the 3 x 3 x 3 fine block of
+// each coarse point, offsets resolved once per axis, separable weights
+template <class T>
+__global__ void __launch_bounds__(256) k_restrict_full(const T* __restrict__ tf, T* __restrict__ rc, Grid gf,
+                                                       Grid gc, const SolveCtrl* ctrl) {
+  if (ctrl->done) return;
+  const int I = blockIdx.x * blockDim.x + threadIdx.x;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y;
+  const int K = blockIdx.z;
+  if (I >= gc.nx || J >= gc.ny) return;
+  int xo[3], yo[3], zo[3];
+#pragma unroll
+  for (int o = 0; o < 3; ++o) {
+    xo[o] = fine_of(I, o - 1, gf.nx, gf.bc[0], 1);
+    yo[o] = gf.nx * fine_of(J, o - 1, gf.ny, gf.bc[1], 1);
+    zo[o] = gf.nx * gf.ny * fine_of(K, o - 1, gf.nz, gf.bc[2], 1);
+  }
+  const T w[3] = {(T)0.25, (T)0.5, (T)0.25};
+  T acc = (T)0;
+#pragma unroll
+  for (int oz = 0; oz < 3; ++oz)
+#pragma unroll
+    for (int oy = 0; oy < 3; ++oy) {
+      const T* row = tf + zo[oz] + yo[oy];
+#pragma unroll
+      for (int ox = 0; ox < 3; ++ox) acc += w[oz] * w[oy] * w[ox] * __ldg(row + xo[ox]);
+    }
+  rc[idx3(gc, I, J, K)] = acc;
 }
 
 // coarse indices and weights of fine index i along one axis
@@ -538,7 +656,8 @@ static void vcycle(MGLevel* lv, int l, int nlev, int pre, int post, int coarse_s
   const MGLevel& C = lv[l + 1];
   Coarsen cz;
   for (int a = 0; a < 3; ++a) cz.c[a] = L.coarsen[a];
-  k_restrict<T><<<g3(C.g), b, 0, s>>>((const T*)L.t, (T*)C.r, L.g, C.g, cz, ctrl);
+  if (cz.c[0] && cz.c[1] && cz.c[2]) k_restrict_full<T><<<g3(C.g), b, 0, s>>>((const T*)L.t, (T*)C.r, L.g, C.g, ctrl);
+  else k_restrict<T><<<g3(C.g), b, 0, s>>>((const T*)L.t, (T*)C.r, L.g, C.g, cz, ctrl);
   *nl += 2;
   vcycle<T>(lv, l + 1, nlev, pre, post, coarse_sweeps, om, ctrl, s, nl, true);
   if (cz.c[0] && cz.c[1] && cz.c[2])
@@ -555,7 +674,7 @@ template <class T, class R>
 void launch_mg_resid(double* p, const R* rhs, MGLevel* lv, SolveCtrl* ctrl, cudaStream_t s, long long* nl) {
   const MGLevel& L0 = lv[0];
   PoiCoef<double> c64 = make_poi<double>(L0.h[0], L0.h[1], L0.h[2]);
-  k_resid_top_max<T, R><<<g3(L0.g), dim3(32, 8), 0, s>>>(p, rhs, (T*)L0.r, L0.g, c64, ctrl);
+  k_resid25<T, R, true><<<rz_grid(L0.g), dim3(RZ_TX, RZ_TY), 0, s>>>(p, rhs, (T*)L0.r, L0.g, c64, ctrl);
   *nl += 1;
 }
 
@@ -616,29 +735,37 @@ __global__ void k_extrapolate_d(double* __restrict__ p, double* __restrict__ ppr
 // prolong(S_r y) starts the first V-cycle (multigrid) or is added to p
 // (SOR).
 // ---------------------------------------------------------------------------
-// S_r = rms(r h^2), S_d = rms(d) over the coarse grid (one block)
+// S_r = rms(r h^2), S_d = rms(d) over the coarse grid (one block; the
+// scales need no more than FP32 accumulation)
 template <class T>
 __global__ void k_rms(const T* __restrict__ r, const T* __restrict__ d, long long n, double h2, SolveCtrl* ctrl) {
-  __shared__ double sh[2][1024];
-  double a = 0.0, b = 0.0;
+  __shared__ float sh[2][32];
+  float a = 0.f, b = 0.f;
   for (long long q = threadIdx.x; q < n; q += blockDim.x) {
-    const double rv = (double)r[q] * h2, dv = (double)d[q];
-    a += rv * rv;
-    b += dv * dv;
+    const float rv = (float)r[q], dv = (float)d[q];
+    a = fmaf(rv, rv, a);
+    b = fmaf(dv, dv, b);
   }
-  sh[0][threadIdx.x] = a;
-  sh[1][threadIdx.x] = b;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+  if (l == 0) { sh[0][w] = a; sh[1][w] = b; }
   __syncthreads();
-  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
-    if ((int)threadIdx.x < st) {
-      sh[0][threadIdx.x] += sh[0][threadIdx.x + st];
-      sh[1][threadIdx.x] += sh[1][threadIdx.x + st];
+  if (w == 0) {
+    a = l < nw ? sh[0][l] : 0.f;
+    b = l < nw ? sh[1][l] : 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      b += __shfl_xor_sync(0xffffffffu, b, o);
     }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    ctrl->learn_scale = sqrt(sh[0][0] / (double)n) + 1e-300;
-    ctrl->learn_scale_d = sqrt(sh[1][0] / (double)n) + 1e-300;
+    if (l == 0) {
+      ctrl->learn_scale = sqrt((double)a / (double)n) * h2 + 1e-300;
+      ctrl->learn_scale_d = sqrt((double)b / (double)n) + 1e-300;
+    }
   }
 }
 
@@ -706,7 +833,10 @@ static T* restrict_to(MGLevel* lv, int ll, const T* f0, int which, SolveCtrl* ct
     Coarsen cz;
     for (int a = 0; a < 3; ++a) cz.c[a] = lv[l].coarsen[a];
     dst = (T*)(which ? lv[l + 1].t : lv[l + 1].e);
-    k_restrict<T><<<g3(lv[l + 1].g), dim3(32, 8), 0, s>>>(src, dst, lv[l].g, lv[l + 1].g, cz, ctrl);
+    if (cz.c[0] && cz.c[1] && cz.c[2])
+      k_restrict_full<T><<<g3(lv[l + 1].g), dim3(32, 8), 0, s>>>(src, dst, lv[l].g, lv[l + 1].g, ctrl);
+    else
+      k_restrict<T><<<g3(lv[l + 1].g), dim3(32, 8), 0, s>>>(src, dst, lv[l].g, lv[l + 1].g, cz, ctrl);
     src = dst;
     *nl += 1;
   }
@@ -788,20 +918,26 @@ O3D_LEARN_INST(double)
 template <class R>
 void launch_rhs_wmean(const R* rhs, const Grid& g, double* part, SolveCtrl* ctrl, cudaStream_t s,
                       long long* nl) {
-  const dim3 grid((g.nx + 31) / 32, (g.ny + 7) / 8, 1);
+  const dim3 grid((g.nx + 31) / 32, (g.ny + 7) / 8, (g.nz + WM_KC - 1) / WM_KC);
   // sum of the weights: per axis n (periodic) or n - 1 (mirror: halves at both ends)
   double wsum = 1.0;
   for (int a = 0; a < 3; ++a) wsum *= g.bc[a] == AX_MIRROR ? (double)(g.len(a) - 1) : (double)g.len(a);
   k_wmean_part<R><<<grid, dim3(32, 8), 0, s>>>(rhs, g, part);
-  k_wmean_final<<<1, 1024, 0, s>>>(part, (long long)grid.x * grid.y, wsum, ctrl);
+  k_wmean_final<<<1, 1024, 0, s>>>(part, (long long)grid.x * grid.y * grid.z, wsum, ctrl);
   *nl += 2;
 }
 
 template <class R>
-void launch_residual_inf(const double* p, const R* rhs, const Grid& g, const PoiCoef<double>& c,
-                         int use_mean, SolveCtrl* ctrl, cudaStream_t s) {
-  k_resid_inf<R><<<g3(g), dim3(32, 8), 0, s>>>(p, rhs, g, c, use_mean, ctrl);
+void launch_residual_inf(const double* p, const R* rhs, const Grid& g, const PoiCoef<double>& c, SolveCtrl* ctrl,
+                         cudaStream_t s) {
+  k_resid_inf<R><<<g3(g), dim3(32, 8), 0, s>>>(p, rhs, g, c, ctrl);
 }
+template <class R>
+void launch_rhs_shift(R* rhs, long long n, SolveCtrl* ctrl, cudaStream_t s) {
+  k_rhs_shift<R><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(rhs, n, ctrl);
+}
+template void launch_rhs_shift<float>(float*, long long, SolveCtrl*, cudaStream_t);
+template void launch_rhs_shift<double>(double*, long long, SolveCtrl*, cudaStream_t);
 
 template <class T, class R>
 void launch_level_kernel(int which, double* p, const R* rhs, const MGLevel& L, SolveCtrl* ctrl,
@@ -811,7 +947,7 @@ void launch_level_kernel(int which, double* p, const R* rhs, const MGLevel& L, S
     k_smooth<T><<<g3rb(L.g), dim3(32, 8), 0, s>>>((T*)L.e, (const T*)L.r, L.g, c, 0, (T)1, ctrl);
   } else {
     PoiCoef<double> c64 = make_poi<double>(L.h[0], L.h[1], L.h[2]);
-    k_resid_top<T, R><<<g3(L.g), dim3(32, 8), 0, s>>>(p, rhs, (T*)L.r, L.g, c64, ctrl);
+    k_resid25<T, R, false><<<rz_grid(L.g), dim3(RZ_TX, RZ_TY), 0, s>>>(p, rhs, (T*)L.r, L.g, c64, ctrl);
   }
 }
 template void launch_level_kernel<float, float>(int, double*, const float*, const MGLevel&, SolveCtrl*,
@@ -826,8 +962,8 @@ template void launch_mg_outer<float, float>(double*, const float*, MGLevel*, int
 template void launch_rhs_wmean<double>(const double*, const Grid&, double*, SolveCtrl*, cudaStream_t, long long*);
 template void launch_rhs_wmean<float>(const float*, const Grid&, double*, SolveCtrl*, cudaStream_t, long long*);
 template void launch_residual_inf<double>(const double*, const double*, const Grid&, const PoiCoef<double>&,
-                                          int, SolveCtrl*, cudaStream_t);
+                                          SolveCtrl*, cudaStream_t);
 template void launch_residual_inf<float>(const double*, const float*, const Grid&, const PoiCoef<double>&,
-                                         int, SolveCtrl*, cudaStream_t);
+                                         SolveCtrl*, cudaStream_t);
 
 }  // namespace o3d

@@ -163,21 +163,33 @@ __global__ void k_scalar_redistribute(T* __restrict__ phi, long long n, const do
 // ---------------------------------------------------------------------------
 // fixed-order finalizers
 // ---------------------------------------------------------------------------
+// G = (warps / M) warps per slot q: lane l of part g folds the records
+// g*32 + l, (G + g)*32 + l, ... in order, the lanes fold by a fixed shuffle
+// tree and the G parts in order (deterministic).
 __global__ void k_finalize(const double* __restrict__ part, long long nblk, int M,
                            unsigned long long opmask, double* out) {
-  __shared__ double sh[1024];
-  for (int q = 0; q < M; ++q) {
-    const int op = (int)((opmask >> (2 * q)) & 3ull);
-    double acc = red_ident(op);
-    const double* slot = part + (long long)q * nblk;
-    for (long long b = threadIdx.x; b < nblk; b += blockDim.x) acc = red_apply(op, acc, slot[b]);
-    sh[threadIdx.x] = acc;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-      if ((int)threadIdx.x < s) sh[threadIdx.x] = red_apply(op, sh[threadIdx.x], sh[threadIdx.x + s]);
-      __syncthreads();
+  __shared__ double sh[32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const int G = nw / M > 0 ? nw / M : 1;
+  for (int base = 0; base < M; base += nw / G) {
+    const int q = base + warp / G, g = warp % G;
+    double acc = 0.0;
+    int op = 0;
+    if (q < M && warp / G < nw / G) {
+      op = (int)((opmask >> (2 * q)) & 3ull);
+      acc = red_ident(op);
+      const double* slot = part + (long long)q * nblk;
+      for (long long b = (long long)g * 32 + lane; b < nblk; b += 32LL * G) acc = red_apply(op, acc, slot[b]);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc = red_apply(op, acc, __shfl_xor_sync(0xffffffffu, acc, o));
+      if (lane == 0) sh[warp] = acc;
     }
-    if (threadIdx.x == 0) out[q] = sh[0];
+    __syncthreads();
+    if (q < M && warp / G < nw / G && g == 0 && lane == 0) {
+      double v = sh[warp];
+      for (int h = 1; h < G; ++h) v = red_apply(op, v, sh[warp + h]);
+      out[q] = v;
+    }
     __syncthreads();
   }
 }

@@ -580,8 +580,15 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
   CK(cudaEventRecord(c->ev[2], c->s));
   const bool use_mg = c->P.solver == O3D_SOLVER_MG;
   if (use_mg || learned || sampling) {
-    if (c->mixed) launch_rhs_wmean<float>((const float*)c->rhs, c->gp, c->part, c->ctrl, c->s, &c->launches);
-    else launch_rhs_wmean<double>((const double*)c->rhs, c->gp, c->part, c->ctrl, c->s, &c->launches);
+    // remove the weighted mean from the rhs in place (compatibility of the singular problem)
+    if (c->mixed) {
+      launch_rhs_wmean<float>((const float*)c->rhs, c->gp, c->part, c->ctrl, c->s, &c->launches);
+      launch_rhs_shift<float>((float*)c->rhs, c->g.n, c->ctrl, c->s);
+    } else {
+      launch_rhs_wmean<double>((const double*)c->rhs, c->gp, c->part, c->ctrl, c->s, &c->launches);
+      launch_rhs_shift<double>((double*)c->rhs, c->g.n, c->ctrl, c->s);
+    }
+    c->launches++;
     CKL();
   }
   c->sample_ready = 0;
@@ -656,8 +663,8 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
   if (!use_mg || c->P.diagnostics >= 2) {
     PoiCoef<double> pc = make_poi<double>(c->dx, c->dy, c->dz);
     CK(cudaMemsetAsync(&c->ctrl->res_key, 0, sizeof(unsigned long long), c->s));
-    if (c->mixed) launch_residual_inf<float>(c->pp, (const float*)c->rhs, c->gp, pc, use_mg, c->ctrl, c->s);
-    else launch_residual_inf<double>(c->pp, (const double*)c->rhs, c->gp, pc, use_mg, c->ctrl, c->s);
+    if (c->mixed) launch_residual_inf<float>(c->pp, (const float*)c->rhs, c->gp, pc, c->ctrl, c->s);
+    else launch_residual_inf<double>(c->pp, (const double*)c->rhs, c->gp, pc, c->ctrl, c->s);
     c->launches++;
     CKL();
   }

@@ -158,7 +158,9 @@ template <class R>
 void launch_rhs_wmean(const R* rhs, const Grid& g, double* part, SolveCtrl* ctrl, cudaStream_t s,
                       long long* nl);
 template <class R>
-void launch_residual_inf(const double* p, const R* rhs, const Grid& g, const PoiCoef<double>& c,
-                         int use_mean, SolveCtrl* ctrl, cudaStream_t s);
+void launch_residual_inf(const double* p, const R* rhs, const Grid& g, const PoiCoef<double>& c, SolveCtrl* ctrl,
+                         cudaStream_t s);
+template <class R>
+void launch_rhs_shift(R* rhs, long long n, SolveCtrl* ctrl, cudaStream_t s);
 
 }  // namespace o3d
