@@ -410,7 +410,10 @@ __global__ void __launch_bounds__(TX * TY) k_div25(const T* __restrict__ fx, con
   }
   T mn = (T)INFINITY, mx = (T)-INFINITY;
   long long imx = 0x7fffffffffffffffll;
+  // column sum: FP64 for T = double; a TwoSum-compensated FP32 pair for
+  // T = float (exact to ~2^-48 over the chunk), widened once at the end
   double sum = 0.0;
+  float sum_hi = 0.f, sum_lo = 0.f;
   for (int lb = 0; lb < np; lb += ZQ) {
 #pragma unroll
     for (int u = 0; u < ZQ; ++u) {
@@ -435,7 +438,8 @@ __global__ void __launch_bounds__(TX * TY) k_div25(const T* __restrict__ fx, con
         if (valid) {
           const long long p = out0 + sz * (k0 + lp);
           if (out) out[p] = (O)(divide ? div / dt : div);
-          sum += to_t<double>(div);
+          if constexpr (sizeof(T) == 4) two_sum_acc(sum_hi, sum_lo, (float)div);
+          else sum += (double)div;
           if (div < mn) mn = div;
           if (div > mx) { mx = div; imx = p; }  // k ascends: the first max of the column is kept
         }
@@ -443,11 +447,10 @@ __global__ void __launch_bounds__(TX * TY) k_div25(const T* __restrict__ fx, con
     }
   }
   cp_async_wait<0>();
+  if constexpr (sizeof(T) == 4) sum = to_t<double>(sum_hi) + to_t<double>(sum_lo);
   if (part) {
-    StatPart st;
-    st.mn = to_t<double>(mn); st.mx = to_t<double>(mx); st.sum = sum; st.imx = imx;
-    if (!(mx >= mn)) { st.mn = INFINITY; st.mx = -INFINITY; st.imx = 0x7fffffffffffffffll; }
-    block_stat(st, part, block_linear_id());
+    if (!(mx >= mn)) { mn = (T)INFINITY; mx = (T)-INFINITY; imx = 0x7fffffffffffffffll; }
+    block_stat_t<T>(mn, mx, sum, imx, part, block_linear_id());
   }
 }
 
@@ -573,17 +576,17 @@ __global__ void __launch_bounds__(TX * TY) k_correct25(CorrArgs<T, S> A, int kc)
     }
   }
   cp_async_wait<0>();
-  double r[10];
+  T r[10];
   const int ops[10] = {RED_MIN, RED_MIN, RED_MIN, RED_MAX, RED_MAX, RED_MAX,
                        RED_MAX, RED_MAX, RED_MAX, RED_MAX};
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    r[a] = to_t<double>(mn[a]);
-    r[3 + a] = to_t<double>(mx[a]);
-    r[6 + a] = to_t<double>(am[a]);
+    r[a] = mn[a];
+    r[3 + a] = mx[a];
+    r[6 + a] = am[a];
   }
-  r[9] = nan ? 1.0 : 0.0;
-  block_reduce_store<10>(r, ops, A.part, block_linear_id());
+  r[9] = nan ? (T)1 : (T)0;
+  block_reduce_store_t<T, 10>(r, ops, A.part, block_linear_id());
 }
 
 // ---------------------------------------------------------------------------

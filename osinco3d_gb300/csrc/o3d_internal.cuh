@@ -91,6 +91,11 @@ __device__ __forceinline__ T ld(const T* __restrict__ p, long long i) { return _
 // 4.3.1).  Zeros and normal numbers take the integer path; subnormal,
 // infinite, NaN and out-of-range values fall back to the FP64 instruction.
 // Results are bit-identical to __double2float_rn and to the exact widening.
+// The fallbacks are out of line so that the compiler cannot turn the branch
+// into a select that runs the FP64 instruction for every value.
+static __device__ __noinline__ float f64_to_f32_rare(double x) { return __double2float_rn(x); }
+static __device__ __noinline__ double f32_to_f64_rare(float x) { return (double)x; }
+
 __device__ __forceinline__ float f64_to_f32(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
@@ -103,7 +108,7 @@ __device__ __forceinline__ float f64_to_f32(double x) {
     return __uint_as_float(sign | f);
   }
   if (((hi << 1) | lo) == 0u) return __uint_as_float(sign);  // +-0
-  return __double2float_rn(x);
+  return f64_to_f32_rare(x);
 }
 
 __device__ __forceinline__ double f32_to_f64(float x) {
@@ -112,7 +117,18 @@ __device__ __forceinline__ double f32_to_f64(float x) {
   if (e - 1u <= 253u)                              // normal: exact widening
     return __hiloint2double((int)((u & 0x80000000u) | ((e + 896u) << 20) | ((u >> 3) & 0xfffffu)), (int)(u << 29));
   if ((u << 1) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);  // +-0
-  return (double)x;
+  return f32_to_f64_rare(x);
+}
+
+// Knuth's TwoSum: s + err == a + b exactly (round-to-nearest FP32), six FP32
+// operations.  Accumulating (hi, lo) with it keeps a column sum of FP32
+// values to about 2^-48 of its magnitude without FP64 arithmetic.
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
+  const float s = hi + x;
+  const float bp = s - hi;
+  const float err = (hi - (s - bp)) + (x - bp);
+  hi = s;
+  lo += err;
 }
 
 // conversion of a loaded value to the compute type
@@ -263,6 +279,43 @@ __device__ inline void block_stat(StatPart s, StatPart* part, long long blk) {
   }
 }
 
+// The same record reduced with the extrema in the field type T (min/max in
+// FP32 are exact and stay off the FP64 pipe, which GB300 runs at 2 lanes
+// per clock) and the sum in FP64; the block record is stored as StatPart.
+template <class T>
+__device__ inline void block_stat_t(T mn, T mx, double sum, long long imx, StatPart* part, long long blk) {
+  __shared__ T shm[2][32];
+  __shared__ double shs[32];
+  __shared__ long long shi[32];
+  const int t = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int nt = blockDim.x * blockDim.y * blockDim.z;
+  auto merge = [&](T omn, T omx, double osum, long long oimx) {
+    mn = omn < mn ? omn : mn;
+    if (omx > mx || (omx == mx && oimx < imx)) { mx = omx; imx = oimx; }
+    sum += osum;
+  };
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    merge(__shfl_xor_sync(0xffffffffu, mn, o), __shfl_xor_sync(0xffffffffu, mx, o),
+          __shfl_xor_sync(0xffffffffu, sum, o), __shfl_xor_sync(0xffffffffu, imx, o));
+  __syncthreads();
+  if ((t & 31) == 0) { shm[0][t >> 5] = mn; shm[1][t >> 5] = mx; shs[t >> 5] = sum; shi[t >> 5] = imx; }
+  __syncthreads();
+  if (t < 32) {
+    if (t < (nt + 31) / 32) { mn = shm[0][t]; mx = shm[1][t]; sum = shs[t]; imx = shi[t]; }
+    else { mn = (T)INFINITY; mx = (T)-INFINITY; sum = 0.0; imx = 0x7fffffffffffffffll; }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+      merge(__shfl_xor_sync(0xffffffffu, mn, o), __shfl_xor_sync(0xffffffffu, mx, o),
+            __shfl_xor_sync(0xffffffffu, sum, o), __shfl_xor_sync(0xffffffffu, imx, o));
+    if (t == 0) {
+      StatPart r;
+      r.mn = to_t<double>(mn); r.mx = to_t<double>(mx); r.sum = sum; r.imx = imx;
+      part[blk] = r;
+    }
+  }
+}
+
 __device__ __forceinline__ StatPart stat_of(double v, long long idx, bool valid) {
   StatPart s;
   if (valid && !(v != v)) { s.mn = v; s.mx = v; s.sum = v; s.imx = idx; }
@@ -310,6 +363,45 @@ __device__ inline void block_reduce_store(double (&v)[M], const int (&ops)[M], d
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) x = red_apply(ops[q], x, __shfl_xor_sync(0xffffffffu, x, o));
       if (t == 0) part[(long long)q * nblk + blk] = x;
+    }
+  }
+}
+
+// The same reduction carried out in T (slots with RED_MIN / RED_MAX only
+// need T's exact min/max), the block's records widened to FP64 on store.
+template <class T>
+__device__ __forceinline__ T red_apply_t(int op, T a, T b) {
+  return op == RED_SUM ? a + b : op == RED_MIN ? (b < a ? b : a) : (b > a ? b : a);
+}
+template <class T>
+__device__ __forceinline__ T red_ident_t(int op) {
+  return op == RED_SUM ? (T)0 : op == RED_MIN ? (T)INFINITY : (T)-INFINITY;
+}
+template <class T, int M>
+__device__ inline void block_reduce_store_t(T (&v)[M], const int (&ops)[M], double* part, long long blk) {
+  const long long nblk = (long long)gridDim.x * gridDim.y * gridDim.z;
+  __shared__ T sh[M][32];
+  const int t = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int nt = blockDim.x * blockDim.y * blockDim.z;
+  const int nw = (nt + 31) / 32;
+#pragma unroll
+  for (int q = 0; q < M; ++q) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[q] = red_apply_t<T>(ops[q], v[q], __shfl_xor_sync(0xffffffffu, v[q], o));
+  }
+  __syncthreads();
+  if ((t & 31) == 0) {
+#pragma unroll
+    for (int q = 0; q < M; ++q) sh[q][t >> 5] = v[q];
+  }
+  __syncthreads();
+  if (t < 32) {
+#pragma unroll
+    for (int q = 0; q < M; ++q) {
+      T x = t < nw ? sh[q][t] : red_ident_t<T>(ops[q]);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x = red_apply_t<T>(ops[q], x, __shfl_xor_sync(0xffffffffu, x, o));
+      if (t == 0) part[(long long)q * nblk + blk] = to_t<double>(x);
     }
   }
 }
