@@ -38,9 +38,15 @@ WORKLOAD = ("Taylor-Green vortex 256^3 periodic [0,2pi)^3 (xlx = 2pi*255/256), R
 # algorithmic bytes per grid point of one launch (float32 storage)
 PRED_BYTES_PER_PT = 15 * 4   # read u,v,w + 6 history, write 3 u* + 3 fluxes
 
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from the
-# ncu capture summarised in profiles/; None until measured
-TRAFFIC_PER_LAUNCH: dict = {}
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
+# 256^3 launches, from the ncu captures summarised in profiles/
+TRAFFIC_PER_LAUNCH: dict = {
+    "mg_smooth": (134.744832 + 18.91968) * 1e6,   # k_smooth_tgv256_finest.md
+    "predict": (623.436032 + 365.83552) * 1e6,    # k_predict25_tgv256.md
+    "rhs": (202.962432 + 3.673088) * 1e6,         # k_div25_tgv256.md (statistics pass, no rhs write)
+    "correct": (339.60832 + 169.290496) * 1e6,    # k_correct25_tgv256.md
+    "resid64": (204.871168 + 49.45792) * 1e6,     # k_resid25_tgv256.md
+}
 
 
 # ---------------------------------------------------------------------------
@@ -233,9 +239,12 @@ KERNEL_BYTES = {
 }
 # FP64 operations per point of the FP64 residual (its bound is the FP64 pipe)
 RESID64_FP64_OPS = 7
-# the kernel the roofline entry describes: the fused predictor, the largest
-# single HBM-bound kernel of the step
-ROOF_KERNEL = "predict"
+# the kernel the roofline entry describes: the finest-level multigrid
+# smoother, the largest HBM-bound share of the step (the FP64 residual, of
+# equal share, is bound by the FP64 pipe and reported beside it)
+ROOF_KERNEL = "mg_smooth"
+# GB300 FP64 pipe: 2 lanes per clock per SM, 152 SMs, 2.07 GHz
+FP64_PEAK_GOPS = 2 * 152 * 2.07
 
 
 def kernel_roofline(o3d, ctx, peaks: dict) -> dict:
@@ -251,6 +260,9 @@ def kernel_roofline(o3d, ctx, peaks: dict) -> dict:
                      "frac": gbs / peak if peak else None}
     r = out["resid64"]
     r["fp64_gops"] = RESID64_FP64_OPS * N ** 3 / (r["ms"] * 1e-3) / 1e9
+    r["fp64_frac"] = r["fp64_gops"] / FP64_PEAK_GOPS
+    for name, v in out.items():
+        v["traffic"] = TRAFFIC_PER_LAUNCH.get(name)
     return out
 
 
