@@ -178,6 +178,48 @@ def tgv_params(n: int, **kw) -> Params:
     return default_params(**base)
 
 
+def mixing_layer_params(nx: int = 512, ny: int = 256, nz: int = 256, lx: float = 60.0, ly: float = 30.0,
+                        lz: float = 30.0, cfl: float = 0.2, ratio: float = 0.5, **kw) -> Params:
+    """Temporal mixing layer: x and z periodic (xlx = lx (nx-1)/nx, zlz likewise),
+    y free-slip on [-ly/2, ly/2] node-inclusive, Re 3000, Smagorinsky c_s 0.17,
+    passive scalar Sc 1, AB3; dt from the CFL number on the faster stream
+    u2 = u0 / (1 - ratio)."""
+    u2 = 1.0 / (1.0 - ratio) if abs(ratio) > 1e-12 else 1.0
+    xl, zl = lx * (nx - 1) / nx, lz * (nz - 1) / nz
+    base = dict(nx=nx, ny=ny, nz=nz, xlx=xl, yly=ly, zlz=zl, x0=0.0, y0=-0.5 * ly, z0=0.0,
+                nbcx1=0, nbcxn=0, nbcy1=1, nbcyn=1, nbcz1=0, nbczn=0, re=3000.0, iles=1, cs=0.17,
+                nscr=1, sc=1.0, itscheme=3, dt=cfl * (xl / (nx - 1)) / u2)
+    base.update(kw)
+    return default_params(**base)
+
+
+def mixing_layer_fields(params: Params, ratio: float = 0.5, u0: float = 1.0, l0: float = 1.0,
+                        noise: float = 0.05, seed: int = 1234):
+    """Initial state of the mixing layer of src/initial_conditions.f90:329-394:
+    u = (u2 + u1)/2 - (u1 - u2)/2 tanh(y ln2 / (2 theta)), u2 = u0/(1 - ratio),
+    u1 = ratio u2, theta = 1/(13 l0); v = w = 0; p = 1; phi = 1/2 - 1/2 tanh(.).
+    The reference's clock-seeded noise is replaced by seeded uniform noise
+    U(-1, 1) * noise * u0 on the three velocity components."""
+    nx, ny, nz = params.nx, params.ny, params.nz
+    dy = params.yly / (ny - 1)
+    u2 = u0 / (1.0 - ratio) if abs(ratio) > 1e-12 else u0
+    u1 = u2 * ratio if abs(ratio) > 1e-12 else 0.0
+    theta = 1.0 / (13.0 * l0)
+    y = params.y0 + np.arange(ny) * dy
+    t3 = y * math.log(2.0) / (2.0 * theta)
+    prof = 0.5 * (u2 + u1) - 0.5 * (u1 - u2) * np.tanh(t3)
+    shape = (nx, ny, nz)
+    ux = np.asfortranarray(np.broadcast_to(prof[None, :, None], shape).copy())
+    uy = np.zeros(shape, order="F")
+    uz = np.zeros(shape, order="F")
+    rng = np.random.default_rng(seed)
+    for f in (ux, uy, uz):
+        f += noise * u0 * rng.uniform(-1.0, 1.0, shape)
+    pp = np.ones(shape, order="F")
+    phi = np.asfortranarray(np.broadcast_to((0.5 - 0.5 * np.tanh(t3))[None, :, None], shape).copy())
+    return ux, uy, uz, pp, phi
+
+
 def _ptr(a: np.ndarray):
     if a.dtype != np.float64 or not a.flags.f_contiguous:
         raise TypeError("fields must be float64 Fortran-ordered arrays")

@@ -152,3 +152,16 @@ def test_rb_and_lexicographic_share_fixed_point(oracle):
             break
     d = (p1 - p1.mean()) - (p2 - p2.mean())
     assert np.abs(d).max() < 1e-10
+
+
+def test_mixing_layer_initial_state_matches_oracle(oracle, o3d):
+    """The product's mixing-layer initial state (without noise) equals the
+    oracle's restatement of src/initial_conditions.f90:329-394."""
+    p = o3d.mixing_layer_params(16, 17, 8, ratio=0.5)
+    ux, uy, uz, pp, phi = o3d.mixing_layer_fields(p, ratio=0.5, noise=0.0)
+    c = oracle.Case(16, 17, 8, p.xlx, p.yly, p.zlz, bcx=0, bcy=1, bcz=0, dt=p.dt, y0=p.y0, nscr=1, ratio=0.5)
+    s = oracle.State.zeros(c)
+    oracle.init_mixing_layer(c, s)
+    assert np.abs(ux - s.u[0]).max() < 1e-14
+    assert np.abs(phi - s.phi).max() < 1e-14
+    assert np.abs(pp - s.pp).max() == 0.0 and np.abs(uy).max() == 0.0
