@@ -909,7 +909,8 @@ void launch_learn_target(const double* p, const double* pprev, MGLevel* lv, int 
                                       long long*);                                                             \
   template void launch_learn_target<T>(const double*, const double*, MGLevel*, int, SolveCtrl*, const float*, \
                                        float*, cudaStream_t, long long*);                                      \
-  template void launch_mg_resid<T, T>(double*, const T*, MGLevel*, SolveCtrl*, cudaStream_t, long long*);      \
+  template void launch_mg_resid<T, double>(double*, const double*, MGLevel*, SolveCtrl*, cudaStream_t,            \
+                                           long long*);                                                        \
   template void launch_mg_cycles<T>(double*, MGLevel*, int, int, int, int, T, int, bool, SolveCtrl*,           \
                                     cudaStream_t, long long*);
 O3D_LEARN_INST(float)
@@ -950,15 +951,15 @@ void launch_level_kernel(int which, double* p, const R* rhs, const MGLevel& L, S
     k_resid25<T, R, false><<<rz_grid(L.g), dim3(RZ_TX, RZ_TY), 0, s>>>(p, rhs, (T*)L.r, L.g, c64, ctrl);
   }
 }
-template void launch_level_kernel<float, float>(int, double*, const float*, const MGLevel&, SolveCtrl*,
-                                                cudaStream_t);
+template void launch_level_kernel<float, double>(int, double*, const double*, const MGLevel&, SolveCtrl*,
+                                                 cudaStream_t);
 template void launch_level_kernel<double, double>(int, double*, const double*, const MGLevel&, SolveCtrl*,
                                                   cudaStream_t);
 
 template void launch_mg_outer<double, double>(double*, const double*, MGLevel*, int, int, int, int,
                                               double, int, SolveCtrl*, cudaStream_t, long long*);
-template void launch_mg_outer<float, float>(double*, const float*, MGLevel*, int, int, int, int,
-                                            float, int, SolveCtrl*, cudaStream_t, long long*);
+template void launch_mg_outer<float, double>(double*, const double*, MGLevel*, int, int, int, int,
+                                             float, int, SolveCtrl*, cudaStream_t, long long*);
 template void launch_rhs_wmean<double>(const double*, const Grid&, double*, SolveCtrl*, cudaStream_t, long long*);
 template void launch_rhs_wmean<float>(const float*, const Grid&, double*, SolveCtrl*, cudaStream_t, long long*);
 template void launch_residual_inf<double>(const double*, const double*, const Grid&, const PoiCoef<double>&,

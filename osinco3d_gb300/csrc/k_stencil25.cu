@@ -437,7 +437,7 @@ __global__ void __launch_bounds__(TX * TY) k_div25(const T* __restrict__ fx, con
         const T div = ddx + ddy + ddz;
         if (valid) {
           const long long p = out0 + sz * (k0 + lp);
-          if (out) out[p] = (O)(divide ? div / dt : div);
+          if (out) out[p] = to_t<O>(divide ? div / dt : div);
           if constexpr (sizeof(T) == 4) two_sum_acc(sum_hi, sum_lo, (float)div);
           else sum += (double)div;
           if (div < mn) mn = div;
@@ -646,6 +646,8 @@ template void launch_div<double, double>(const double*, const double*, const dou
                                          const Coef3<double>&, int, double, int, StatPart*, cudaStream_t);
 template void launch_div<float, float>(const float*, const float*, const float*, float*, const Grid&,
                                        const Coef3<float>&, int, float, int, StatPart*, cudaStream_t);
+template void launch_div<float, double>(const float*, const float*, const float*, double*, const Grid&,
+                                        const Coef3<float>&, int, float, int, StatPart*, cudaStream_t);
 template void launch_correct<double, double>(const CorrArgs<double, double>&, cudaStream_t);
 template void launch_correct<float, double>(const CorrArgs<float, double>&, cudaStream_t);
 

@@ -189,7 +189,7 @@ void* field_ptr(o3d_ctx* c, int f, bool* is_pp) {
     case O3D_FIELD_PHI: return c->phi;
     case O3D_FIELD_SRC: return c->src;
     case O3D_FIELD_NU_T: return c->nu_t;
-    case O3D_FIELD_RHS: return c->rhs;
+    case O3D_FIELD_RHS: *is_pp = true; return c->rhs;  // FP64 in both methods
     default: break;
   }
   if (f >= O3D_FIELD_FU0 && f < O3D_FIELD_FU0 + 6) {
@@ -259,8 +259,11 @@ int predict_t(o3d_ctx* c, int itime) {
 template <class T>
 int rhs_t(o3d_ctx* c) {
   Coef3<T> cf = cast_coef<T>(c->cf);
-  launch_div<T, T>((const T*)c->up[0], (const T*)c->up[1], (const T*)c->up[2], (T*)c->rhs, c->g, cf,
-                   1, (T)c->P.dt, 1, c->spart, c->s);
+  // the Poisson rhs is FP64 in both methods (the mixed method's FP32
+  // divergence widened exactly), so that removing its weighted mean leaves a
+  // compatible problem to FP64 rounding
+  launch_div<T, double>((const T*)c->up[0], (const T*)c->up[1], (const T*)c->up[2], (double*)c->rhs, c->g, cf,
+                        1, (T)c->P.dt, 1, c->spart, c->s);
   launch_finalize_stats(c->spart, z_blocks(c->g), c->g, c->diag->divp, c->s);
   c->launches += 2;
   CKL();
@@ -455,7 +458,7 @@ int capture_mg(o3d_ctx* c) {
     const int cyc = mg_cycles_of(c);
     const double om = mg_omega_of(c);
     if (c->mixed)
-      launch_mg_outer<float, float>(c->pp, (const float*)c->rhs, c->mg.data(), (int)c->mg.size(), pre,
+      launch_mg_outer<float, double>(c->pp, (const double*)c->rhs, c->mg.data(), (int)c->mg.size(), pre,
                                     post, coarse_sweeps, (float)om, cyc, c->ctrl, c->s, &nl);
     else
       launch_mg_outer<double, double>(c->pp, (const double*)c->rhs, c->mg.data(), (int)c->mg.size(),
@@ -513,10 +516,10 @@ int enqueue_learned_first(o3d_ctx* c, bool learned, bool sampling, bool use_mg, 
   if (c->mixed) launch_learn_extrapolate<float>(c->pp, c->pp_prev, lv, c->s, nl);
   else launch_learn_extrapolate<double>(c->pp, c->pp_prev, lv, c->s, nl);
   if (use_mg) {
-    if (c->mixed) launch_mg_resid<float, float>(c->pp, (const float*)c->rhs, lv, c->ctrl, c->s, nl);
+    if (c->mixed) launch_mg_resid<float, double>(c->pp, (const double*)c->rhs, lv, c->ctrl, c->s, nl);
     else launch_mg_resid<double, double>(c->pp, (const double*)c->rhs, lv, c->ctrl, c->s, nl);
   } else {
-    if (c->mixed) launch_level_kernel<float, float>(1, c->pp, (const float*)c->rhs, lv[0], c->ctrl, c->s);
+    if (c->mixed) launch_level_kernel<float, double>(1, c->pp, (const double*)c->rhs, lv[0], c->ctrl, c->s);
     else launch_level_kernel<double, double>(1, c->pp, (const double*)c->rhs, lv[0], c->ctrl, c->s);
     *nl += 1;
   }
@@ -582,8 +585,8 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
   if (use_mg || learned || sampling) {
     // remove the weighted mean from the rhs in place (compatibility of the singular problem)
     if (c->mixed) {
-      launch_rhs_wmean<float>((const float*)c->rhs, c->gp, c->part, c->ctrl, c->s, &c->launches);
-      launch_rhs_shift<float>((float*)c->rhs, c->g.n, c->ctrl, c->s);
+      launch_rhs_wmean<double>((const double*)c->rhs, c->gp, c->part, c->ctrl, c->s, &c->launches);
+      launch_rhs_shift<double>((double*)c->rhs, c->g.n, c->ctrl, c->s);
     } else {
       launch_rhs_wmean<double>((const double*)c->rhs, c->gp, c->part, c->ctrl, c->s, &c->launches);
       launch_rhs_shift<double>((double*)c->rhs, c->g.n, c->ctrl, c->s);
@@ -663,7 +666,7 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
   if (!use_mg || c->P.diagnostics >= 2) {
     PoiCoef<double> pc = make_poi<double>(c->dx, c->dy, c->dz);
     CK(cudaMemsetAsync(&c->ctrl->res_key, 0, sizeof(unsigned long long), c->s));
-    if (c->mixed) launch_residual_inf<float>(c->pp, (const float*)c->rhs, c->gp, pc, c->ctrl, c->s);
+    if (c->mixed) launch_residual_inf<double>(c->pp, (const double*)c->rhs, c->gp, pc, c->ctrl, c->s);
     else launch_residual_inf<double>(c->pp, (const double*)c->rhs, c->gp, pc, c->ctrl, c->s);
     c->launches++;
     CKL();
@@ -801,7 +804,7 @@ int o3d_create(const o3d_params* p, o3d_ctx** out) {
     for (int h = 0; h < 3 && !st; ++h) st = dalloc(c->s, &c->fu[q][h], fb);
   }
   st = st ? st : dalloc(c->s, &c->nu_t, fb);
-  st = st ? st : dalloc(c->s, &c->rhs, fb);
+  st = st ? st : dalloc(c->s, &c->rhs, (size_t)c->g.n * 8);
   st = st ? st : dalloc(c->s, (void**)&c->pp, (size_t)c->g.n * 8);
   if (!st && p->nscr) {
     st = st ? st : dalloc(c->s, &c->phi, fb);
@@ -979,8 +982,8 @@ int o3d_poisson_solve(o3d_ctx* c, double* pp, const double* rhs, double* omega, 
                       int idyn, int* iters, double* dmax) {
   if (!c || !pp || !rhs || !omega) return O3D_ERR_BADARG;
   CK(cudaMemcpyAsync(c->pp, pp, (size_t)c->g.n * 8, cudaMemcpyHostToDevice, c->s));
-  int st = put_field(c, c->rhs, rhs);
-  if (st) return st;
+  CK(cudaMemcpyAsync(c->rhs, rhs, (size_t)c->g.n * 8, cudaMemcpyHostToDevice, c->s));
+  int st = O3D_OK;
   o3d_step_info info;
   memset(&info, 0, sizeof info);
   const int guess = c->P.guess;
@@ -1187,7 +1190,7 @@ int o3d_time_kernel(o3d_ctx* c, int kernel, int reps, double* ms_per_launch) {
       case 2: return c->mixed ? correct_t<float>(c) : correct_t<double>(c);
       default:
         if (c->mixed)
-          launch_level_kernel<float, float>(kernel - 3, c->pp, (const float*)c->rhs, c->mg[0], c->ctrl, c->s);
+          launch_level_kernel<float, double>(kernel - 3, c->pp, (const double*)c->rhs, c->mg[0], c->ctrl, c->s);
         else
           launch_level_kernel<double, double>(kernel - 3, c->pp, (const double*)c->rhs, c->mg[0], c->ctrl, c->s);
         c->launches++;

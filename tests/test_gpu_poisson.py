@@ -98,6 +98,24 @@ def test_fixed_point_matches_lexicographic_sor(oracle, o3d, shape, bcs, solver):
     assert err < (200 * eps if solver == "sor" else 5 * eps), (err, it)
 
 
+def test_even_free_slip_axis_multigrid(oracle, o3d):
+    """An even free-slip axis cannot be coarsened vertex-centred: the
+    hierarchy keeps it (semi-coarsening) and the multigrid still reaches the
+    lexicographic SOR fixed point, with more V-cycles."""
+    eps = 1e-9
+    c = _case(oracle, (32, 32, 16), (0, 1, 0))
+    rhs = _compatible_rhs(c, 5)
+    ref = oracle.field3(c.shape)
+    st, _, _, _ = oracle.poisson_sor(c, ref, rhs, 1.8, eps * 1e-3, 200000)
+    assert st == oracle.SOR_CONVERGED
+    with o3d.Context(params_of(o3d, c, solver=o3d.SOLVER_MG)) as ctx:
+        got = ctx.field()
+        st, it, dm, om = ctx.poisson_solve(got, rhs, 1.8, eps, 400, 0)
+    assert st == o3d.OK, (st, it, dm)
+    err = np.abs(_demean(got) - _demean(ref)).max()
+    assert err < 5 * eps, (err, it)
+
+
 @pytest.mark.parametrize("shape,bcs", VARIANTS)
 def test_mixed_precision_multigrid(oracle, o3d, shape, bcs):
     """FP32 V-cycles inside the FP64 correction loop reach the FP64 fixed point."""
@@ -110,7 +128,6 @@ def test_mixed_precision_multigrid(oracle, o3d, shape, bcs):
         got = ctx.field()
         st, it, dm, om = ctx.poisson_solve(got, rhs, 1.0, eps, 100, 0)
     assert st == o3d.OK, (st, it, dm)
-    # the rhs itself is rounded to FP32 in the mixed method
     err = np.abs(_demean(got) - _demean(ref)).max()
     assert err < 1e-6 * np.abs(ref).max() + 5 * eps, err
 
