@@ -67,6 +67,18 @@ __device__ __forceinline__ T lap_nb(const S* __restrict__ p, const Grid& g, int 
 // ---------------------------------------------------------------------------
 // red-black SOR sweep of one colour (FP64, reference semantics)
 // ---------------------------------------------------------------------------
+// On a periodic axis with an odd point count the wrap joins two points of
+// the same colour, so the points of its last plane (n - 1) form separate
+// "seam" classes: class bit a is set when coordinate a = n_a - 1 on such an
+// axis.  A sweep updates class 0 red, class 0 black, then each seam class
+// red and black: within a class and colour no two points are neighbours,
+// so this is a Gauss-Seidel ordering (converging to the lexicographic
+// sweep's fixed point) for any point counts.
+__device__ __forceinline__ int seam_bits(const Grid& g) {
+  return (g.bc[0] == AX_PERIODIC && (g.nx & 1) ? 1 : 0) | (g.bc[1] == AX_PERIODIC && (g.ny & 1) ? 2 : 0) |
+         (g.bc[2] == AX_PERIODIC && (g.nz & 1) ? 4 : 0);
+}
+
 __global__ void __launch_bounds__(256) k_sor_rb(double* __restrict__ p, const double* __restrict__ rhs,
                                                 Grid g, PoiCoef<double> c, int color,
                                                 SolveCtrl* ctrl, double omega_fixed, int use_ctrl) {
@@ -75,10 +87,11 @@ __global__ void __launch_bounds__(256) k_sor_rb(double* __restrict__ p, const do
   const int ih = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
+  const int sb = seam_bits(g);  // class 0 only: the seam planes are left to k_sor_seam
   double d = 0.0;
-  if (j < g.ny) {
+  if (j < g.ny - ((sb >> 1) & 1) && k < g.nz - ((sb >> 2) & 1)) {
     const int i = 2 * ih + ((j + k + color) & 1);
-    if (i < g.nx) {
+    if (i < g.nx - (sb & 1)) {
       const int q = idx3(g, i, j, k);
       const double s = lap6<double>(p, q, nb6(g, i, j, k), c);
       const double pc = p[q];
@@ -92,6 +105,61 @@ __global__ void __launch_bounds__(256) k_sor_rb(double* __restrict__ p, const do
     if (threadIdx.x == 0 && threadIdx.y == 0 && bm > 0.0)
       atomicMax(&ctrl->dmax_key, (unsigned long long)__double_as_longlong(bm));
   }
+}
+
+// the points of seam class cls != 0 and one colour, one thread each
+__global__ void __launch_bounds__(256) k_sor_seam(double* __restrict__ p, const double* __restrict__ rhs, Grid g,
+                                                  PoiCoef<double> c, int cls, int color, SolveCtrl* ctrl,
+                                                  double omega_fixed, int use_ctrl) {
+  if (use_ctrl && ctrl->done) return;
+  const double om = use_ctrl ? ctrl->omega : omega_fixed;
+  const int sb = seam_bits(g);
+  // free axes run over 0 .. n - 1, less the seam plane when that axis has one
+  const int ex = (cls & 1) ? 1 : g.nx - (sb & 1);
+  const int ey = (cls & 2) ? 1 : g.ny - ((sb >> 1) & 1);
+  const int ez = (cls & 4) ? 1 : g.nz - ((sb >> 2) & 1);
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double d = 0.0;
+  if (t < (long long)ex * ey * ez) {
+    const int a = (int)(t % ex), b = (int)((t / ex) % ey), e3 = (int)(t / ((long long)ex * ey));
+    const int i = (cls & 1) ? g.nx - 1 : a, j = (cls & 2) ? g.ny - 1 : b, k = (cls & 4) ? g.nz - 1 : e3;
+    if (((i + j + k) & 1) == color) {
+      const int q = idx3(g, i, j, k);
+      const double s = lap6<double>(p, q, nb6(g, i, j, k), c);
+      const double pc = p[q];
+      const double pnew = (rhs[q] - s) * c.invA;
+      d = fabs(pnew - pc);
+      p[q] = pc + om * (pnew - pc);
+    }
+  }
+  if (ctrl) {
+    const double bm = block_max(d);
+    if (threadIdx.x == 0 && bm > 0.0) atomicMax(&ctrl->dmax_key, (unsigned long long)__double_as_longlong(bm));
+  }
+}
+
+static int host_seam_bits(const Grid& g) {
+  return (g.bc[0] == AX_PERIODIC && (g.nx & 1) ? 1 : 0) | (g.bc[1] == AX_PERIODIC && (g.ny & 1) ? 2 : 0) |
+         (g.bc[2] == AX_PERIODIC && (g.nz & 1) ? 4 : 0);
+}
+
+// the seam-class passes of one sweep (none when every periodic axis is even)
+static int sor_seam_passes(double* p, const double* rhs, const Grid& g, const PoiCoef<double>& c, SolveCtrl* ctrl,
+                           double omega, int use_ctrl, cudaStream_t s) {
+  const int sb = host_seam_bits(g);
+  int nl = 0;
+  for (int cls = 1; cls < 8; ++cls) {
+    if ((cls & sb) != cls) continue;
+    const long long ex = (cls & 1) ? 1 : g.nx - (sb & 1);
+    const long long ey = (cls & 2) ? 1 : g.ny - ((sb >> 1) & 1);
+    const long long ez = (cls & 4) ? 1 : g.nz - ((sb >> 2) & 1);
+    const unsigned blocks = (unsigned)((ex * ey * ez + 255) / 256);
+    for (int color = 0; color < 2; ++color) {
+      k_sor_seam<<<blocks, 256, 0, s>>>(p, rhs, g, c, cls, color, ctrl, omega, use_ctrl);
+      ++nl;
+    }
+  }
+  return nl;
 }
 
 // stop test and dynamic omega of src/poisson.f90:110-122, once per sweep
@@ -119,6 +187,7 @@ void launch_sor_fixed(double* p, const double* rhs, const Grid& g, const PoiCoef
                       double omega, SolveCtrl* ctrl, cudaStream_t s) {
   k_sor_rb<<<rb_grid(g), dim3(32, 8), 0, s>>>(p, rhs, g, c, 0, ctrl, omega, 0);
   k_sor_rb<<<rb_grid(g), dim3(32, 8), 0, s>>>(p, rhs, g, c, 1, ctrl, omega, 0);
+  sor_seam_passes(p, rhs, g, c, ctrl, omega, 0, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -360,10 +429,11 @@ __global__ void __launch_bounds__(256) k_smooth(T* __restrict__ e, const T* __re
   e[q] = ec + om * (en - ec);
 }
 
-void launch_sor_sweep_ctrl(double* p, const double* rhs, const Grid& g, const PoiCoef<double>& c,
-                           SolveCtrl* ctrl, cudaStream_t s) {
+int launch_sor_sweep_ctrl(double* p, const double* rhs, const Grid& g, const PoiCoef<double>& c,
+                          SolveCtrl* ctrl, cudaStream_t s) {
   k_sor_rb<<<rb_grid(g), dim3(32, 8), 0, s>>>(p, rhs, g, c, 0, ctrl, 0.0, 1);
   k_sor_rb<<<rb_grid(g), dim3(32, 8), 0, s>>>(p, rhs, g, c, 1, ctrl, 0.0, 1);
+  return 2 + sor_seam_passes(p, rhs, g, c, ctrl, 0.0, 1, s);
 }
 
 // `n` red-black sweeps of A e = r with relaxation om, in place on e

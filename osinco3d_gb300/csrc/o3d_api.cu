@@ -413,14 +413,16 @@ int capture_sor(o3d_ctx* c) {
   PoiCoef<double> pc = make_poi<double>(c->dx, c->dy, c->dz);
   cudaGraph_t graph;
   CK(cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal));
+  long long nodes = 0;
   for (int q = 0; q < c->sor_batch; ++q) {
-    launch_sor_sweep_ctrl(c->pp, (const double*)c->rhs, c->gp, pc, c->ctrl, c->s);
+    nodes += launch_sor_sweep_ctrl(c->pp, (const double*)c->rhs, c->gp, pc, c->ctrl, c->s);
     launch_sor_control(c->ctrl, c->s);
+    nodes += 1;
   }
   CK(cudaStreamEndCapture(c->s, &graph));
   CK(cudaGraphInstantiate(&c->sor_exec, graph, 0));
   CK(cudaGraphDestroy(graph));
-  c->sor_nodes = 3LL * c->sor_batch;
+  c->sor_nodes = nodes;
   return O3D_OK;
 }
 
@@ -769,13 +771,6 @@ int o3d_create(const o3d_params* p, o3d_ctx** out) {
   if (p->nbcx1 == 0 && p->nbcy1 == 0) { c->gp.bc[0] = c->gp.bc[1] = c->gp.bc[2] = AX_PERIODIC; }
   else if (p->nbcx1 == 0) { c->gp.bc[0] = AX_PERIODIC; c->gp.bc[1] = AX_MIRROR; c->gp.bc[2] = AX_PERIODIC; }
   else { c->gp.bc[0] = c->gp.bc[1] = c->gp.bc[2] = AX_MIRROR; }
-  for (int a = 0; a < 3; ++a)
-    if (c->gp.bc[a] == AX_PERIODIC && c->gp.len(a) % 2) {
-      errf("periodic axis %c needs an even point count for red-black ordering (got %d)",
-           "xyz"[a], c->gp.len(a));
-      delete c;
-      return O3D_ERR_BADARG;
-    }
   // src/initialization.f90:182-202
   c->dx = p->xlx / (double)(p->nx - 1);
   c->dy = p->yly / (double)(p->ny - 1);

@@ -118,8 +118,10 @@ struct MGLevel {
   void* t;          // residual scratch (T)
 };
 
-void launch_sor_sweep_ctrl(double* p, const double* rhs, const Grid& g, const PoiCoef<double>& c,
-                           SolveCtrl* ctrl, cudaStream_t s);
+// one red-black sweep (plus the seam-class passes of odd periodic axes);
+// returns the kernels launched
+int launch_sor_sweep_ctrl(double* p, const double* rhs, const Grid& g, const PoiCoef<double>& c,
+                          SolveCtrl* ctrl, cudaStream_t s);
 void launch_sor_control(SolveCtrl* ctrl, cudaStream_t s);
 void launch_sor_fixed(double* p, const double* rhs, const Grid& g, const PoiCoef<double>& c,
                       double omega, SolveCtrl* ctrl, cudaStream_t s);

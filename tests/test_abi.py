@@ -53,7 +53,6 @@ def test_default_params(o3d):
     (dict(nbcx1=1, nbcxn=1), "no Poisson solver"),  # x free-slip, y periodic: no poisson_solver bound
     (dict(itscheme=4), "itscheme"),               # src/integration.f90:99-104
     (dict(nx=5), "too small"),
-    (dict(nx=63), "even point count"),
     (dict(solver=7), "solver"),
 ])
 def test_bad_params_rejected_before_any_device_work(o3d, kw, msg):

@@ -98,6 +98,25 @@ def test_fixed_point_matches_lexicographic_sor(oracle, o3d, shape, bcs, solver):
     assert err < (200 * eps if solver == "sor" else 5 * eps), (err, it)
 
 
+@pytest.mark.parametrize("shape,bcs", [((15, 15, 15), (0, 0, 0)), ((17, 17, 9), (0, 1, 0))])
+def test_odd_periodic_sor_fixed_point(oracle, o3d, shape, bcs):
+    """Odd point counts on periodic axes: the red-black sweep adds seam-class
+    passes (the wrap plane of each odd periodic axis) and still reaches the
+    lexicographic SOR fixed point."""
+    eps = 1e-9
+    c = _case(oracle, shape, bcs)
+    rhs = _compatible_rhs(c, 3)
+    ref = oracle.field3(c.shape)
+    st, _, _, _ = oracle.poisson_sor(c, ref, rhs, 1.6, eps * 1e-3, 200000)
+    assert st == oracle.SOR_CONVERGED
+    with o3d.Context(params_of(o3d, c, solver=o3d.SOLVER_SOR)) as ctx:
+        got = ctx.field()
+        st, it, dm, om = ctx.poisson_solve(got, rhs, 1.6, eps, 100000, 0)
+    assert st == o3d.OK, (st, it, dm)
+    err = np.abs(_demean(got) - _demean(ref)).max()
+    assert err < 200 * eps, (err, it)
+
+
 def test_even_free_slip_axis_multigrid(oracle, o3d):
     """An even free-slip axis cannot be coarsened vertex-centred: the
     hierarchy keeps it (semi-coarsening) and the multigrid still reaches the

@@ -100,6 +100,20 @@ def test_mixing_layer_0011_steps(oracle, o3d):
     ctx.close()
 
 
+def test_mixing_layer_odd_periodic_steps(oracle, o3d):
+    """The layout of the reference's mixing-layer example (odd point counts
+    on the periodic x and z axes, src/../examples/mixing_layer_re3000_les:
+    241 x 241 x 81), scaled down: red-black SOR with the seam classes of the
+    odd periodic axes reaches the lexicographic solver's fixed point."""
+    nx, ny, nz = 31, 33, 17
+    c = oracle.Case(nx, ny, nz, 12.0 * (nx - 1) / nx, 12.0, 4.0 * (nz - 1) / nz, bcx=0, bcy=1, bcz=0,
+                    y0=-6.0, z0=-2.0, ratio=0.5, re=3000.0, iles=1, cs=0.17, nscr=1, sc=1.0,
+                    dt=0.01, omega=1.7, eps=EPS, kmax=100000)
+    s, ctx, infos = _run_both(oracle, o3d, c, 3, init="ml")
+    _check_fields(s, ctx, c)
+    ctx.close()
+
+
 @pytest.mark.parametrize("guess,cycles", [(0, 1), (0, 2), (3, 1), (1, 1)])
 def test_multigrid_step_matches(oracle, o3d, guess, cycles):
     """The multigrid solver inside the step gives the same velocity, whatever
