@@ -198,6 +198,37 @@ O3D_API int o3d_step_host(o3d_ctx *ctx, int itime, double *ux, double *uy, doubl
  * dzeta, <u^2>, <v^2>, <w^2>, nine <(du_i/dx_j)^2>, FP64 reductions. */
 O3D_API int o3d_statistics_calc(o3d_ctx *ctx, double t, double out[17]);
 
+/* ---- output-cadence diagnostics ------------------------------------------
+ * rotational(rotx, roty, rotz, ux, uy, uz, ...) and calculate_Q_criterion
+ * (src/differential_operators.f90:40-108) of the current velocity into host
+ * arrays of nx*ny*nz doubles; any pointer may be NULL. */
+O3D_API int o3d_vorticity(o3d_ctx *ctx, double *rotx, double *roty, double *rotz, double *q_criterion);
+/* old_values (src/utils.f90:209-218): keep the current velocity on the
+ * device for o3d_velocity_residuals. */
+O3D_API int o3d_save_old_velocity(o3d_ctx *ctx);
+/* calculate_residuals (src/utils.f90:93-163) of the current velocity against
+ * the one kept by o3d_save_old_velocity: out = res_u, res_v, res_w (rms of
+ * |old - u|/(2 dt) over the interior points, normalised by nx*ny*nz),
+ * linf_u, linf_v, linf_w (max), each scaled by t_ref/u_ref, then the
+ * 1-based (i, j, k) of each max (the last in i-fastest order on ties). */
+O3D_API int o3d_velocity_residuals(o3d_ctx *ctx, double t_ref, double u_ref, double out[15]);
+
+/* ---- checkpoint and restart ----------------------------------------------
+ * save_fields / read_fields (src/IOfunctions.f90:360-470): the flow-state
+ * file of the reference, stream-unformatted: time (f8), nx ny nz (int32),
+ * x, y, z (f8), then ux, uy, uz, pp, phi (f8, column-major); phi is written
+ * as zeros without a scalar.  o3d_load_fields checks the grid and uploads
+ * the fields; *time may be NULL. */
+O3D_API int o3d_save_fields(o3d_ctx *ctx, const char *path, double time);
+O3D_API int o3d_load_fields(o3d_ctx *ctx, const char *path, double *time);
+/* What the flow-state file lacks for an exact restart: the Adams-Bashforth
+ * flux history of the velocity and the scalar, the previous pressure of the
+ * extrapolated and learned guesses and the dynamic SOR omega.  With both
+ * files, a restarted run continues bit for bit.  No counterpart in the
+ * reference (its restart resets the history). */
+O3D_API int o3d_save_history(o3d_ctx *ctx, const char *path);
+O3D_API int o3d_load_history(o3d_ctx *ctx, const char *path);
+
 /* ---- learned Poisson warm start ------------------------------------------
  * A 3D U-Net (BF16 tensor-core convolutions, FP32 accumulation) corrects the
  * extrapolated pressure p_ex = 2 p(n) - p(n-1).  Its input, on the multigrid

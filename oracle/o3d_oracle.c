@@ -10,6 +10,7 @@
  */
 #include "o3d_oracle.h"
 
+#include <float.h>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -563,6 +564,68 @@ void orc_init_mixing_layer(const orc_model *m, double x0, double y0, double z0,
         pp[c] = 1.0;
       }
     }
+}
+
+/* rotational(rotx, roty, rotz, ux, uy, uz, ...), src/differential_operators.f90:
+ * 40-77: the curl with the even ("p") closures of the bound derivatives */
+void orc_rotational(const orc_model *m, double *const u[3], double *rot[3]) {
+  double *a = fld(m), *b = fld(m);
+  size_t n = npts(m);
+  der1(m, a, u[2], 1, 0); der1(m, b, u[1], 2, 0);          /* deryp(uz), derzp(uy) */
+  for (size_t q = 0; q < n; ++q) rot[0][q] = a[q] - b[q];
+  der1(m, a, u[0], 2, 0); der1(m, b, u[2], 0, 0);          /* derzp(ux), derxp(uz) */
+  for (size_t q = 0; q < n; ++q) rot[1][q] = a[q] - b[q];
+  der1(m, a, u[1], 0, 0); der1(m, b, u[0], 1, 0);          /* derxp(uy), deryp(ux) */
+  for (size_t q = 0; q < n; ++q) rot[2][q] = a[q] - b[q];
+  free(a); free(b);
+}
+
+/* calculate_Q_criterion, src/differential_operators.f90:79-108 */
+void orc_q_criterion(const orc_model *m, double *q, double *const u[3]) {
+  size_t n = npts(m);
+  double *g[9];
+  for (int k = 0; k < 9; ++k) g[k] = fld(m);
+  der1(m, g[0], u[0], 0, 1); der1(m, g[1], u[1], 1, 1); der1(m, g[2], u[2], 2, 1); /* derxi, deryi, derzi */
+  der1(m, g[3], u[0], 1, 0); der1(m, g[4], u[0], 2, 0); der1(m, g[5], u[1], 0, 0); /* duxdy, duxdz, duydx */
+  der1(m, g[6], u[1], 2, 0); der1(m, g[7], u[2], 0, 0); der1(m, g[8], u[2], 1, 0); /* duydz, duzdx, duzdy */
+  for (size_t c = 0; c < n; ++c) {
+    q[c] = -0.5 * (pow(g[0][c], 2.0) + pow(g[1][c], 2.0) + pow(g[2][c], 2.0)) -
+           g[3][c] * g[5][c] - g[4][c] * g[7][c] - g[6][c] * g[8][c];
+  }
+  for (int k = 0; k < 9; ++k) free(g[k]);
+}
+
+/* calculate_residuals, src/utils.f90:93-163: over the interior points
+ * (2..n-1 in Fortran indexing) of each component, the rms and the max of
+ * |old - u| / (2 dt), scaled by t_ref / u_ref, the rms normalised by all
+ * nx ny nz points; the max's location is the last one in loop order
+ * (i fastest), 1-based.  out = res_u, res_v, res_w, linf_u, linf_v, linf_w,
+ * then (i, j, k) of each max. */
+void orc_residuals(const orc_model *m, double *const u[3], double *const old[3], double dt,
+                   double t_ref, double u_ref, double out[15]) {
+  int nx = m->nx, ny = m->ny, nz = m->nz;
+  for (int a = 0; a < 3; ++a) {
+    double res = 0.0, linf = 0.0;
+    int ia = 0, ja = 0, ka = 0;
+    for (int k = 1; k < nz - 1; ++k)
+      for (int j = 1; j < ny - 1; ++j)
+        for (int i = 1; i < nx - 1; ++i) {
+          size_t c = IDX(m, i, j, k);
+          double v = fabs(old[a][c] - u[a][c]) / (2.0 * dt);
+          res += pow(v, 2.0);
+          if (v > linf) linf = v;
+        }
+    for (int k = 1; k < nz - 1; ++k)
+      for (int j = 1; j < ny - 1; ++j)
+        for (int i = 1; i < nx - 1; ++i) {
+          size_t c = IDX(m, i, j, k);
+          double v = fabs(old[a][c] - u[a][c]) / (2.0 * dt);
+          if (fabs(linf - v) <= DBL_MIN) { ia = i + 1; ja = j + 1; ka = k + 1; }
+        }
+    out[a] = (t_ref / u_ref) * sqrt((1.0 / (double)((long long)nx * ny * nz)) * res);
+    out[3 + a] = (t_ref / u_ref) * linf;
+    out[6 + 3 * a] = ia; out[7 + 3 * a] = ja; out[8 + 3 * a] = ka;
+  }
 }
 
 /* one pass of the time loop body, src/osinco3d_main.f90:104-128, no I/O */

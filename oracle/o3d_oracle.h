@@ -84,6 +84,10 @@ void orc_cfl(const orc_model *m, double *const u[3], double out[3]);
 /* out[17] = t, E_k, eps, eps2, dzeta, <u^2>,<v^2>,<w^2>, 9 x <(du_i/dx_j)^2> */
 void orc_statistics(const orc_model *m, double *const u[3], double t,
                     double out[17]);
+void orc_rotational(const orc_model *m, double *const u[3], double *rot[3]);
+void orc_q_criterion(const orc_model *m, double *q, double *const u[3]);
+void orc_residuals(const orc_model *m, double *const u[3], double *const old[3], double dt,
+                   double t_ref, double u_ref, double out[15]);
 
 /* ---- initial_conditions.f90 -------------------------------------------- */
 void orc_init_tgv(const orc_model *m, double x0, double y0, double z0,

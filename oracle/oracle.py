@@ -224,6 +224,32 @@ def statistics(case: Case, state: State, t: float, omp: bool = False) -> np.ndar
     return np.array(out[:])
 
 
+def rotational(case: Case, u) -> list:
+    """curl of u (src/differential_operators.f90:40-77)."""
+    m = case.model()
+    rot = [field3(case.shape) for _ in range(3)]
+    lib().orc_rotational(C.byref(m), (_dp * 3)(*[ptr(a) for a in u]), (_dp * 3)(*[ptr(a) for a in rot]))
+    return rot
+
+
+def q_criterion(case: Case, u) -> np.ndarray:
+    """Q-criterion of u (src/differential_operators.f90:79-108)."""
+    m = case.model()
+    q = field3(case.shape)
+    lib().orc_q_criterion(C.byref(m), ptr(q), (_dp * 3)(*[ptr(a) for a in u]))
+    return q
+
+
+def residuals(case: Case, u, old, dt: float, t_ref: float, u_ref: float) -> np.ndarray:
+    """calculate_residuals (src/utils.f90:93-163): res_u, res_v, res_w,
+    linf_u, linf_v, linf_w, then the 1-based (i, j, k) of each max."""
+    m = case.model()
+    out = (C.c_double * 15)()
+    lib().orc_residuals(C.byref(m), (_dp * 3)(*[ptr(a) for a in u]), (_dp * 3)(*[ptr(a) for a in old]),
+                        C.c_double(dt), C.c_double(t_ref), C.c_double(u_ref), out)
+    return np.array(out[:])
+
+
 class Runner:
     """Drives orc_step like the reference's time loop, keeping omega across steps."""
 

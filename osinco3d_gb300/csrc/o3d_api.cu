@@ -97,6 +97,9 @@ struct o3d_ctx {
   int sample_ready;
   int learn_level;     // multigrid level of the network grid
   double* stage[4];  // FP64 staging buffers for host transfers (lazy)
+  void* uold[3];     // velocity kept by o3d_save_old_velocity (lazy)
+  void* vout[4];     // curl and Q-criterion outputs (lazy)
+  void* rscratch;    // velocity residual block records (lazy)
 
   double* part;      // per-block reduction records
   StatPart* spart;
@@ -836,6 +839,9 @@ int o3d_destroy(o3d_ctx* c) {
   cudaFree(c->feat); cudaFree(c->ynet);
   cudaFree(c->phi); cudaFree(c->phi2); cudaFree(c->src);
   for (int q = 0; q < 4; ++q) cudaFree(c->stage[q]);
+  for (int q = 0; q < 3; ++q) cudaFree(c->uold[q]);
+  for (int q = 0; q < 4; ++q) cudaFree(c->vout[q]);
+  cudaFree(c->rscratch);
   cudaFree(c->part); cudaFree(c->spart); cudaFree(c->diag); cudaFree(c->ctrl);
   if (c->diag_h) cudaFreeHost(c->diag_h);
   if (c->ctrl_h) cudaFreeHost(c->ctrl_h);
@@ -1081,6 +1087,126 @@ int o3d_statistics_calc(o3d_ctx* c, double t, double out[17]) {
   out[4] = S[14] / N;
   for (int q = 0; q < 3; ++q) out[5 + q] = S[q] / N;
   for (int q = 0; q < 9; ++q) out[8 + q] = S[3 + q] / N;
+  return O3D_OK;
+}
+
+}  // extern "C"
+
+namespace o3d {
+int ctx_geometry(o3d_ctx* c, o3d_params* p, int* nx, int* ny, int* nz, double* dx, double* dy, double* dz) {
+  *p = c->P;
+  *nx = c->g.nx; *ny = c->g.ny; *nz = c->g.nz;
+  *dx = c->dx; *dy = c->dy; *dz = c->dz;
+  return O3D_OK;
+}
+
+int ctx_history_state(o3d_ctx* c, double* omega, int* has_prev, double* prev_host) {
+  if (omega) *omega = c->omega;
+  if (has_prev) *has_prev = c->pp_prev && c->pp_prev_valid ? 1 : 0;
+  if (prev_host && c->pp_prev && c->pp_prev_valid) {
+    CK(cudaMemcpyAsync(prev_host, c->pp_prev, (size_t)c->g.n * 8, cudaMemcpyDeviceToHost, c->s));
+    CK(cudaStreamSynchronize(c->s));
+  }
+  return O3D_OK;
+}
+
+int ctx_restore_history(o3d_ctx* c, double omega, int has_prev, const double* prev_host) {
+  c->omega = omega;
+  if (!has_prev) {
+    c->pp_prev_valid = 0;
+    return O3D_OK;
+  }
+  if (!c->pp_prev) {
+    int st = dalloc(c->s, (void**)&c->pp_prev, (size_t)c->g.n * 8);
+    if (st) return st;
+  }
+  CK(cudaMemcpyAsync(c->pp_prev, prev_host, (size_t)c->g.n * 8, cudaMemcpyHostToDevice, c->s));
+  CK(cudaStreamSynchronize(c->s));
+  c->pp_prev_valid = 1;
+  return O3D_OK;
+}
+}  // namespace o3d
+
+extern "C" {
+
+int o3d_vorticity(o3d_ctx* c, double* rotx, double* roty, double* rotz, double* q) {
+  if (!c) return O3D_ERR_BADARG;
+  double* host[4] = {rotx, roty, rotz, q};
+  const size_t tsz = c->mixed ? 4 : 8;
+  for (int k = 0; k < 4; ++k)
+    if (host[k] && !c->vout[k]) {
+      int st = dalloc(c->s, &c->vout[k], (size_t)c->g.n * tsz);
+      if (st) return st;
+    }
+  void* out[4];
+  for (int k = 0; k < 4; ++k) out[k] = host[k] ? c->vout[k] : nullptr;
+  if (c->mixed) {
+    const float* u[3] = {(const float*)c->u[0], (const float*)c->u[1], (const float*)c->u[2]};
+    launch_vorticity<float>(u, (float*)out[0], (float*)out[1], (float*)out[2], (float*)out[3], c->g,
+                            cast_coef<float>(c->cf), c->s);
+  } else {
+    const double* u[3] = {(const double*)c->u[0], (const double*)c->u[1], (const double*)c->u[2]};
+    launch_vorticity<double>(u, (double*)out[0], (double*)out[1], (double*)out[2], (double*)out[3], c->g, c->cf,
+                             c->s);
+  }
+  c->launches++;
+  CKL();
+  for (int k = 0; k < 4; ++k)
+    if (host[k]) {
+      int st = get_field(c, out[k], host[k]);
+      if (st) return st;
+    }
+  CK(cudaStreamSynchronize(c->s));
+  return O3D_OK;
+}
+
+int o3d_save_old_velocity(o3d_ctx* c) {
+  if (!c) return O3D_ERR_BADARG;
+  const size_t bytes = (size_t)c->g.n * (c->mixed ? 4 : 8);
+  for (int a = 0; a < 3; ++a) {
+    if (!c->uold[a]) {
+      int st = dalloc(c->s, &c->uold[a], bytes);
+      if (st) return st;
+    }
+    CK(cudaMemcpyAsync(c->uold[a], c->u[a], bytes, cudaMemcpyDeviceToDevice, c->s));
+  }
+  return O3D_OK;
+}
+
+int o3d_velocity_residuals(o3d_ctx* c, double t_ref, double u_ref, double out[15]) {
+  if (!c || !out) return O3D_ERR_BADARG;
+  if (!c->uold[0]) {
+    errf("o3d_velocity_residuals needs o3d_save_old_velocity first");
+    return O3D_ERR_BADARG;
+  }
+  if (!c->rscratch) {
+    int st = dalloc(c->s, &c->rscratch, vel_residual_scratch_bytes(c->g));
+    if (st) return st;
+  }
+  if (c->mixed) {
+    const float* u[3] = {(const float*)c->u[0], (const float*)c->u[1], (const float*)c->u[2]};
+    const float* o[3] = {(const float*)c->uold[0], (const float*)c->uold[1], (const float*)c->uold[2]};
+    launch_vel_residuals<float>(u, o, c->g, c->P.dt, c->rscratch, c->s);
+  } else {
+    const double* u[3] = {(const double*)c->u[0], (const double*)c->u[1], (const double*)c->u[2]};
+    const double* o[3] = {(const double*)c->uold[0], (const double*)c->uold[1], (const double*)c->uold[2]};
+    launch_vel_residuals<double>(u, o, c->g, c->P.dt, c->rscratch, c->s);
+  }
+  c->launches += 2;
+  CKL();
+  struct { double sum, mx; long long imx; } r[3];
+  CK(cudaMemcpyAsync(r, (const char*)c->rscratch + vel_residual_result_offset(c->g), sizeof r,
+                     cudaMemcpyDeviceToHost, c->s));
+  CK(cudaStreamSynchronize(c->s));
+  const double scale = t_ref / u_ref, N = (double)c->g.n;
+  for (int a = 0; a < 3; ++a) {
+    out[a] = scale * std::sqrt((1.0 / N) * r[a].sum);
+    out[3 + a] = scale * (r[a].mx > 0.0 ? r[a].mx : 0.0);
+    const long long p = r[a].imx < 0 ? 0 : r[a].imx;
+    out[6 + 3 * a] = (double)(p % c->g.nx + 1);
+    out[7 + 3 * a] = (double)((p / c->g.nx) % c->g.ny + 1);
+    out[8 + 3 * a] = (double)(p / ((long long)c->g.nx * c->g.ny) + 1);
+  }
   return O3D_OK;
 }
 

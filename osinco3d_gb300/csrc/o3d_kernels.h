@@ -118,6 +118,23 @@ struct MGLevel {
   void* t;          // residual scratch (T)
 };
 
+// context state for checkpoint and restart (o3d_api.cu, used by o3d_io.cu)
+int ctx_geometry(o3d_ctx* c, o3d_params* p, int* nx, int* ny, int* nz, double* dx, double* dy, double* dz);
+// omega and whether a previous pressure exists; prev_host (may be null)
+// receives the previous pressure
+int ctx_history_state(o3d_ctx* c, double* omega, int* has_prev, double* prev_host);
+int ctx_restore_history(o3d_ctx* c, double omega, int has_prev, const double* prev_host);
+
+// output-cadence diagnostics (k_diag.cu)
+template <class T>
+void launch_vorticity(const T* const u[3], T* rx, T* ry, T* rz, T* q, const Grid& g, const Coef3<T>& cf,
+                      cudaStream_t s);
+template <class T>
+void launch_vel_residuals(const T* const u[3], const T* const old[3], const Grid& g, double dt, void* scratch,
+                          cudaStream_t s);
+size_t vel_residual_scratch_bytes(const Grid& g);
+size_t vel_residual_result_offset(const Grid& g);
+
 // one red-black sweep (plus the seam-class passes of odd periodic axes);
 // returns the kernels launched
 int launch_sor_sweep_ctrl(double* p, const double* rhs, const Grid& g, const PoiCoef<double>& c,

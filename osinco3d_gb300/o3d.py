@@ -124,6 +124,13 @@ def lib(build_if_missing: bool = True):
             "o3d_step": (C.c_int, [vp, C.c_int, C.POINTER(StepInfo)]),
             "o3d_step_host": (C.c_int, [vp, C.c_int, _dp, _dp, _dp, _dp, C.POINTER(StepInfo)]),
             "o3d_statistics_calc": (C.c_int, [vp, C.c_double, _dp]),
+            "o3d_vorticity": (C.c_int, [vp, _dp, _dp, _dp, _dp]),
+            "o3d_save_fields": (C.c_int, [vp, C.c_char_p, C.c_double]),
+            "o3d_load_fields": (C.c_int, [vp, C.c_char_p, _dp]),
+            "o3d_save_history": (C.c_int, [vp, C.c_char_p]),
+            "o3d_load_history": (C.c_int, [vp, C.c_char_p]),
+            "o3d_save_old_velocity": (C.c_int, [vp]),
+            "o3d_velocity_residuals": (C.c_int, [vp, C.c_double, C.c_double, _dp]),
             "o3d_rbsor_sweeps_dev": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, _dp]),
             "o3d_time_kernel": (C.c_int, [vp, C.c_int, C.c_int, _dp]),
             "o3d_check_conversions": (C.c_int, [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)]),
@@ -339,6 +346,39 @@ class Context:
     def statistics_calc(self, t: float) -> np.ndarray:
         out = (C.c_double * 17)()
         self._check(self.L.o3d_statistics_calc(self.h, t, out))
+        return np.array(out[:])
+
+    # -- checkpoint and restart ------------------------------------------------
+    def save_fields(self, path: str, time: float) -> None:
+        """The reference's fields_%06d.bin flow-state file (save_fields)."""
+        self._check(self.L.o3d_save_fields(self.h, os.fsencode(path), time))
+
+    def load_fields(self, path: str) -> float:
+        t = C.c_double(0.0)
+        self._check(self.L.o3d_load_fields(self.h, os.fsencode(path), C.byref(t)))
+        return t.value
+
+    def save_history(self, path: str) -> None:
+        self._check(self.L.o3d_save_history(self.h, os.fsencode(path)))
+
+    def load_history(self, path: str) -> None:
+        self._check(self.L.o3d_load_history(self.h, os.fsencode(path)))
+
+    # -- output-cadence diagnostics ----------------------------------------------
+    def vorticity(self):
+        """(rotx, roty, rotz, Q-criterion) of the current velocity."""
+        out = [self.field() for _ in range(4)]
+        self._check(self.L.o3d_vorticity(self.h, *[a.ctypes.data_as(_dp) for a in out]))
+        return out
+
+    def save_old_velocity(self) -> None:
+        self._check(self.L.o3d_save_old_velocity(self.h))
+
+    def velocity_residuals(self, t_ref: float = 1.0, u_ref: float = 1.0) -> np.ndarray:
+        """res_u, res_v, res_w, linf_u, linf_v, linf_w and the 1-based (i, j, k)
+        of each max (calculate_residuals, src/utils.f90:93-163)."""
+        out = (C.c_double * 15)()
+        self._check(self.L.o3d_velocity_residuals(self.h, t_ref, u_ref, out))
         return np.array(out[:])
 
     # -- learned warm start ----------------------------------------------------

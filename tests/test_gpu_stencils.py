@@ -139,3 +139,41 @@ def test_integer_pipe_conversions_are_bit_exact(o3d):
     over raw patterns, widened-and-nudged binary32 values, exact ties and the
     edges of the binary32 normal range."""
     assert o3d.check_conversions(1 << 24, seed=7) == 0
+
+
+@pytest.mark.parametrize("maker,n", [("periodic", 16), ("free_slip", 13)])
+def test_vorticity_and_q_criterion(oracle, o3d, maker, n):
+    """rotational and calculate_Q_criterion (src/differential_operators.f90:
+    40-108) against the oracle, FP64, 1e-12."""
+    c = periodic_case(oracle, n) if maker == "periodic" else free_slip_case(oracle, n)
+    rng = np.random.default_rng(21)
+    u = [perturbed(np.asfortranarray(rng.standard_normal(c.shape)), 60 + a) for a in range(3)]
+    rot = oracle.rotational(c, u)
+    q = oracle.q_criterion(c, u)
+    with o3d.Context(params_of(o3d, c)) as ctx:
+        for a, name in enumerate(("ux", "uy", "uz")):
+            ctx.upload(name, u[a])
+        got = ctx.vorticity()
+    for a in range(3):
+        assert rel_err(got[a], rot[a]) < 1e-12, a
+    assert rel_err(got[3], q) < 1e-12
+
+
+def test_velocity_residuals(oracle, o3d):
+    """calculate_residuals (src/utils.f90:93-163) of a step against the kept
+    old velocity: rms, max and the max's location equal the oracle's."""
+    c = periodic_case(oracle, 16, omega=1.6, eps=1e-11, kmax=100000)
+    s = oracle.State.zeros(c)
+    oracle.init_tgv(c, s)
+    with o3d.Context(params_of(o3d, c)) as ctx:
+        for a, name in enumerate(("ux", "uy", "uz")):
+            ctx.upload(name, s.u[a])
+        ctx.upload("pp", s.pp)
+        ctx.save_old_velocity()
+        old = [ctx.download(nm) for nm in ("ux", "uy", "uz")]
+        ctx.step(1)
+        got = ctx.velocity_residuals(t_ref=2.0, u_ref=0.5)
+        new = [ctx.download(nm) for nm in ("ux", "uy", "uz")]
+    ref = oracle.residuals(c, new, old, c.dt, 2.0, 0.5)
+    assert np.abs(got[:6] - ref[:6]).max() < 1e-12 * np.abs(ref[:6]).max()
+    assert (got[6:] == ref[6:]).all(), (got[6:], ref[6:])
