@@ -286,8 +286,10 @@ O3D_API int o3d_time_kernel(o3d_ctx *ctx, int kernel, int reps, double *ms_per_l
 /* Self-check of the binary64 <-> binary32 conversions the kernels perform on
  * the integer pipe (round to nearest even): converts n seeded pseudo-random
  * bit patterns (normal, subnormal, zero, tie and out-of-range cases) both
- * ways on the device and counts results that differ bit-wise from the FP64
- * conversion instructions.  No counterpart in the reference. */
+ * ways on the device, and splits each binary64 value into the double-float
+ * pair hi = RN32(x), lo = RN32(x - hi) of the mixed method's residual, and
+ * counts results that differ bit-wise from the FP64 instructions.  No
+ * counterpart in the reference. */
 O3D_API int o3d_check_conversions(long long n, unsigned long long seed, long long *mismatches);
 
 /* divergence(divf, fx, fy, fz, ..., odd) with function_stats of the result

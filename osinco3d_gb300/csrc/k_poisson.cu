@@ -282,15 +282,40 @@ __global__ void k_rhs_shift(R* __restrict__ rhs, long long n, const SolveCtrl* c
 // p at k-1, k, k+1 of its point in registers, the plane's x/y neighbours
 // come from a double-buffered shared tile with a 1-point halo (the halo
 // cell of a thread and the next queue head are loaded one plane ahead).
-// The operator is evaluated as one FMA chain,
+// The neighbour remap is that of src/poisson.f90:57-92 (periodic wrap, or
+// mirror about the end node).
+// T = double (the FP64 method): one FMA chain,
 //   r = fma(-oz, pb+pt, fma(-oy, ps+pn, fma(-ox, pw+pe, fma(-A, pc, rhs)))),
-// 7 FP64 operations per point (GB300 runs 2 FP64 lanes per clock per SM:
-// this kernel is bound by them); the neighbour remap is that of
-// src/poisson.f90:57-92 (periodic wrap, or mirror about the end node).
+// 7 FP64 operations per point, bound by GB300's 2 FP64 lanes per clock.
+// T = float (the mixed method, whose V-cycles take r0 in FP32): every p and
+// rhs value is split on the integer pipe into a double-float (hi + lo, 48
+// bits) as it is loaded and the operator is evaluated in double-float on
+// the FP32 pipe (df_resid7), with no FP64 instruction; its error, about
+// 2^-46 of the largest term, is far below what one FP32 V-cycle resolves.
 // ---------------------------------------------------------------------------
 constexpr int RZ_TX = 32, RZ_TY = 8, RZ_KC = 32;
 static inline dim3 rz_grid(const Grid& g) {
   return dim3((g.nx + RZ_TX - 1) / RZ_TX, (g.ny + RZ_TY - 1) / RZ_TY, (g.nz + RZ_KC - 1) / RZ_KC);
+}
+
+template <bool DFP>
+struct RzVal {
+  using V = double;
+  static __device__ __forceinline__ double of(double x) { return x; }
+  static __device__ __forceinline__ double of(float x) { return f32_to_f64(x); }
+};
+template <>
+struct RzVal<true> {
+  using V = DF;
+  static __device__ __forceinline__ DF of(double x) { return split_df(x); }
+  static __device__ __forceinline__ DF of(float x) { return DF{x, 0.f}; }
+};
+
+__device__ __forceinline__ DF df_const(double c) {
+  DF r;
+  r.h = (float)c;
+  r.l = (float)(c - (double)r.h);
+  return r;
 }
 
 template <class T, class R, bool MAX>
@@ -298,8 +323,11 @@ __global__ void __launch_bounds__(RZ_TX * RZ_TY) k_resid25(const double* __restr
                                                            T* __restrict__ r0, Grid g, PoiCoef<double> c,
                                                            SolveCtrl* ctrl) {
   if (ctrl->done) return;
+  constexpr bool DFP = sizeof(T) == 4;
+  using Cv = RzVal<DFP>;
+  using V = typename Cv::V;
   constexpr int TX = RZ_TX, TY = RZ_TY, SW = TX + 2;
-  __shared__ double tile[2][(TY + 2) * SW];
+  __shared__ V tile[2][(TY + 2) * SW];
   const int tx = threadIdx.x, ty = threadIdx.y, t = ty * TX + tx;
   const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
   const int i = i0 + tx, j = j0 + ty;
@@ -319,36 +347,48 @@ __global__ void __launch_bounds__(RZ_TX * RZ_TY) k_resid25(const double* __restr
   const int sc = (ty + 1) * SW + tx + 1;
   auto zoff = [&](int k) { return sz * ghost(k, g.nz, g.bc[2], &f); };
   const long long out0 = valid ? (long long)i + (long long)g.nx * j : 0;
+  DF cA, cx, cy, cz;
+  if constexpr (DFP) {
+    cA = df_const(c.A); cx = df_const(c.ox); cy = df_const(c.oy); cz = df_const(c.oz);
+  }
 
-  double pb = __ldg(p + zoff(k0 - 1) + cxy), pc = __ldg(p + zoff(k0) + cxy), pt = __ldg(p + zoff(k0 + 1) + cxy);
+  // loads run one plane ahead and stay raw until they are used, so that the
+  // split of a value never waits on a load issued in the same plane step
+  V pb = Cv::of(__ldg(p + zoff(k0 - 1) + cxy)), pc = Cv::of(__ldg(p + zoff(k0) + cxy));
+  double ptraw = __ldg(p + zoff(k0 + 1) + cxy);
   double hv = hon ? __ldg(p + zoff(k0) + hxy) : 0.0;
+  R rr = valid ? __ldg(rhs + out0 + sz * k0) : (R)0;
   float m = 0.f;
   int buf = 0;
   for (int k = k0; k < k1; ++k) {
+    const V pt = Cv::of(ptraw);
     tile[buf][sc] = pc;
-    if (hon) tile[buf][hidx] = hv;
-    double npt = 0.0;
+    if (hon) tile[buf][hidx] = Cv::of(hv);
+    const R rcur = rr;
     if (k + 1 < k1) {
-      npt = __ldg(p + zoff(k + 2) + cxy);
+      ptraw = __ldg(p + zoff(k + 2) + cxy);
       if (hon) hv = __ldg(p + zoff(k + 1) + hxy);
+      if (valid) rr = __ldg(rhs + out0 + sz * (k + 1));
     }
-    const long long q = out0 + sz * k;
-    const double rh = valid ? to_t<double>(__ldg(rhs + q)) : 0.0;
     __syncthreads();
     if (valid) {
-      const double pw = tile[buf][sc - 1], pe = tile[buf][sc + 1];
-      const double ps = tile[buf][sc - SW], pn = tile[buf][sc + SW];
-      double r = fma(-c.A, pc, rh);
-      r = fma(-c.ox, pw + pe, r);
-      r = fma(-c.oy, ps + pn, r);
-      r = fma(-c.oz, pb + pt, r);
-      const T rv = to_t<T>(r);
-      r0[q] = rv;
+      const V pw = tile[buf][sc - 1], pe = tile[buf][sc + 1];
+      const V ps = tile[buf][sc - SW], pn = tile[buf][sc + SW];
+      T rv;
+      if constexpr (DFP) {
+        rv = df_resid7(Cv::of(rcur), pc, pw, pe, ps, pn, pb, pt, cA, cx, cy, cz);
+      } else {
+        double r = fma(-c.A, pc, Cv::of(rcur));
+        r = fma(-c.ox, pw + pe, r);
+        r = fma(-c.oy, ps + pn, r);
+        r = fma(-c.oz, pb + pt, r);
+        rv = (T)r;
+      }
+      r0[out0 + sz * k] = rv;
       if (MAX) m = fmaxf(m, fabsf((float)rv));
     }
     pb = pc;
     pc = pt;
-    pt = npt;
     buf ^= 1;
   }
   if (MAX) {

@@ -131,6 +131,85 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
   lo += err;
 }
 
+// ---- double-float arithmetic (Dekker 1971; Knuth TAOCP vol. 2, 4.2.2) ----
+// A value held as hi + lo, two FP32 numbers with |lo| <= ulp(hi) / 2: 48
+// significant bits, evaluated on the FP32 pipe (64x the FP64 rate here).
+struct __align__(8) DF {
+  float h, l;
+};
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bp = s - a;
+  e = (a - (s - bp)) + (b - bp);
+}
+
+// x = h + l with h = RN32(x) (as f64_to_f32) and l = RN32(x - h), on the
+// integer pipe: the 29 fraction bits that h drops (less 2^29 when h rounded
+// up) scaled by 2^(e - 1075), e the biased binary64 exponent.  That is exact
+// for 2^-74 <= |x| < 2^128 (e in [949, 1150]).  Outside it the split uses no
+// FP64 instruction either: below, l = 0 (|x - h| < 2^-98) and h = +-0 under
+// 2^-126; above, h = +-inf (NaN for a NaN) and l = 0.
+__device__ __forceinline__ DF split_df(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const unsigned e = (hi >> 20) & 0x7ffu;
+  const unsigned sign = hi & 0x80000000u;
+  unsigned f = ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+  const unsigned rem = lo & 0x1fffffffu;
+  const bool up = rem > 0x10000000u || (rem == 0x10000000u && (f & 1u));
+  f += up ? 1u : 0u;
+  int ri = up ? (int)rem - (1 << 29) : (int)rem;
+  ri = sign ? -ri : ri;                            // a zero remainder stays +0, as x - h does
+  DF r;
+  r.h = __uint_as_float(sign | f);
+  r.l = (float)ri * __uint_as_float((e - 948u) << 23);  // 2^(e - 1075)
+  if (e - 949u > 201u) {
+    r.l = 0.f;
+    if (e < 897u) r.h = __uint_as_float(sign);
+    else if (e > 1150u)
+      r.h = __uint_as_float(sign | 0x7f800000u | ((e == 2047u && ((hi & 0xfffffu) | lo)) ? 0x400000u : 0u));
+  }
+  return r;
+}
+
+// a * c to about 2^-46 relative, left unnormalised as (p, q): p = RN(a.h c.h)
+// and q its exact FMA error plus the cross terms
+__device__ __forceinline__ void df_mul(const DF& a, const DF& c, float& p, float& q) {
+  p = a.h * c.h;
+  q = fmaf(a.h, c.h, -p);
+  q = fmaf(a.h, c.l, q);
+  q = fmaf(a.l, c.h, q);
+}
+
+// rhs - (A pc + ox (pw + pe) + oy (ps + pn) + oz (pb + pt)) with double-float
+// operands and coefficients, rounded once to FP32 at the end: the large
+// partial sums are carried exactly by TwoSum, so the cancellation between rhs
+// and the operator leaves an error of about 2^-46 of the largest term.
+__device__ __forceinline__ float df_resid7(const DF& rh, const DF& pc, const DF& pw, const DF& pe, const DF& ps,
+                                           const DF& pn, const DF& pb, const DF& pt, const DF& cA, const DF& cx,
+                                           const DF& cy, const DF& cz) {
+  DF sx, sy, sz;
+  two_sum(pw.h, pe.h, sx.h, sx.l);
+  sx.l += pw.l + pe.l;
+  two_sum(ps.h, pn.h, sy.h, sy.l);
+  sy.l += ps.l + pn.l;
+  two_sum(pb.h, pt.h, sz.h, sz.l);
+  sz.l += pb.l + pt.l;
+  float qa, la, qx, lx, qy, ly, qz, lz;
+  df_mul(pc, cA, qa, la);
+  df_mul(sx, cx, qx, lx);
+  df_mul(sy, cy, qy, ly);
+  df_mul(sz, cz, qz, lz);
+  float s, e1, e2, e3, e4;
+  two_sum(rh.h, -qa, s, e1);
+  two_sum(s, -qx, s, e2);
+  two_sum(s, -qy, s, e3);
+  two_sum(s, -qz, s, e4);
+  const float l = ((rh.l - la) - (lx + ly + lz)) + ((e1 + e2) + (e3 + e4));
+  return s + l;
+}
+
 // conversion of a loaded value to the compute type
 template <class T, class S>
 __device__ __forceinline__ T to_t(S v) { return (T)v; }

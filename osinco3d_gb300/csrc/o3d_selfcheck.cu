@@ -1,6 +1,6 @@
 // o3d_selfcheck.cu -- device self-check of the integer-pipe binary64 <->
-// binary32 conversions (f64_to_f32, f32_to_f64 in o3d_internal.cuh) against
-// the FP64 conversion instructions.
+// binary32 conversions (f64_to_f32, f32_to_f64 in o3d_internal.cuh) and of
+// the double-float split (split_df) against the FP64 instructions.
 #include <cstdio>
 
 #include "o3d_internal.cuh"
@@ -41,6 +41,22 @@ __global__ void k_check_conversions(long long n, unsigned long long seed, unsign
     if (x == x) {
       const float a = f64_to_f32(x), c = __double2float_rn(x);
       if (__float_as_uint(a) != __float_as_uint(c)) ++local;
+      // split: h = RN32(x), l = RN32(x - h) (x - h is exact in binary64) for
+      // 2^-74 <= |x| < 2^128; below, h = RN32(x) flushed to 0 under 2^-126
+      // and l = 0; above, h = +-inf and l = 0
+      const DF s = split_df(x);
+      const double ax = fabs(x);
+      DF w;
+      if (ax >= 0x1p-74 && ax < 0x1p128) {
+        w.h = c;
+        w.l = __double2float_rn(x - (double)c);
+      } else {
+        w.h = ax < 0x1p-126 ? copysignf(0.f, c) : c;
+        w.l = 0.f;
+      }
+      const bool edge = isinf(c) && ax < 0x1p128;  // rounds up to inf: l is left unspecified
+      if (!edge && (__float_as_uint(s.h) != __float_as_uint(w.h) || __float_as_uint(s.l) != __float_as_uint(w.l)))
+        ++local;
     }
     const float f = __uint_as_float((unsigned)(r >> 17));
     if (f == f) {
