@@ -113,6 +113,8 @@ typedef struct o3d_params {
   int mg_cycles;          /* V-cycles per FP64 residual; 0 -> 1 */
   double mg_omega;        /* relaxation of the red-black smoother; 0 -> 1 (Gauss-Seidel)
                              in FP64, 1.15 mixed */
+  int mg_kernels;         /* mixed multigrid: 0 = fused level kernels where a level allows
+                             them, 1 = one kernel per pass (same results, for comparison) */
 } o3d_params;
 
 /* Fills *p with the defaults of the reference's namelists (periodic 64^3). */

@@ -194,26 +194,6 @@ void launch_sor_fixed(double* p, const double* rhs, const Grid& g, const PoiCoef
 // multigrid
 // ---------------------------------------------------------------------------
 
-// block-wide max of nonnegative floats, result valid in thread 0
-__device__ __forceinline__ float block_max_f(float v) {
-  __shared__ float sh[32];
-  const int t = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
-  const int nt = blockDim.x * blockDim.y * blockDim.z;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
-  __syncthreads();
-  if ((t & 31) == 0) sh[t >> 5] = v;
-  __syncthreads();
-  if (t < 32) {
-    v = t < (nt + 31) / 32 ? sh[t] : 0.f;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
-  }
-  return v;
-}
-
-
-
 // trapezoid weight of the left null vector of the mirror operator (1/2 at
 // the end nodes of a mirror axis, 1 elsewhere)
 __device__ __forceinline__ double wnode(const Grid& g, int i, int j, int k) {
@@ -736,10 +716,22 @@ static inline dim3 g3rb(const Grid& g) { return dim3((unsigned)(((g.nx + 1) / 2 
 
 // One V-cycle on level l for A e = r, from e = 0 (zero_init: the first
 // sweep in one pass from r) or from the current e.
+// On a fused level (FP32 only) k_mg_down and k_mg_up do the level's work;
+// p_upd (finest level, last cycle) asks k_mg_up for p += e and max |e| as
+// well, and the return value tells whether that happened.
 template <class T>
-static void vcycle(MGLevel* lv, int l, int nlev, int pre, int post, int coarse_sweeps, T om, SolveCtrl* ctrl,
-                   cudaStream_t s, long long* nl, bool zero_init) {
+static bool vcycle(MGLevel* lv, int l, int nlev, int pre, int post, int coarse_sweeps, T om, SolveCtrl* ctrl,
+                   cudaStream_t s, long long* nl, bool zero_init, double* p_upd = nullptr) {
   const MGLevel& L = lv[l];
+  if constexpr (sizeof(T) == 4) {
+    if (L.fused && l + 1 < nlev) {
+      launch_mg_down(L, lv[l + 1], (float)om, pre, zero_init, ctrl, s);
+      vcycle<T>(lv, l + 1, nlev, pre, post, coarse_sweeps, om, ctrl, s, nl, true);
+      launch_mg_up(L, lv[l + 1], (float)om, post, p_upd, ctrl, s);
+      *nl += 2;
+      return p_upd != nullptr;
+    }
+  }
   T* e = (T*)L.e;
   T* r = (T*)L.r;
   PoiCoef<T> c = make_poi<T>(L.h[0], L.h[1], L.h[2]);
@@ -753,7 +745,7 @@ static void vcycle(MGLevel* lv, int l, int nlev, int pre, int post, int coarse_s
       *nl += 1;
       smooth_sweeps<T>(L, e, r, c, (T)1, coarse_sweeps - 1, ctrl, s, nl);
     }
-    return;
+    return false;
   }
   int sweeps = pre;
   if (zero_init) {
@@ -776,6 +768,7 @@ static void vcycle(MGLevel* lv, int l, int nlev, int pre, int post, int coarse_s
     k_prolong<T><<<g3(L.g), b, 0, s>>>(e, (const T*)C.e, L.g, C.g, cz, ctrl);
   *nl += 1;
   smooth_sweeps<T>(L, e, r, c, om, post, ctrl, s, nl);
+  return false;
 }
 
 // One outer iteration of the defect-correction loop, in two parts.
@@ -795,12 +788,17 @@ template <class T>
 void launch_mg_cycles(double* p, MGLevel* lv, int nlev, int pre, int post, int coarse_sweeps, T smooth_omega,
                       int cycles, bool from_e, SolveCtrl* ctrl, cudaStream_t s, long long* nl) {
   const MGLevel& L0 = lv[0];
+  bool updated = false;
   for (int q = 0; q < cycles; ++q)
-    vcycle<T>(lv, 0, nlev, pre, post, coarse_sweeps, smooth_omega, ctrl, s, nl, q == 0 && !from_e);
-  k_update<T><<<(unsigned)((L0.g.n + 256LL * UPD_PER - 1) / (256LL * UPD_PER)), 256, 0, s>>>(p, (const T*)L0.e,
-                                                                                         L0.g.n, ctrl);
+    updated = vcycle<T>(lv, 0, nlev, pre, post, coarse_sweeps, smooth_omega, ctrl, s, nl, q == 0 && !from_e,
+                        q == cycles - 1 ? p : nullptr);
+  if (!updated) {
+    k_update<T><<<(unsigned)((L0.g.n + 256LL * UPD_PER - 1) / (256LL * UPD_PER)), 256, 0, s>>>(
+        p, (const T*)L0.e, L0.g.n, ctrl);
+    *nl += 1;
+  }
   k_mg_control<<<1, 1, 0, s>>>(ctrl);
-  *nl += 2;
+  *nl += 1;
 }
 
 template <class T, class R>

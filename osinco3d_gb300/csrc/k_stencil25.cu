@@ -35,18 +35,6 @@
 
 namespace o3d {
 
-// ---- cp.async (global -> shared, bypassing the registers) -----------------
-template <int B>
-__device__ __forceinline__ void cp_async(void* smem, const void* gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gmem), "n"(B) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
-
 // xy part of a ghost-mapped cell: offset within a z-plane and the flips
 struct XYCell {
   int off;

@@ -338,6 +338,8 @@ int transeq_t(o3d_ctx* c, int itime) {
 
 // ---- pressure solve --------------------------------------------------------
 
+int mg_smooth_cfg(const o3d_ctx* c, int* pre, int* post);
+
 int build_mg(o3d_ctx* c) {
   const int maxlev = c->P.mg_levels > 0 ? c->P.mg_levels : 32;
   Grid g = c->gp;
@@ -372,6 +374,16 @@ int build_mg(o3d_ctx* c) {
       if (c->mg.back().coarsen[a]) h[a] *= 2.0;
     g = ng;
   }
+  // fused level kernels (FP32): every level that coarsens on all axes and is
+  // large enough, unless the caller asked for one kernel per pass
+  int pre, post;
+  mg_smooth_cfg(c, &pre, &post);
+  const bool fuse = c->mixed && c->P.mg_kernels == 0;
+  if (fuse && mg_fused_setup()) {
+    errf("fused multigrid kernels: %s", cudaGetErrorString(cudaGetLastError()));
+    return O3D_ERR_CUDA;
+  }
+  for (size_t l = 0; l + 1 < c->mg.size(); ++l) c->mg[l].fused = fuse && mg_fusable(c->mg[l], pre, post);
   const size_t tsz = c->mixed ? 4 : 8;
   for (auto& L : c->mg) {
     int st;

@@ -82,6 +82,36 @@ __device__ __forceinline__ int ghost(int m, int n, int bc, bool* flip) {
 template <class T>
 __device__ __forceinline__ T ld(const T* __restrict__ p, long long i) { return __ldg(p + i); }
 
+// block-wide max of nonnegative floats, result valid in thread 0
+__device__ __forceinline__ float block_max_f(float v) {
+  __shared__ float sh[32];
+  const int t = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int nt = blockDim.x * blockDim.y * blockDim.z;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if ((t & 31) == 0) sh[t >> 5] = v;
+  __syncthreads();
+  if (t < 32) {
+    v = t < (nt + 31) / 32 ? sh[t] : 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  }
+  return v;
+}
+
+// ---- cp.async (global -> shared, bypassing the registers) -----------------
+template <int B>
+__device__ __forceinline__ void cp_async(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gmem), "n"(B) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
 // ---- binary64 <-> binary32 conversions on the integer pipe ---------------
 // GB300 executes FP64 instructions (conversions included) at 2 lanes per
 // clock per SM, so a kernel that converts every point is bound by them.

@@ -115,8 +115,17 @@ struct MGLevel {
   int coarsen[3];   // axis coarsened towards the next level
   void* e;          // correction (T)
   void* r;          // right-hand side (T)
-  void* t;          // residual scratch (T)
+  void* t;          // residual scratch (T); the smoothed e between the fused kernels
+  int fused;        // pre/post-smoothing, residual and transfers by k_mg_down / k_mg_up
 };
+
+// fused FP32 level kernels (k_mgfused.cu)
+int mg_fused_setup();
+bool mg_fusable(const MGLevel& L, int pre, int post);
+void launch_mg_down(const MGLevel& L, const MGLevel& C, float om, int pre, bool zero, const SolveCtrl* ctrl,
+                    cudaStream_t s);
+void launch_mg_up(const MGLevel& L, const MGLevel& C, float om, int post, double* p, SolveCtrl* ctrl,
+                  cudaStream_t s);
 
 // context state for checkpoint and restart (o3d_api.cu, used by o3d_io.cu)
 int ctx_geometry(o3d_ctx* c, o3d_params* p, int* nx, int* ny, int* nz, double* dx, double* dy, double* dz);

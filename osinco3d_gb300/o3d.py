@@ -61,7 +61,7 @@ class Params(C.Structure):
         ("iles", C.c_int), ("cs", C.c_double),
         ("precision", C.c_int), ("solver", C.c_int), ("mg_levels", C.c_int),
         ("mg_pre", C.c_int), ("mg_post", C.c_int), ("guess", C.c_int), ("diagnostics", C.c_int),
-        ("mg_cycles", C.c_int), ("mg_omega", C.c_double),
+        ("mg_cycles", C.c_int), ("mg_omega", C.c_double), ("mg_kernels", C.c_int),
     ]
 
 

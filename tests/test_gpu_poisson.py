@@ -151,6 +151,33 @@ def test_mixed_precision_multigrid(oracle, o3d, shape, bcs):
     assert err < 1e-6 * np.abs(ref).max() + 5 * eps, err
 
 
+FUSED_CASES = [
+    # shape, boundaries, multigrid options: the zero-start and from-correction
+    # fused kernels, V(2,1) and V(1,2), fused and unfused levels in one cycle
+    ((64, 64, 64), (0, 0, 0), {}),
+    ((64, 65, 32), (0, 1, 0), {"mg_cycles": 2}),
+    ((33, 33, 33), (1, 1, 1), {"mg_pre": 1, "mg_post": 2}),
+]
+
+
+@pytest.mark.parametrize("shape,bcs,kw", FUSED_CASES)
+def test_fused_level_kernels_match_unfused(oracle, o3d, shape, bcs, kw):
+    """The fused level kernels (pre-smoothing + residual + restriction, and
+    prolongation + post-smoothing + update) evaluate the expressions of the
+    one-pass kernels in the same order: both solves agree bit for bit."""
+    c = _case(oracle, shape, bcs)
+    rhs = _compatible_rhs(c, 13)
+    out = []
+    for mk in (0, 1):
+        prm = params_of(o3d, c, solver=o3d.SOLVER_MG, precision=o3d.PREC_MIXED, mg_kernels=mk, **kw)
+        with o3d.Context(prm) as ctx:
+            got = ctx.field()
+            st, it, dm, om = ctx.poisson_solve(got, rhs, 1.0, 1e-9, 100, 0)
+        out.append((st, it, dm, got))
+    assert out[0][:3] == out[1][:3]
+    np.testing.assert_array_equal(out[0][3], out[1][3])
+
+
 def test_dynamic_omega_follows_reference_rule(oracle, o3d):
     """idyn = 1: same omega trajectory rule (src/poisson.f90:115-121); the final
     omega of a long solve stays within the rule's bounds."""
