@@ -218,16 +218,18 @@ __global__ void __launch_bounds__(256) k_wmean_part(const R* __restrict__ rhs, G
     double wxy = 1.0;
     if (g.bc[0] == AX_MIRROR && (i == 0 || i == g.nx - 1)) wxy *= 0.5;
     if (g.bc[1] == AX_MIRROR && (j == 0 || j == g.ny - 1)) wxy *= 0.5;
-    // the column chunk is summed in the rhs type (at most WM_KC terms), the
-    // chunks and blocks in FP64
-    R acc = (R)0, edge = (R)0;
+    // the column chunk is summed in the rhs type (at most WM_KC terms, one
+    // addition each), the chunks and blocks in FP64; on a mirror z axis the
+    // end planes, inside the sum with weight 1, are taken half back out
+    R acc = (R)0;
     const R* col = rhs + (long long)i + g.sy() * j;
-    for (int k = k0; k < k1; ++k) {
-      const R v = __ldg(col + g.sz() * k);
-      if (k == 0 || k == g.nz - 1) edge += v; else acc += v;
+    for (int k = k0; k < k1; ++k) acc += __ldg(col + g.sz() * k);
+    double sum = to_t<double>(acc);
+    if (g.bc[2] == AX_MIRROR) {
+      if (k0 == 0) sum -= 0.5 * to_t<double>(__ldg(col));
+      if (k1 == g.nz) sum -= 0.5 * to_t<double>(__ldg(col + g.sz() * (g.nz - 1)));
     }
-    const double wz = g.bc[2] == AX_MIRROR ? 0.5 : 1.0;
-    r[0] = wxy * (to_t<double>(acc) + wz * to_t<double>(edge));
+    r[0] = wxy * sum;
   }
   block_reduce_store<1>(r, ops, part, block_linear_id());
 }
@@ -242,7 +244,12 @@ __global__ void k_wmean_final(const double* __restrict__ part, long long nblk, d
     if ((int)threadIdx.x < s) s0[threadIdx.x] += s0[threadIdx.x + s];
     __syncthreads();
   }
-  if (threadIdx.x == 0) ctrl->rhs_mean = s0[0] / wsum;
+  if (threadIdx.x == 0) {
+    const double m = s0[0] / wsum;
+    ctrl->rhs_mean = m;
+    ctrl->rhs_mean_h = (float)m;
+    ctrl->rhs_mean_l = (float)(m - (double)ctrl->rhs_mean_h);
+  }
 }
 
 // rhs <- rhs - mean (the trapezoid-weighted mean of k_wmean_final), in
@@ -272,10 +279,21 @@ __global__ void k_rhs_shift(R* __restrict__ rhs, long long n, const SolveCtrl* c
 // bits) as it is loaded and the operator is evaluated in double-float on
 // the FP32 pipe (df_resid7), with no FP64 instruction; its error, about
 // 2^-46 of the largest term, is far below what one FP32 V-cycle resolves.
+// With shift (T = float only) the rhs is taken less its weighted mean
+// (ctrl->rhs_mean), in double-float, instead of a shifted copy.
 // ---------------------------------------------------------------------------
 constexpr int RZ_TX = 32, RZ_TY = 8, RZ_KC = 32;
 static inline dim3 rz_grid(const Grid& g) {
   return dim3((g.nx + RZ_TX - 1) / RZ_TX, (g.ny + RZ_TY - 1) / RZ_TY, (g.nz + RZ_KC - 1) / RZ_KC);
+}
+
+static inline PoiDF poi_df(const PoiCoef<double>& c) {
+  PoiDF d;
+  d.A = df_split_host(c.A);
+  d.ox = df_split_host(c.ox);
+  d.oy = df_split_host(c.oy);
+  d.oz = df_split_host(c.oz);
+  return d;
 }
 
 template <bool DFP>
@@ -291,17 +309,10 @@ struct RzVal<true> {
   static __device__ __forceinline__ DF of(float x) { return DF{x, 0.f}; }
 };
 
-__device__ __forceinline__ DF df_const(double c) {
-  DF r;
-  r.h = (float)c;
-  r.l = (float)(c - (double)r.h);
-  return r;
-}
-
 template <class T, class R, bool MAX>
 __global__ void __launch_bounds__(RZ_TX * RZ_TY) k_resid25(const double* __restrict__ p, const R* __restrict__ rhs,
                                                            T* __restrict__ r0, Grid g, PoiCoef<double> c,
-                                                           SolveCtrl* ctrl) {
+                                                           PoiDF cdf, SolveCtrl* ctrl, int shift) {
   if (ctrl->done) return;
   constexpr bool DFP = sizeof(T) == 4;
   using Cv = RzVal<DFP>;
@@ -327,9 +338,10 @@ __global__ void __launch_bounds__(RZ_TX * RZ_TY) k_resid25(const double* __restr
   const int sc = (ty + 1) * SW + tx + 1;
   auto zoff = [&](int k) { return sz * ghost(k, g.nz, g.bc[2], &f); };
   const long long out0 = valid ? (long long)i + (long long)g.nx * j : 0;
-  DF cA, cx, cy, cz;
-  if constexpr (DFP) {
-    cA = df_const(c.A); cx = df_const(c.ox); cy = df_const(c.oy); cz = df_const(c.oz);
+  DF mean = {0.f, 0.f};
+  if (DFP && shift) {
+    mean.h = ctrl->rhs_mean_h;
+    mean.l = ctrl->rhs_mean_l;
   }
 
   // loads run one plane ahead and stay raw until they are used, so that the
@@ -356,7 +368,10 @@ __global__ void __launch_bounds__(RZ_TX * RZ_TY) k_resid25(const double* __restr
       const V ps = tile[buf][sc - SW], pn = tile[buf][sc + SW];
       T rv;
       if constexpr (DFP) {
-        rv = df_resid7(Cv::of(rcur), pc, pw, pe, ps, pn, pb, pt, cA, cx, cy, cz);
+        DF rh = Cv::of(rcur), rs;  // rhs - mean: exact TwoSum of the high parts, low parts added
+        two_sum(rh.h, -mean.h, rs.h, rs.l);
+        rs.l += rh.l - mean.l;
+        rv = df_resid7(rs, pc, pw, pe, ps, pn, pb, pt, cdf.A, cdf.ox, cdf.oy, cdf.oz);
       } else {
         double r = fma(-c.A, pc, Cv::of(rcur));
         r = fma(-c.ox, pw + pe, r);
@@ -380,10 +395,11 @@ __global__ void __launch_bounds__(RZ_TX * RZ_TY) k_resid25(const double* __restr
   }
 }
 
-// max |rhs - A p| after a solve (the multigrid rhs is already mean-free)
+// max |rhs - A p| after a solve (less the rhs mean when shift: the mixed
+// multigrid solve leaves the rhs unshifted)
 template <class R>
 __global__ void __launch_bounds__(256) k_resid_inf(const double* __restrict__ p, const R* __restrict__ rhs,
-                                                   Grid g, PoiCoef<double> c, SolveCtrl* ctrl) {
+                                                   Grid g, PoiCoef<double> c, SolveCtrl* ctrl, int shift) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
@@ -391,7 +407,7 @@ __global__ void __launch_bounds__(256) k_resid_inf(const double* __restrict__ p,
   if (i < g.nx && j < g.ny) {
     const long long q = (long long)i + g.sy() * j + g.sz() * k;
     const double ap = lap_nb<double>(p, g, i, j, k, c) + c.A * p[q];
-    d = fabs(to_t<double>(rhs[q]) - ap);
+    d = fabs((to_t<double>(rhs[q]) - (shift ? ctrl->rhs_mean : 0.0)) - ap);
   }
   const double bm = block_max(d);
   if (threadIdx.x == 0 && threadIdx.y == 0 && bm > 0.0)
@@ -621,7 +637,11 @@ __global__ void __launch_bounds__(256) k_prolong_cell(T* __restrict__ ef, const 
 }
 
 // Coarsest level: one block, shared memory, weighted mean of r removed,
-// `sweeps` red-black Gauss-Seidel sweeps from e = 0.
+// `sweeps` red-black Gauss-Seidel sweeps from e = 0.  Each thread resolves
+// once the cells it updates in each colour (the colour's cells of a (j, k)
+// row are i = 2m + ((colour + j + k) & 1)) and their neighbours' offsets,
+// so a sweep is loads, the update and one barrier per colour.
+constexpr int COARSE_MAXC = 3;  // cells per thread and colour: 3 x 1024 >= the colour slots of coarse_max()
 template <class T>
 __global__ void __launch_bounds__(1024) k_coarse(T* __restrict__ e, const T* __restrict__ r, Grid g,
                                                  PoiCoef<T> c, int sweeps, const SolveCtrl* ctrl) {
@@ -630,9 +650,9 @@ __global__ void __launch_bounds__(1024) k_coarse(T* __restrict__ e, const T* __r
   __shared__ T sr[coarse_max<T>()];
   __shared__ double red[2][32];
   const int n = (int)g.n;
-  const int t = threadIdx.x;
+  const int t = threadIdx.x, nt = blockDim.x;
   double a = 0.0, b = 0.0;
-  for (int q = t; q < n; q += blockDim.x) {
+  for (int q = t; q < n; q += nt) {
     const int i = q % g.nx, j = (q / g.nx) % g.ny, k = q / (g.nx * g.ny);
     const double w = wnode(g, i, j, k);
     sr[q] = r[q];
@@ -645,28 +665,66 @@ __global__ void __launch_bounds__(1024) k_coarse(T* __restrict__ e, const T* __r
   if ((t & 31) == 0) { red[0][t >> 5] = a; red[1][t >> 5] = b; }
   __syncthreads();
   if (t < 32) {
-    a = t < (int)(blockDim.x + 31) / 32 ? red[0][t] : 0.0;
-    b = t < (int)(blockDim.x + 31) / 32 ? red[1][t] : 0.0;
+    a = t < (nt + 31) / 32 ? red[0][t] : 0.0;
+    b = t < (nt + 31) / 32 ? red[1][t] : 0.0;
     a = warp_sum(a);
     b = warp_sum(b);
     if (t == 0) red[0][0] = a / b;
   }
   __syncthreads();
   const T mean = (T)red[0][0];
-  for (int q = t; q < n; q += blockDim.x) sr[q] -= mean;
+  for (int q = t; q < n; q += nt) sr[q] -= mean;
+  // this thread's cells: centre and the neighbours w, e, s, n, b, t (lap_nb's remap)
+  int cell[2][COARSE_MAXC][7];
+  const int nxh = (g.nx + 1) / 2;
+#pragma unroll
+  for (int col = 0; col < 2; ++col)
+#pragma unroll
+    for (int u = 0; u < COARSE_MAXC; ++u) {
+      const int id = t + u * nt, row = id / nxh, m = id - row * nxh;
+      const int j = row % g.ny, k = row / g.ny;
+      const int i = 2 * m + ((col + j + k) & 1);
+      int* cq = cell[col][u];
+      cq[0] = -1;
+      if (k < g.nz && i < g.nx) {
+        const int sy = g.nx, sz = g.nx * g.ny;
+        cq[0] = i + sy * j + sz * k;
+        cq[1] = nb_lo(i, g.nx, g.bc[0]) + sy * j + sz * k;
+        cq[2] = nb_hi(i, g.nx, g.bc[0]) + sy * j + sz * k;
+        cq[3] = i + sy * nb_lo(j, g.ny, g.bc[1]) + sz * k;
+        cq[4] = i + sy * nb_hi(j, g.ny, g.bc[1]) + sz * k;
+        cq[5] = i + sy * j + sz * nb_lo(k, g.nz, g.bc[2]);
+        cq[6] = i + sy * j + sz * nb_hi(k, g.nz, g.bc[2]);
+      }
+    }
   __syncthreads();
   for (int s = 0; s < sweeps; ++s) {
-    for (int color = 0; color < 2; ++color) {
-      for (int q = t; q < n; q += blockDim.x) {
-        const int i = q % g.nx, j = (q / g.nx) % g.ny, k = q / (g.nx * g.ny);
-        if (((i + j + k) & 1) != color) continue;
-        const T sn = lap_nb<T>(se, g, i, j, k, c);
-        se[q] = (sr[q] - sn) * c.invA;
+#pragma unroll
+    for (int col = 0; col < 2; ++col) {
+#pragma unroll
+      for (int u = 0; u < COARSE_MAXC; ++u) {
+        const int* cq = cell[col][u];
+        if (cq[0] < 0) continue;
+        const T sn = c.ox * (se[cq[1]] + se[cq[2]]) + c.oy * (se[cq[3]] + se[cq[4]]) + c.oz * (se[cq[5]] + se[cq[6]]);
+        se[cq[0]] = (sr[cq[0]] - sn) * c.invA;
       }
       __syncthreads();
     }
   }
-  for (int q = t; q < n; q += blockDim.x) e[q] = se[q];
+  for (int q = t; q < n; q += nt) e[q] = se[q];
+}
+
+// whether k_coarse takes a level: it fits shared memory and every colour
+// slot has a thread
+template <class T>
+static inline bool coarse_fits(const Grid& g) {
+  return g.n <= coarse_max<T>() && (long long)((g.nx + 1) / 2) * g.ny * g.nz <= 1024LL * COARSE_MAXC;
+}
+// threads of k_coarse for a level: one per cell of the larger colour, at most 1024
+static inline int coarse_threads(const Grid& g) {
+  const long long slots = (long long)((g.nx + 1) / 2) * g.ny * g.nz;
+  const long long nt = ((slots + 31) / 32) * 32;
+  return (int)(nt < 1024 ? (nt < 32 ? 32 : nt) : 1024);
 }
 
 // p += e (FP64), max |e| into the control block.  Each thread handles
@@ -737,8 +795,8 @@ static bool vcycle(MGLevel* lv, int l, int nlev, int pre, int post, int coarse_s
   PoiCoef<T> c = make_poi<T>(L.h[0], L.h[1], L.h[2]);
   const dim3 b(32, 8);
   if (l == nlev - 1) {
-    if (L.g.n <= coarse_max<T>()) {
-      k_coarse<T><<<1, 1024, 0, s>>>(e, r, L.g, c, coarse_sweeps, ctrl);
+    if (coarse_fits<T>(L.g)) {
+      k_coarse<T><<<1, coarse_threads(L.g), 0, s>>>(e, r, L.g, c, coarse_sweeps, ctrl);
       *nl += 1;
     } else {
       k_smooth_first<T><<<g3(L.g), b, 0, s>>>(e, r, L.g, c, (T)1, ctrl);
@@ -777,7 +835,9 @@ template <class T, class R>
 void launch_mg_resid(double* p, const R* rhs, MGLevel* lv, SolveCtrl* ctrl, cudaStream_t s, long long* nl) {
   const MGLevel& L0 = lv[0];
   PoiCoef<double> c64 = make_poi<double>(L0.h[0], L0.h[1], L0.h[2]);
-  k_resid25<T, R, true><<<rz_grid(L0.g), dim3(RZ_TX, RZ_TY), 0, s>>>(p, rhs, (T*)L0.r, L0.g, c64, ctrl);
+  // the mixed method subtracts the rhs mean here; the FP64 method's rhs was shifted in place
+  k_resid25<T, R, true><<<rz_grid(L0.g), dim3(RZ_TX, RZ_TY), 0, s>>>(p, rhs, (T*)L0.r, L0.g, c64, poi_df(c64),
+                                                                      ctrl, sizeof(T) == 4);
   *nl += 1;
 }
 
@@ -1038,8 +1098,8 @@ void launch_rhs_wmean(const R* rhs, const Grid& g, double* part, SolveCtrl* ctrl
 
 template <class R>
 void launch_residual_inf(const double* p, const R* rhs, const Grid& g, const PoiCoef<double>& c, SolveCtrl* ctrl,
-                         cudaStream_t s) {
-  k_resid_inf<R><<<g3(g), dim3(32, 8), 0, s>>>(p, rhs, g, c, ctrl);
+                         bool shift, cudaStream_t s) {
+  k_resid_inf<R><<<g3(g), dim3(32, 8), 0, s>>>(p, rhs, g, c, ctrl, shift);
 }
 template <class R>
 void launch_rhs_shift(R* rhs, long long n, SolveCtrl* ctrl, cudaStream_t s) {
@@ -1056,7 +1116,8 @@ void launch_level_kernel(int which, double* p, const R* rhs, const MGLevel& L, S
     k_smooth<T><<<g3rb(L.g), dim3(32, 8), 0, s>>>((T*)L.e, (const T*)L.r, L.g, c, 0, (T)1, ctrl);
   } else {
     PoiCoef<double> c64 = make_poi<double>(L.h[0], L.h[1], L.h[2]);
-    k_resid25<T, R, false><<<rz_grid(L.g), dim3(RZ_TX, RZ_TY), 0, s>>>(p, rhs, (T*)L.r, L.g, c64, ctrl);
+    k_resid25<T, R, false><<<rz_grid(L.g), dim3(RZ_TX, RZ_TY), 0, s>>>(p, rhs, (T*)L.r, L.g, c64, poi_df(c64),
+                                                                       ctrl, 0);
   }
 }
 template void launch_level_kernel<float, double>(int, double*, const double*, const MGLevel&, SolveCtrl*,
@@ -1071,8 +1132,8 @@ template void launch_mg_outer<float, double>(double*, const double*, MGLevel*, i
 template void launch_rhs_wmean<double>(const double*, const Grid&, double*, SolveCtrl*, cudaStream_t, long long*);
 template void launch_rhs_wmean<float>(const float*, const Grid&, double*, SolveCtrl*, cudaStream_t, long long*);
 template void launch_residual_inf<double>(const double*, const double*, const Grid&, const PoiCoef<double>&,
-                                          SolveCtrl*, cudaStream_t);
+                                          SolveCtrl*, bool, cudaStream_t);
 template void launch_residual_inf<float>(const double*, const float*, const Grid&, const PoiCoef<double>&,
-                                         SolveCtrl*, cudaStream_t);
+                                         SolveCtrl*, bool, cudaStream_t);
 
 }  // namespace o3d

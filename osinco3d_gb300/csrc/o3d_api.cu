@@ -600,15 +600,14 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
   CK(cudaEventRecord(c->ev[2], c->s));
   const bool use_mg = c->P.solver == O3D_SOLVER_MG;
   if (use_mg || learned || sampling) {
-    // remove the weighted mean from the rhs in place (compatibility of the singular problem)
-    if (c->mixed) {
-      launch_rhs_wmean<double>((const double*)c->rhs, c->gp, c->part, c->ctrl, c->s, &c->launches);
+    // the weighted mean of the rhs (compatibility of the singular problem):
+    // removed in place, except for the mixed multigrid solve, whose FP64
+    // residual kernel subtracts it as it reads the rhs
+    launch_rhs_wmean<double>((const double*)c->rhs, c->gp, c->part, c->ctrl, c->s, &c->launches);
+    if (!(c->mixed && use_mg)) {
       launch_rhs_shift<double>((double*)c->rhs, c->g.n, c->ctrl, c->s);
-    } else {
-      launch_rhs_wmean<double>((const double*)c->rhs, c->gp, c->part, c->ctrl, c->s, &c->launches);
-      launch_rhs_shift<double>((double*)c->rhs, c->g.n, c->ctrl, c->s);
+      c->launches++;
     }
-    c->launches++;
     CKL();
   }
   c->sample_ready = 0;
@@ -683,8 +682,7 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
   if (!use_mg || c->P.diagnostics >= 2) {
     PoiCoef<double> pc = make_poi<double>(c->dx, c->dy, c->dz);
     CK(cudaMemsetAsync(&c->ctrl->res_key, 0, sizeof(unsigned long long), c->s));
-    if (c->mixed) launch_residual_inf<double>(c->pp, (const double*)c->rhs, c->gp, pc, c->ctrl, c->s);
-    else launch_residual_inf<double>(c->pp, (const double*)c->rhs, c->gp, pc, c->ctrl, c->s);
+    launch_residual_inf<double>(c->pp, (const double*)c->rhs, c->gp, pc, c->ctrl, c->mixed && use_mg, c->s);
     c->launches++;
     CKL();
   }

@@ -203,6 +203,18 @@ __device__ __forceinline__ DF split_df(double x) {
   return r;
 }
 
+// double-float coefficients of the 7-point operator (hi + lo of A, ox, oy,
+// oz), split on the host so that no kernel evaluates FP64 for them
+struct PoiDF {
+  DF A, ox, oy, oz;
+};
+inline DF df_split_host(double v) {
+  DF r;
+  r.h = (float)v;
+  r.l = (float)(v - (double)r.h);
+  return r;
+}
+
 // a * c to about 2^-46 relative, left unnormalised as (p, q): p = RN(a.h c.h)
 // and q its exact FMA error plus the cross terms
 __device__ __forceinline__ void df_mul(const DF& a, const DF& c, float& p, float& q) {
@@ -539,6 +551,7 @@ struct SolveCtrl {
   double dmax;                   // last completed sweep
   double eps, factor;
   double rhs_mean;               // weighted mean removed from the rhs (multigrid)
+  float rhs_mean_h, rhs_mean_l;  // the same as a double-float (hi + lo)
   double res_inf;
   int iter, kmax, idyn, done, status;
   int cycles;            // V-cycles run so far

@@ -187,6 +187,7 @@ void launch_rhs_wmean(const R* rhs, const Grid& g, double* part, SolveCtrl* ctrl
                       long long* nl);
 template <class R>
 void launch_residual_inf(const double* p, const R* rhs, const Grid& g, const PoiCoef<double>& c, SolveCtrl* ctrl,
+                         bool shift,
                          cudaStream_t s);
 template <class R>
 void launch_rhs_shift(R* rhs, long long n, SolveCtrl* ctrl, cudaStream_t s);
