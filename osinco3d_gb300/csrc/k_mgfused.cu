@@ -203,6 +203,7 @@ template <int S, bool ZERO>
 __global__ void __launch_bounds__(MF_NT, 3)
     k_mg_down(const float* __restrict__ r, const float* __restrict__ ein, float* __restrict__ eout,
               float* __restrict__ rc, Grid gf, Grid gc, PoiCoef<float> c, float om, int kc, const SolveCtrl* ctrl) {
+  pdl_enter();
   if (ctrl->done) return;
   using X = Ext<MF_FX + 2 * S + 3, MF_FY + 2 * S + 3>;
   constexpr int PL = X::PL, XH = X::XH, D = down_d<ZERO>();
@@ -363,6 +364,7 @@ __global__ void __launch_bounds__(MF_NT, 3)
     k_mg_up(const float* __restrict__ epre, const float* __restrict__ ecrs, const float* __restrict__ r,
             float* __restrict__ eout, double* __restrict__ p, Grid gf, Grid gc, PoiCoef<float> c, float om, int kc,
             SolveCtrl* ctrl) {
+  pdl_enter();
   if (ctrl->done) return;
   using G = UpGeom<S2>;
   using X = typename G::X;
@@ -593,7 +595,7 @@ void launch_mg_down(const MGLevel& L, const MGLevel& C, float om, int pre, bool 
   float* eout = (float*)L.t;
   float* rc = (float*)C.r;
 #define MF_DOWN(S, Z) \
-  k_mg_down<S, Z><<<grid, MF_NT, down_smem<S, Z>(), s>>>(r, ein, eout, rc, L.g, C.g, c, om, kc, ctrl)
+  launch_pdl(k_mg_down<S, Z>, grid, MF_NT, down_smem<S, Z>(), s, r, ein, eout, rc, L.g, C.g, c, om, kc, ctrl)
   if (pre == 1) {
     if (zero) MF_DOWN(2, true);
     else MF_DOWN(2, false);
@@ -614,7 +616,7 @@ void launch_mg_up(const MGLevel& L, const MGLevel& C, float om, int post, double
   const float* r = (const float*)L.r;
   float* eout = (float*)L.e;
 #define MF_UP(S2, U) \
-  k_mg_up<S2, U><<<grid, MF_NT, up_smem<S2>(), s>>>(epre, ec, r, eout, p, L.g, C.g, c, om, kc, ctrl)
+  launch_pdl(k_mg_up<S2, U>, grid, MF_NT, up_smem<S2>(), s, epre, ec, r, eout, p, L.g, C.g, c, om, kc, ctrl)
   if (post == 1) {
     if (p) MF_UP(2, true);
     else MF_UP(2, false);

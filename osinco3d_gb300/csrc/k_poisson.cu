@@ -313,6 +313,7 @@ template <class T, class R, bool MAX>
 __global__ void __launch_bounds__(RZ_TX * RZ_TY) k_resid25(const double* __restrict__ p, const R* __restrict__ rhs,
                                                            T* __restrict__ r0, Grid g, PoiCoef<double> c,
                                                            PoiDF cdf, SolveCtrl* ctrl, int shift) {
+  pdl_enter();
   if (ctrl->done) return;
   constexpr bool DFP = sizeof(T) == 4;
   using Cv = RzVal<DFP>;
@@ -433,6 +434,7 @@ __global__ void __launch_bounds__(256) k_smooth_zero(T* __restrict__ e, const T*
 template <class T>
 __global__ void __launch_bounds__(256) k_smooth_first(T* __restrict__ e, const T* __restrict__ r, Grid g,
                                                       PoiCoef<T> c, T om, const SolveCtrl* ctrl) {
+  pdl_enter();
   if (ctrl->done) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -451,6 +453,7 @@ __global__ void __launch_bounds__(256) k_smooth_first(T* __restrict__ e, const T
 template <class T>
 __global__ void __launch_bounds__(256) k_smooth(T* __restrict__ e, const T* __restrict__ r, Grid g,
                                                 PoiCoef<T> c, int color, T om, const SolveCtrl* ctrl) {
+  pdl_enter();
   if (ctrl->done) return;
   const int ih = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -478,8 +481,8 @@ static void smooth_sweeps(const MGLevel& L, T* e, const T* r, const PoiCoef<T>& 
                           const SolveCtrl* ctrl, cudaStream_t s, long long* nl) {
   for (int q = 0; q < n; ++q)
     for (int color = 0; color < 2; ++color)
-      k_smooth<T><<<dim3((unsigned)(((L.g.nx + 1) / 2 + 31) / 32), (L.g.ny + 7) / 8, L.g.nz), dim3(32, 8), 0, s>>>(
-          e, r, L.g, c, color, om, ctrl);
+      launch_pdl(k_smooth<T>, dim3((unsigned)(((L.g.nx + 1) / 2 + 31) / 32), (L.g.ny + 7) / 8, L.g.nz), dim3(32, 8),
+                 0, s, e, r, L.g, c, color, om, ctrl);
   *nl += 2 * n;
 }
 
@@ -487,6 +490,7 @@ template <class T>
 __global__ void __launch_bounds__(256) k_resid(const T* __restrict__ e, const T* __restrict__ r,
                                                T* __restrict__ t, Grid g, PoiCoef<T> c,
                                                const SolveCtrl* ctrl) {
+  pdl_enter();
   if (ctrl->done) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -513,6 +517,7 @@ __device__ __forceinline__ int fine_of(int I, int o, int nf, int bc, int coarsen
 template <class T>
 __global__ void __launch_bounds__(256) k_restrict(const T* __restrict__ tf, T* __restrict__ rc, Grid gf,
                                                   Grid gc, Coarsen cz, const SolveCtrl* ctrl) {
+  pdl_enter();
   if (ctrl->done) return;
   const int I = blockIdx.x * blockDim.x + threadIdx.x;
   const int J = blockIdx.y * blockDim.y + threadIdx.y;
@@ -541,6 +546,7 @@ __global__ void __launch_bounds__(256) k_restrict(const T* __restrict__ tf, T* _
 template <class T>
 __global__ void __launch_bounds__(256) k_restrict_full(const T* __restrict__ tf, T* __restrict__ rc, Grid gf,
                                                        Grid gc, const SolveCtrl* ctrl) {
+  pdl_enter();
   if (ctrl->done) return;
   const int I = blockIdx.x * blockDim.x + threadIdx.x;
   const int J = blockIdx.y * blockDim.y + threadIdx.y;
@@ -580,6 +586,7 @@ __device__ __forceinline__ void prol_axis(int i, int nc, int bc, int coarsened, 
 template <class T>
 __global__ void __launch_bounds__(256) k_prolong(T* __restrict__ ef, const T* __restrict__ ec, Grid gf,
                                                  Grid gc, Coarsen cz, const SolveCtrl* ctrl) {
+  pdl_enter();
   if (ctrl->done) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -607,6 +614,7 @@ __device__ __forceinline__ int prol_hi(int I, int nc, int bc) {
 template <class T>
 __global__ void __launch_bounds__(256) k_prolong_cell(T* __restrict__ ef, const T* __restrict__ ec, Grid gf,
                                                       Grid gc, const SolveCtrl* ctrl) {
+  pdl_enter();
   if (ctrl->done) return;
   const int I = blockIdx.x * blockDim.x + threadIdx.x;
   const int J = blockIdx.y * blockDim.y + threadIdx.y;
@@ -645,6 +653,7 @@ constexpr int COARSE_MAXC = 3;  // cells per thread and colour: 3 x 1024 >= the 
 template <class T>
 __global__ void __launch_bounds__(1024) k_coarse(T* __restrict__ e, const T* __restrict__ r, Grid g,
                                                  PoiCoef<T> c, int sweeps, const SolveCtrl* ctrl) {
+  pdl_enter();
   if (ctrl->done) return;
   __shared__ T se[coarse_max<T>()];
   __shared__ T sr[coarse_max<T>()];
@@ -735,6 +744,7 @@ constexpr int UPD_PER = 8;
 template <class T>
 __global__ void __launch_bounds__(256) k_update(double* __restrict__ p, const T* __restrict__ e, long long n,
                                                 SolveCtrl* ctrl) {
+  pdl_enter();
   if (ctrl->done) return;
   const long long base = (long long)blockIdx.x * blockDim.x * UPD_PER + threadIdx.x;
   T m = (T)0;
@@ -754,6 +764,7 @@ __global__ void __launch_bounds__(256) k_update(double* __restrict__ p, const T*
 }
 
 __global__ void k_mg_control(SolveCtrl* c) {
+  pdl_enter();
   if (c->done) return;
   const double dmax = __longlong_as_double((long long)c->dmax_key);
   c->dmax_key = 0ull;
@@ -796,10 +807,10 @@ static bool vcycle(MGLevel* lv, int l, int nlev, int pre, int post, int coarse_s
   const dim3 b(32, 8);
   if (l == nlev - 1) {
     if (coarse_fits<T>(L.g)) {
-      k_coarse<T><<<1, coarse_threads(L.g), 0, s>>>(e, r, L.g, c, coarse_sweeps, ctrl);
+      launch_pdl(k_coarse<T>, 1, coarse_threads(L.g), 0, s, e, r, L.g, c, coarse_sweeps, ctrl);
       *nl += 1;
     } else {
-      k_smooth_first<T><<<g3(L.g), b, 0, s>>>(e, r, L.g, c, (T)1, ctrl);
+      launch_pdl(k_smooth_first<T>, g3(L.g), b, 0, s, e, r, L.g, c, (T)1, ctrl);
       *nl += 1;
       smooth_sweeps<T>(L, e, r, c, (T)1, coarse_sweeps - 1, ctrl, s, nl);
     }
@@ -807,23 +818,25 @@ static bool vcycle(MGLevel* lv, int l, int nlev, int pre, int post, int coarse_s
   }
   int sweeps = pre;
   if (zero_init) {
-    k_smooth_first<T><<<g3(L.g), b, 0, s>>>(e, r, L.g, c, om, ctrl);
+    launch_pdl(k_smooth_first<T>, g3(L.g), b, 0, s, e, r, L.g, c, om, ctrl);
     *nl += 1;
     sweeps -= 1;
   }
   smooth_sweeps<T>(L, e, r, c, om, sweeps, ctrl, s, nl);
-  k_resid<T><<<g3(L.g), b, 0, s>>>(e, r, (T*)L.t, L.g, c, ctrl);
+  launch_pdl(k_resid<T>, g3(L.g), b, 0, s, e, r, (T*)L.t, L.g, c, ctrl);
   const MGLevel& C = lv[l + 1];
   Coarsen cz;
   for (int a = 0; a < 3; ++a) cz.c[a] = L.coarsen[a];
-  if (cz.c[0] && cz.c[1] && cz.c[2]) k_restrict_full<T><<<g3(C.g), b, 0, s>>>((const T*)L.t, (T*)C.r, L.g, C.g, ctrl);
-  else k_restrict<T><<<g3(C.g), b, 0, s>>>((const T*)L.t, (T*)C.r, L.g, C.g, cz, ctrl);
+  if (cz.c[0] && cz.c[1] && cz.c[2])
+    launch_pdl(k_restrict_full<T>, g3(C.g), b, 0, s, (const T*)L.t, (T*)C.r, L.g, C.g, ctrl);
+  else
+    launch_pdl(k_restrict<T>, g3(C.g), b, 0, s, (const T*)L.t, (T*)C.r, L.g, C.g, cz, ctrl);
   *nl += 2;
   vcycle<T>(lv, l + 1, nlev, pre, post, coarse_sweeps, om, ctrl, s, nl, true);
   if (cz.c[0] && cz.c[1] && cz.c[2])
-    k_prolong_cell<T><<<g3(C.g), b, 0, s>>>(e, (const T*)C.e, L.g, C.g, ctrl);
+    launch_pdl(k_prolong_cell<T>, g3(C.g), b, 0, s, e, (const T*)C.e, L.g, C.g, ctrl);
   else
-    k_prolong<T><<<g3(L.g), b, 0, s>>>(e, (const T*)C.e, L.g, C.g, cz, ctrl);
+    launch_pdl(k_prolong<T>, g3(L.g), b, 0, s, e, (const T*)C.e, L.g, C.g, cz, ctrl);
   *nl += 1;
   smooth_sweeps<T>(L, e, r, c, om, post, ctrl, s, nl);
   return false;
@@ -836,8 +849,8 @@ void launch_mg_resid(double* p, const R* rhs, MGLevel* lv, SolveCtrl* ctrl, cuda
   const MGLevel& L0 = lv[0];
   PoiCoef<double> c64 = make_poi<double>(L0.h[0], L0.h[1], L0.h[2]);
   // the mixed method subtracts the rhs mean here; the FP64 method's rhs was shifted in place
-  k_resid25<T, R, true><<<rz_grid(L0.g), dim3(RZ_TX, RZ_TY), 0, s>>>(p, rhs, (T*)L0.r, L0.g, c64, poi_df(c64),
-                                                                      ctrl, sizeof(T) == 4);
+  launch_pdl(k_resid25<T, R, true>, rz_grid(L0.g), dim3(RZ_TX, RZ_TY), 0, s, p, rhs, (T*)L0.r, L0.g, c64,
+             poi_df(c64), ctrl, (int)(sizeof(T) == 4));
   *nl += 1;
 }
 
@@ -853,11 +866,11 @@ void launch_mg_cycles(double* p, MGLevel* lv, int nlev, int pre, int post, int c
     updated = vcycle<T>(lv, 0, nlev, pre, post, coarse_sweeps, smooth_omega, ctrl, s, nl, q == 0 && !from_e,
                         q == cycles - 1 ? p : nullptr);
   if (!updated) {
-    k_update<T><<<(unsigned)((L0.g.n + 256LL * UPD_PER - 1) / (256LL * UPD_PER)), 256, 0, s>>>(
-        p, (const T*)L0.e, L0.g.n, ctrl);
+    launch_pdl(k_update<T>, (unsigned)((L0.g.n + 256LL * UPD_PER - 1) / (256LL * UPD_PER)), 256, 0, s, p,
+               (const T*)L0.e, L0.g.n, ctrl);
     *nl += 1;
   }
-  k_mg_control<<<1, 1, 0, s>>>(ctrl);
+  launch_pdl(k_mg_control, 1, 1, 0, s, ctrl);
   *nl += 1;
 }
 

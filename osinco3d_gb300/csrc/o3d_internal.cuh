@@ -100,6 +100,33 @@ __device__ __forceinline__ float block_max_f(float v) {
   return v;
 }
 
+// ---- programmatic dependent launch ----------------------------------------
+// A kernel launched by launch_pdl may be scheduled while its predecessor in
+// the stream is still running; it calls pdl_enter() before anything else:
+// let its own dependents be scheduled, then wait until the predecessor has
+// completed and its writes are visible.  For a kernel launched without the
+// attribute both instructions do nothing.  This overlaps the launch of the
+// many short kernels of a V-cycle with the end of the kernel before.
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");
+}
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, (KArgs)args...);
+}
+
 // ---- cp.async (global -> shared, bypassing the registers) -----------------
 template <int B>
 __device__ __forceinline__ void cp_async(void* smem, const void* gmem) {
