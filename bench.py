@@ -41,11 +41,12 @@ PRED_BYTES_PER_PT = 15 * 4   # read u,v,w + 6 history, write 3 u* + 3 fluxes
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
 # 256^3 launches, from the ncu captures summarised in profiles/
 TRAFFIC_PER_LAUNCH: dict = {
-    "mg_smooth": (134.744832 + 18.91968) * 1e6,   # k_smooth_tgv256_finest.md
+    "mg_down": (74.900736 + 31.665664) * 1e6,     # k_mg_down_tgv256.md
+    "mg_up": (286.49984 + 151.700992) * 1e6,      # k_mg_up_tgv256.md
     "predict": (623.436032 + 365.83552) * 1e6,    # k_predict25_tgv256.md
     "rhs": (202.962432 + 3.673088) * 1e6,         # k_div25_tgv256.md (statistics pass, no rhs write)
     "correct": (339.60832 + 169.290496) * 1e6,    # k_correct25_tgv256.md
-    "resid64": (204.871168 + 49.45792) * 1e6,     # k_resid25_tgv256.md
+    "resid64": (270.596864 + 53.38368) * 1e6,     # k_resid25_tgv256.md
 }
 
 
@@ -232,19 +233,17 @@ def measure_e2e(o3d, steps: int, warmup: int, world: int, weights=None, **kw) ->
 # algorithmic bytes per grid point of the hot kernels (float32 storage)
 KERNEL_BYTES = {
     "predict": (PRED_BYTES_PER_PT, "k_predict25<float>"),
-    "mg_smooth": (8, "k_smooth<float> (one red-black colour pass, finest level)"),  # half-grid e, r in/out
-    "rhs": (16, "k_div25<float>"),
+    # read r, write e and the coarse rhs (1/8)
+    "mg_down": (4 + 4 + 0.5, "k_mg_down<4,zero> (pre-smoothing + residual + restriction, finest level)"),
+    # read e, r, p and the coarse correction (1/8), write e and p
+    "mg_up": (4 + 4 + 8 + 0.5 + 4 + 8, "k_mg_up<2,update> (prolongation + post-smoothing + p += e, finest)"),
+    "rhs": (4 * 3 + 8, "k_div25<float,double>"),  # read u* (3 x FP32), write the FP64 rhs
     "correct": (4 * 6 + 8, "k_correct25<float,double>"),
-    "resid64": (8 + 4 + 4, "k_resid25<float,float> (FP64 residual, finest level)"),  # read p, rhs; write r
+    "resid64": (8 + 8 + 4, "k_resid25<float,double> (double-float residual, finest level)"),  # read p, rhs; write r
 }
-# FP64 operations per point of the FP64 residual (its bound is the FP64 pipe)
-RESID64_FP64_OPS = 7
-# the kernel the roofline entry describes: the finest-level multigrid
-# smoother, the largest HBM-bound share of the step (the FP64 residual, of
-# equal share, is bound by the FP64 pipe and reported beside it)
-ROOF_KERNEL = "mg_smooth"
-# GB300 FP64 pipe: 2 lanes per clock per SM, 152 SMs, 2.07 GHz
-FP64_PEAK_GOPS = 2 * 152 * 2.07
+# the kernel the roofline entry describes: the finest level's fused
+# pre-smoothing kernel, the largest share of the step
+ROOF_KERNEL = "mg_down"
 
 
 def kernel_roofline(o3d, ctx, peaks: dict) -> dict:
@@ -258,9 +257,6 @@ def kernel_roofline(o3d, ctx, peaks: dict) -> dict:
         gbs = bpp * N ** 3 / (t * 1e-3) / 1e9
         out[name] = {"kernel": label, "ms": t, "bytes_per_point": bpp, "achieved": gbs,
                      "frac": gbs / peak if peak else None}
-    r = out["resid64"]
-    r["fp64_gops"] = RESID64_FP64_OPS * N ** 3 / (r["ms"] * 1e-3) / 1e9
-    r["fp64_frac"] = r["fp64_gops"] / FP64_PEAK_GOPS
     for name, v in out.items():
         v["traffic"] = TRAFFIC_PER_LAUNCH.get(name)
     return out
@@ -325,6 +321,8 @@ def gpu_arm(args, rank, world, local):
         fp64 = dict(precision=o3d.PREC_FP64, solver=o3d.SOLVER_MG, kmax=100)
         for name, kw in (("mixed_mg", mixed), ("mixed_mg_extrapolated", dict(mixed, guess=o3d.GUESS_EXTRAPOLATED)),
                          ("mixed_mg_zero", dict(mixed, guess=o3d.GUESS_ZERO)),
+                         # one kernel per multigrid pass instead of the fused level kernels
+                         ("mixed_mg_unfused", dict(mixed, mg_kernels=1)),
                          # the plain method: FP64 V(2,2) Gauss-Seidel from the previous pressure
                          ("fp64_mg", fp64),
                          # FP64 with the mixed method's smoother settings and extrapolated guess

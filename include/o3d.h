@@ -279,10 +279,13 @@ O3D_API int o3d_sample_ready(const o3d_ctx *ctx);
  * `reps` back-to-back launches timed with CUDA events on the context's stream.
  * kernel: 0 fused predictor, 1 divergence -> rhs, 2 velocity correction,
  * 3 multigrid smoother colour pass on the finest level, 4 FP64 residual of
- * the defect-correction loop.  The launches only rewrite scratch outputs
- * (u*, the free flux slot, rhs, the finest-level correction and residual) or
- * recompute the velocity identically from u* and p.  No counterpart in the
- * reference (measurement hook). */
+ * the defect-correction loop, 5 fused pre-smoothing + residual + restriction
+ * of the finest level (mixed method, from a zero correction), 6 fused
+ * prolongation + post-smoothing + p += e of the finest level (mixed method;
+ * the update goes to a scratch copy of p).  The launches only rewrite
+ * scratch outputs (u*, the free flux slot, rhs, the multigrid levels'
+ * corrections and residuals) or recompute the velocity identically from u*
+ * and p.  No counterpart in the reference (measurement hook). */
 O3D_API int o3d_time_kernel(o3d_ctx *ctx, int kernel, int reps, double *ms_per_launch);
 
 /* Self-check of the binary64 <-> binary32 conversions the kernels perform on

@@ -1295,14 +1295,23 @@ int o3d_set_sample_buffers(o3d_ctx* c, float* d_feat, float* d_tgt) {
 int o3d_sample_ready(const o3d_ctx* c) { return c ? c->sample_ready : 0; }
 
 int o3d_time_kernel(o3d_ctx* c, int kernel, int reps, double* ms_per_launch) {
-  if (!c || reps < 1 || !ms_per_launch || kernel < 0 || kernel > 4) {
+  if (!c || reps < 1 || !ms_per_launch || kernel < 0 || kernel > 6) {
     errf("bad o3d_time_kernel request");
     return O3D_ERR_BADARG;
   }
+  double* p_scratch = nullptr;
   if (kernel >= 3) {
     if (!c->mg_ok) {
       int st = build_mg(c);
       if (st) return st;
+    }
+    if (kernel >= 5 && !(c->mg.size() > 1 && c->mg[0].fused)) {
+      errf("o3d_time_kernel: the finest level does not run the fused multigrid kernels");
+      return O3D_ERR_BADARG;
+    }
+    if (kernel == 6) {
+      CK(cudaMalloc(&p_scratch, (size_t)c->g.n * 8));
+      CK(cudaMemcpyAsync(p_scratch, c->pp, (size_t)c->g.n * 8, cudaMemcpyDeviceToDevice, c->s));
     }
     // the multigrid kernels return at once on a finished solve: re-open it
     CK(cudaMemsetAsync(&c->ctrl->done, 0, sizeof(int), c->s));
@@ -1319,6 +1328,17 @@ int o3d_time_kernel(o3d_ctx* c, int kernel, int reps, double* ms_per_launch) {
       }
       case 1: return c->mixed ? rhs_t<float>(c) : rhs_t<double>(c);
       case 2: return c->mixed ? correct_t<float>(c) : correct_t<double>(c);
+      case 5:
+      case 6: {
+        int pre, post;
+        mg_smooth_cfg(c, &pre, &post);
+        const float om = (float)mg_omega_of(c);
+        if (kernel == 5) launch_mg_down(c->mg[0], c->mg[1], om, pre, true, c->ctrl, c->s);
+        else launch_mg_up(c->mg[0], c->mg[1], om, post, p_scratch, c->ctrl, c->s);
+        c->launches++;
+        CKL();
+        return O3D_OK;
+      }
       default:
         if (c->mixed)
           launch_level_kernel<float, double>(kernel - 3, c->pp, (const double*)c->rhs, c->mg[0], c->ctrl, c->s);
@@ -1341,6 +1361,7 @@ int o3d_time_kernel(o3d_ctx* c, int kernel, int reps, double* ms_per_launch) {
   *ms_per_launch = ms / reps;
   if (kernel >= 3) CK(cudaMemsetAsync(&c->ctrl->done, 0xff, sizeof(int), c->s));
   CK(cudaStreamSynchronize(c->s));
+  if (p_scratch) CK(cudaFree(p_scratch));
   return O3D_OK;
 }
 

@@ -397,7 +397,7 @@ class Context:
     def sample_ready(self) -> bool:
         return bool(self.L.o3d_sample_ready(self.h))
 
-    KERNELS = {"predict": 0, "rhs": 1, "correct": 2, "mg_smooth": 3, "resid64": 4}
+    KERNELS = {"predict": 0, "rhs": 1, "correct": 2, "mg_smooth": 3, "resid64": 4, "mg_down": 5, "mg_up": 6}
 
     def time_kernel(self, name: str, reps: int = 20) -> float:
         """Milliseconds per launch of one hot kernel on the live state."""
