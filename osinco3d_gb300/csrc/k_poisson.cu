@@ -82,6 +82,7 @@ __device__ __forceinline__ int seam_bits(const Grid& g) {
 __global__ void __launch_bounds__(256) k_sor_rb(double* __restrict__ p, const double* __restrict__ rhs,
                                                 Grid g, PoiCoef<double> c, int color,
                                                 SolveCtrl* ctrl, double omega_fixed, int use_ctrl) {
+  pdl_enter();
   if (use_ctrl && ctrl->done) return;
   const double om = use_ctrl ? ctrl->omega : omega_fixed;
   const int ih = blockIdx.x * blockDim.x + threadIdx.x;
@@ -111,6 +112,7 @@ __global__ void __launch_bounds__(256) k_sor_rb(double* __restrict__ p, const do
 __global__ void __launch_bounds__(256) k_sor_seam(double* __restrict__ p, const double* __restrict__ rhs, Grid g,
                                                   PoiCoef<double> c, int cls, int color, SolveCtrl* ctrl,
                                                   double omega_fixed, int use_ctrl) {
+  pdl_enter();
   if (use_ctrl && ctrl->done) return;
   const double om = use_ctrl ? ctrl->omega : omega_fixed;
   const int sb = seam_bits(g);
@@ -155,7 +157,7 @@ static int sor_seam_passes(double* p, const double* rhs, const Grid& g, const Po
     const long long ez = (cls & 4) ? 1 : g.nz - ((sb >> 2) & 1);
     const unsigned blocks = (unsigned)((ex * ey * ez + 255) / 256);
     for (int color = 0; color < 2; ++color) {
-      k_sor_seam<<<blocks, 256, 0, s>>>(p, rhs, g, c, cls, color, ctrl, omega, use_ctrl);
+      launch_pdl(k_sor_seam, blocks, 256, 0, s, p, rhs, g, c, cls, color, ctrl, omega, use_ctrl);
       ++nl;
     }
   }
@@ -164,6 +166,7 @@ static int sor_seam_passes(double* p, const double* rhs, const Grid& g, const Po
 
 // stop test and dynamic omega of src/poisson.f90:110-122, once per sweep
 __global__ void k_sor_control(SolveCtrl* c) {
+  pdl_enter();
   if (c->done) return;
   const double dmax = __longlong_as_double((long long)c->dmax_key);
   c->dmax_key = 0ull;
@@ -182,11 +185,11 @@ __global__ void k_sor_control(SolveCtrl* c) {
 static dim3 rb_grid(const Grid& g) { return dim3((unsigned)((g.nx + 1) / 2 + 31) / 32, (g.ny + 7) / 8, g.nz); }
 
 
-void launch_sor_control(SolveCtrl* ctrl, cudaStream_t s) { k_sor_control<<<1, 1, 0, s>>>(ctrl); }
+void launch_sor_control(SolveCtrl* ctrl, cudaStream_t s) { launch_pdl(k_sor_control, 1, 1, 0, s, ctrl); }
 void launch_sor_fixed(double* p, const double* rhs, const Grid& g, const PoiCoef<double>& c,
                       double omega, SolveCtrl* ctrl, cudaStream_t s) {
-  k_sor_rb<<<rb_grid(g), dim3(32, 8), 0, s>>>(p, rhs, g, c, 0, ctrl, omega, 0);
-  k_sor_rb<<<rb_grid(g), dim3(32, 8), 0, s>>>(p, rhs, g, c, 1, ctrl, omega, 0);
+  launch_pdl(k_sor_rb, rb_grid(g), dim3(32, 8), 0, s, p, rhs, g, c, 0, ctrl, omega, 0);
+  launch_pdl(k_sor_rb, rb_grid(g), dim3(32, 8), 0, s, p, rhs, g, c, 1, ctrl, omega, 0);
   sor_seam_passes(p, rhs, g, c, ctrl, omega, 0, s);
 }
 
@@ -209,6 +212,7 @@ __device__ __forceinline__ double wnode(const Grid& g, int i, int j, int k) {
 constexpr int WM_KC = 32;
 template <class R>
 __global__ void __launch_bounds__(256) k_wmean_part(const R* __restrict__ rhs, Grid g, double* part) {
+  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k0 = blockIdx.z * WM_KC, k1 = min(k0 + WM_KC, g.nz);
@@ -235,6 +239,7 @@ __global__ void __launch_bounds__(256) k_wmean_part(const R* __restrict__ rhs, G
 }
 
 __global__ void k_wmean_final(const double* __restrict__ part, long long nblk, double wsum, SolveCtrl* ctrl) {
+  pdl_enter();
   __shared__ double s0[1024];
   double a = 0.0;
   for (long long q = threadIdx.x; q < nblk; q += blockDim.x) a += part[q];
@@ -257,6 +262,7 @@ __global__ void k_wmean_final(const double* __restrict__ part, long long nblk, d
 // compatible rhs and skip the subtraction.
 template <class R>
 __global__ void k_rhs_shift(R* __restrict__ rhs, long long n, const SolveCtrl* ctrl) {
+  pdl_enter();
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const R mean = to_t<R>(ctrl->rhs_mean);  // subtracted in the rhs type
   if (q < n) rhs[q] = rhs[q] - mean;
@@ -401,6 +407,7 @@ __global__ void __launch_bounds__(RZ_TX * RZ_TY) k_resid25(const double* __restr
 template <class R>
 __global__ void __launch_bounds__(256) k_resid_inf(const double* __restrict__ p, const R* __restrict__ rhs,
                                                    Grid g, PoiCoef<double> c, SolveCtrl* ctrl, int shift) {
+  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
@@ -419,6 +426,7 @@ __global__ void __launch_bounds__(256) k_resid_inf(const double* __restrict__ p,
 template <class T>
 __global__ void __launch_bounds__(256) k_smooth_zero(T* __restrict__ e, const T* __restrict__ r, Grid g,
                                                      PoiCoef<T> c, T om, const SolveCtrl* ctrl) {
+  pdl_enter();
   if (ctrl->done) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -470,8 +478,8 @@ __global__ void __launch_bounds__(256) k_smooth(T* __restrict__ e, const T* __re
 
 int launch_sor_sweep_ctrl(double* p, const double* rhs, const Grid& g, const PoiCoef<double>& c,
                           SolveCtrl* ctrl, cudaStream_t s) {
-  k_sor_rb<<<rb_grid(g), dim3(32, 8), 0, s>>>(p, rhs, g, c, 0, ctrl, 0.0, 1);
-  k_sor_rb<<<rb_grid(g), dim3(32, 8), 0, s>>>(p, rhs, g, c, 1, ctrl, 0.0, 1);
+  launch_pdl(k_sor_rb, rb_grid(g), dim3(32, 8), 0, s, p, rhs, g, c, 0, ctrl, 0.0, 1);
+  launch_pdl(k_sor_rb, rb_grid(g), dim3(32, 8), 0, s, p, rhs, g, c, 1, ctrl, 0.0, 1);
   return 2 + sor_seam_passes(p, rhs, g, c, ctrl, 0.0, 1, s);
 }
 
@@ -884,6 +892,7 @@ void launch_mg_outer(double* p, const R* rhs, MGLevel* lv, int nlev, int pre, in
 
 // p <- 2 p - p_prev, p_prev <- p (linear extrapolation of the pressure in time)
 __global__ void k_extrapolate(double* __restrict__ p, double* __restrict__ pprev, long long n) {
+  pdl_enter();
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
   const double pc = p[q];
@@ -891,12 +900,13 @@ __global__ void k_extrapolate(double* __restrict__ p, double* __restrict__ pprev
   pprev[q] = pc;
 }
 void launch_extrapolate(double* p, double* pprev, long long n, cudaStream_t s) {
-  k_extrapolate<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p, pprev, n);
+  launch_pdl(k_extrapolate, (unsigned)((n + 255) / 256), 256, 0, s, p, pprev, n);
 }
 
 // the same extrapolation, also writing the last increment d = p - p_prev in T
 template <class T>
 __global__ void k_extrapolate_d(double* __restrict__ p, double* __restrict__ pprev, T* __restrict__ d, long long n) {
+  pdl_enter();
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
   const double pc = p[q], pv = pprev[q];
@@ -920,6 +930,7 @@ __global__ void k_extrapolate_d(double* __restrict__ p, double* __restrict__ ppr
 // scales need no more than FP32 accumulation)
 template <class T>
 __global__ void k_rms(const T* __restrict__ r, const T* __restrict__ d, long long n, double h2, SolveCtrl* ctrl) {
+  pdl_enter();
   __shared__ float sh[2][32];
   float a = 0.f, b = 0.f;
   for (long long q = threadIdx.x; q < n; q += blockDim.x) {
@@ -954,6 +965,7 @@ __global__ void k_rms(const T* __restrict__ r, const T* __restrict__ d, long lon
 template <class T>
 __global__ void k_features(const T* __restrict__ r, const T* __restrict__ d, long long n, double h2,
                            const SolveCtrl* ctrl, float* __restrict__ feat) {
+  pdl_enter();
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
   feat[q] = (float)((double)r[q] * h2 / ctrl->learn_scale);
@@ -963,6 +975,7 @@ __global__ void k_features(const T* __restrict__ r, const T* __restrict__ d, lon
 // coarse correction e = S_r * y
 template <class T>
 __global__ void k_unscale(const float* __restrict__ y, long long n, const SolveCtrl* ctrl, T* __restrict__ e) {
+  pdl_enter();
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q < n) e[q] = (T)((double)y[q] * ctrl->learn_scale);
 }
@@ -973,6 +986,7 @@ __global__ void k_unscale(const float* __restrict__ y, long long n, const SolveC
 template <class T>
 __global__ void k_target(const T* __restrict__ dp, long long n, const SolveCtrl* ctrl, const float* __restrict__ ch1,
                          float* __restrict__ t) {
+  pdl_enter();
   __shared__ double sh[1024];
   const double sd = ctrl->learn_scale_d;
   double a = 0.0;
@@ -991,6 +1005,7 @@ __global__ void k_target(const T* __restrict__ dp, long long n, const SolveCtrl*
 // d = p - pprev in T
 template <class T>
 __global__ void k_pdiff(const double* __restrict__ p, const double* __restrict__ pprev, T* __restrict__ d, long long n) {
+  pdl_enter();
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q < n) d[q] = to_t<T>(p[q] - pprev[q]);
 }
@@ -998,6 +1013,7 @@ __global__ void k_pdiff(const double* __restrict__ p, const double* __restrict__
 // p += e
 template <class T>
 __global__ void k_padd(double* __restrict__ p, const T* __restrict__ e, long long n) {
+  pdl_enter();
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q < n) p[q] += to_t<double>(e[q]);
 }
@@ -1015,9 +1031,9 @@ static T* restrict_to(MGLevel* lv, int ll, const T* f0, int which, SolveCtrl* ct
     for (int a = 0; a < 3; ++a) cz.c[a] = lv[l].coarsen[a];
     dst = (T*)(which ? lv[l + 1].t : lv[l + 1].e);
     if (cz.c[0] && cz.c[1] && cz.c[2])
-      k_restrict_full<T><<<g3(lv[l + 1].g), dim3(32, 8), 0, s>>>(src, dst, lv[l].g, lv[l + 1].g, ctrl);
+      launch_pdl(k_restrict_full<T>, g3(lv[l + 1].g), dim3(32, 8), 0, s, src, dst, lv[l].g, lv[l + 1].g, ctrl);
     else
-      k_restrict<T><<<g3(lv[l + 1].g), dim3(32, 8), 0, s>>>(src, dst, lv[l].g, lv[l + 1].g, cz, ctrl);
+      launch_pdl(k_restrict<T>, g3(lv[l + 1].g), dim3(32, 8), 0, s, src, dst, lv[l].g, lv[l + 1].g, cz, ctrl);
     src = dst;
     *nl += 1;
   }
@@ -1027,7 +1043,7 @@ static T* restrict_to(MGLevel* lv, int ll, const T* f0, int which, SolveCtrl* ct
 // p <- p_ex, p_prev <- p, and the increment into the finest level's t
 template <class T>
 void launch_learn_extrapolate(double* p, double* pprev, MGLevel* lv, cudaStream_t s, long long* nl) {
-  k_extrapolate_d<T><<<b256(lv[0].g.n), 256, 0, s>>>(p, pprev, (T*)lv[0].t, lv[0].g.n);
+  launch_pdl(k_extrapolate_d<T>, b256(lv[0].g.n), 256, 0, s, p, pprev, (T*)lv[0].t, lv[0].g.n);
   *nl += 1;
 }
 
@@ -1040,8 +1056,8 @@ void launch_learn_features(MGLevel* lv, int ll, SolveCtrl* ctrl, float* feat, cu
   const T* dc = restrict_to<T>(lv, ll, (const T*)lv[0].t, 1, ctrl, s, nl);
   const long long n2 = lv[ll].g.n;
   const double h2 = lv[ll].h[0] * lv[ll].h[0];
-  k_rms<T><<<1, 1024, 0, s>>>(rc, dc, n2, h2, ctrl);
-  k_features<T><<<b256(n2), 256, 0, s>>>(rc, dc, n2, h2, ctrl, feat);
+  launch_pdl(k_rms<T>, 1, 1024, 0, s, rc, dc, n2, h2, ctrl);
+  launch_pdl(k_features<T>, b256(n2), 256, 0, s, rc, dc, n2, h2, ctrl, feat);
   *nl += 2;
 }
 
@@ -1051,22 +1067,22 @@ template <class T>
 void launch_learn_apply(double* p, const float* y, MGLevel* lv, int ll, bool add_to_p, SolveCtrl* ctrl,
                         cudaStream_t s, long long* nl) {
   const long long n2 = lv[ll].g.n;
-  k_unscale<T><<<b256(n2), 256, 0, s>>>(y, n2, ctrl, (T*)lv[ll].e);
+  launch_pdl(k_unscale<T>, b256(n2), 256, 0, s, y, n2, ctrl, (T*)lv[ll].e);
   *nl += 1;
   for (int l = ll - 1; l >= 0; --l) {
     cudaMemsetAsync(lv[l].e, 0, (size_t)lv[l].g.n * sizeof(T), s);
     Coarsen cz;
     for (int a = 0; a < 3; ++a) cz.c[a] = lv[l].coarsen[a];
     if (cz.c[0] && cz.c[1] && cz.c[2])
-      k_prolong_cell<T><<<g3(lv[l + 1].g), dim3(32, 8), 0, s>>>((T*)lv[l].e, (const T*)lv[l + 1].e, lv[l].g,
+      launch_pdl(k_prolong_cell<T>, g3(lv[l + 1].g), dim3(32, 8), 0, s, (T*)lv[l].e, (const T*)lv[l + 1].e, lv[l].g,
                                                                 lv[l + 1].g, ctrl);
     else
-      k_prolong<T><<<g3(lv[l].g), dim3(32, 8), 0, s>>>((T*)lv[l].e, (const T*)lv[l + 1].e, lv[l].g, lv[l + 1].g,
+      launch_pdl(k_prolong<T>, g3(lv[l].g), dim3(32, 8), 0, s, (T*)lv[l].e, (const T*)lv[l + 1].e, lv[l].g, lv[l + 1].g,
                                                        cz, ctrl);
     *nl += 1;
   }
   if (add_to_p) {
-    k_padd<T><<<b256(lv[0].g.n), 256, 0, s>>>(p, (const T*)lv[0].e, lv[0].g.n);
+    launch_pdl(k_padd<T>, b256(lv[0].g.n), 256, 0, s, p, (const T*)lv[0].e, lv[0].g.n);
     *nl += 1;
   }
 }
@@ -1077,9 +1093,9 @@ template <class T>
 void launch_learn_target(const double* p, const double* pprev, MGLevel* lv, int ll, SolveCtrl* ctrl,
                          const float* ch1, float* tgt, cudaStream_t s, long long* nl) {
   const MGLevel& L0 = lv[0];
-  k_pdiff<T><<<b256(L0.g.n), 256, 0, s>>>(p, pprev, (T*)L0.t, L0.g.n);
+  launch_pdl(k_pdiff<T>, b256(L0.g.n), 256, 0, s, p, pprev, (T*)L0.t, L0.g.n);
   const T* dc = restrict_to<T>(lv, ll, (const T*)L0.t, 1, ctrl, s, nl);
-  k_target<T><<<1, 1024, 0, s>>>(dc, lv[ll].g.n, ctrl, ch1, tgt);
+  launch_pdl(k_target<T>, 1, 1024, 0, s, dc, lv[ll].g.n, ctrl, ch1, tgt);
   *nl += 2;
 }
 
@@ -1104,19 +1120,19 @@ void launch_rhs_wmean(const R* rhs, const Grid& g, double* part, SolveCtrl* ctrl
   // sum of the weights: per axis n (periodic) or n - 1 (mirror: halves at both ends)
   double wsum = 1.0;
   for (int a = 0; a < 3; ++a) wsum *= g.bc[a] == AX_MIRROR ? (double)(g.len(a) - 1) : (double)g.len(a);
-  k_wmean_part<R><<<grid, dim3(32, 8), 0, s>>>(rhs, g, part);
-  k_wmean_final<<<1, 1024, 0, s>>>(part, (long long)grid.x * grid.y * grid.z, wsum, ctrl);
+  launch_pdl(k_wmean_part<R>, grid, dim3(32, 8), 0, s, rhs, g, part);
+  launch_pdl(k_wmean_final, 1, 1024, 0, s, part, (long long)grid.x * grid.y * grid.z, wsum, ctrl);
   *nl += 2;
 }
 
 template <class R>
 void launch_residual_inf(const double* p, const R* rhs, const Grid& g, const PoiCoef<double>& c, SolveCtrl* ctrl,
                          bool shift, cudaStream_t s) {
-  k_resid_inf<R><<<g3(g), dim3(32, 8), 0, s>>>(p, rhs, g, c, ctrl, shift);
+  launch_pdl(k_resid_inf<R>, g3(g), dim3(32, 8), 0, s, p, rhs, g, c, ctrl, shift);
 }
 template <class R>
 void launch_rhs_shift(R* rhs, long long n, SolveCtrl* ctrl, cudaStream_t s) {
-  k_rhs_shift<R><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(rhs, n, ctrl);
+  launch_pdl(k_rhs_shift<R>, (unsigned)((n + 255) / 256), 256, 0, s, rhs, n, ctrl);
 }
 template void launch_rhs_shift<float>(float*, long long, SolveCtrl*, cudaStream_t);
 template void launch_rhs_shift<double>(double*, long long, SolveCtrl*, cudaStream_t);
@@ -1126,10 +1142,10 @@ void launch_level_kernel(int which, double* p, const R* rhs, const MGLevel& L, S
                          cudaStream_t s) {
   PoiCoef<T> c = make_poi<T>(L.h[0], L.h[1], L.h[2]);
   if (which == 0) {
-    k_smooth<T><<<g3rb(L.g), dim3(32, 8), 0, s>>>((T*)L.e, (const T*)L.r, L.g, c, 0, (T)1, ctrl);
+    launch_pdl(k_smooth<T>, g3rb(L.g), dim3(32, 8), 0, s, (T*)L.e, (const T*)L.r, L.g, c, 0, (T)1, ctrl);
   } else {
     PoiCoef<double> c64 = make_poi<double>(L.h[0], L.h[1], L.h[2]);
-    k_resid25<T, R, false><<<rz_grid(L.g), dim3(RZ_TX, RZ_TY), 0, s>>>(p, rhs, (T*)L.r, L.g, c64, poi_df(c64),
+    launch_pdl(k_resid25<T, R, false>, rz_grid(L.g), dim3(RZ_TX, RZ_TY), 0, s, p, rhs, (T*)L.r, L.g, c64, poi_df(c64),
                                                                        ctrl, 0);
   }
 }

@@ -13,6 +13,7 @@ namespace o3d {
 template <class T>
 __global__ void k_der(const T* __restrict__ f, T* __restrict__ df, Grid g, AxisCoef<T> c,
                       int axis, int order, int odd) {
+  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
@@ -31,6 +32,7 @@ __global__ void k_der(const T* __restrict__ f, T* __restrict__ df, Grid g, AxisC
 template <class T>
 __global__ void k_nu_t(const T* __restrict__ ux, const T* __restrict__ uy, const T* __restrict__ uz,
                        T* __restrict__ nu_t, Grid g, Coef3<T> cf, T csd2) {
+  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
@@ -63,6 +65,7 @@ template <class T>
 __global__ void __launch_bounds__(256) k_stats(const T* __restrict__ ux, const T* __restrict__ uy,
                                                const T* __restrict__ uz, Grid g, Coef3<T> cf,
                                                double xnu, double* part) {
+  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
@@ -111,6 +114,7 @@ __global__ void __launch_bounds__(256) k_stats(const T* __restrict__ ux, const T
 // ---------------------------------------------------------------------------
 template <class T>
 __global__ void __launch_bounds__(256) k_transeq(ScalArgs<T> A) {
+  pdl_enter();
   const Grid& g = A.g;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -150,6 +154,7 @@ __global__ void __launch_bounds__(256) k_transeq(ScalArgs<T> A) {
 // finalized totals of k_transeq.
 template <class T>
 __global__ void k_scalar_redistribute(T* __restrict__ phi, long long n, const double* sums) {
+  pdl_enter();
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
   const double wsum = sums[2];
@@ -168,6 +173,7 @@ __global__ void k_scalar_redistribute(T* __restrict__ phi, long long n, const do
 // tree and the G parts in order (deterministic).
 __global__ void k_finalize(const double* __restrict__ part, long long nblk, int M,
                            unsigned long long opmask, double* out) {
+  pdl_enter();
   __shared__ double sh[32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   const int G = nw / M > 0 ? nw / M : 1;
@@ -196,6 +202,7 @@ __global__ void k_finalize(const double* __restrict__ part, long long nblk, int 
 
 __global__ void k_finalize_stats(const StatPart* __restrict__ part, long long nblk, Grid g,
                                  double* out6) {
+  pdl_enter();
   __shared__ StatPart sh[1024];
   StatPart acc;
   acc.mn = INFINITY; acc.mx = -INFINITY; acc.sum = 0.0; acc.imx = 0x7fffffffffffffffll;
@@ -220,6 +227,7 @@ __global__ void k_finalize_stats(const StatPart* __restrict__ part, long long nb
 
 template <class S, class D>
 __global__ void k_convert(const S* __restrict__ s, D* __restrict__ d, long long n) {
+  pdl_enter();
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q < n) d[q] = (D)s[q];
 }
@@ -234,36 +242,36 @@ long long pt_blocks(const Grid& g) { dim3 b = pt_grid(g); return (long long)b.x 
 template <class T>
 void launch_der(const T* f, T* df, const Grid& g, const AxisCoef<T>& c, int axis, int order,
                 int odd, cudaStream_t s) {
-  k_der<T><<<pt_grid(g), pt_block(), 0, s>>>(f, df, g, c, axis, order, odd);
+  launch_pdl(k_der<T>, pt_grid(g), pt_block(), 0, s, f, df, g, c, axis, order, odd);
 }
 template <class T>
 void launch_nu_t(const T* ux, const T* uy, const T* uz, T* nu, const Grid& g, const Coef3<T>& cf,
                  T csd2, cudaStream_t s) {
-  k_nu_t<T><<<pt_grid(g), pt_block(), 0, s>>>(ux, uy, uz, nu, g, cf, csd2);
+  launch_pdl(k_nu_t<T>, pt_grid(g), pt_block(), 0, s, ux, uy, uz, nu, g, cf, csd2);
 }
 template <class T>
 void launch_stats(const T* ux, const T* uy, const T* uz, const Grid& g, const Coef3<T>& cf,
                   double xnu, double* part, cudaStream_t s) {
-  k_stats<T><<<pt_grid(g), pt_block(), 0, s>>>(ux, uy, uz, g, cf, xnu, part);
+  launch_pdl(k_stats<T>, pt_grid(g), pt_block(), 0, s, ux, uy, uz, g, cf, xnu, part);
 }
 template <class T>
 void launch_transeq(const ScalArgs<T>& a, const double* sums, cudaStream_t s, long long* nl) {
-  k_transeq<T><<<pt_grid(a.g), pt_block(), 0, s>>>(a);
+  launch_pdl(k_transeq<T>, pt_grid(a.g), pt_block(), 0, s, a);
   launch_finalize(a.part, pt_blocks(a.g), 3, 0ull, (double*)sums, s);
-  k_scalar_redistribute<T><<<(unsigned)((a.g.n + 255) / 256), 256, 0, s>>>(a.phi_out, a.g.n, sums);
+  launch_pdl(k_scalar_redistribute<T>, (unsigned)((a.g.n + 255) / 256), 256, 0, s, a.phi_out, a.g.n, sums);
   *nl += 3;
 }
 void launch_finalize(const double* part, long long nblk, int M, unsigned long long opmask,
                      double* out, cudaStream_t s) {
-  k_finalize<<<1, 1024, 0, s>>>(part, nblk, M, opmask, out);
+  launch_pdl(k_finalize, 1, 1024, 0, s, part, nblk, M, opmask, out);
 }
 void launch_finalize_stats(const StatPart* part, long long nblk, const Grid& g, double* out6,
                            cudaStream_t s) {
-  k_finalize_stats<<<1, 1024, 0, s>>>(part, nblk, g, out6);
+  launch_pdl(k_finalize_stats, 1, 1024, 0, s, part, nblk, g, out6);
 }
 template <class S, class D>
 void launch_convert(const S* s_, D* d, long long n, cudaStream_t s) {
-  k_convert<S, D><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(s_, d, n);
+  launch_pdl(k_convert<S, D>, (unsigned)((n + 255) / 256), 256, 0, s, s_, d, n);
 }
 
 #define O3D_INST(T)                                                                            \

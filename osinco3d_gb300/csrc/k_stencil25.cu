@@ -153,6 +153,7 @@ struct PredRing {
 
 template <class T, int TX, int TY, bool LES, bool ZON>
 __global__ void __launch_bounds__(TX * TY, sizeof(T) == 4 ? 3 : 1) k_predict25(PredArgs<T> A, int kc) {
+  pdl_enter();
   using Ring = PredRing<T, TX, TY>;
   constexpr int SW = Ring::SW;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -336,6 +337,7 @@ __global__ void __launch_bounds__(TX * TY) k_div25(const T* __restrict__ fx, con
                                                    const T* __restrict__ fz, O* __restrict__ out, Grid g,
                                                    Coef3<T> cf, int odd, T dt, int divide, StatPart* part,
                                                    int kc) {
+  pdl_enter();
   using Ring = DivRing<T, TX, TY>;
   constexpr int SW = Ring::SW;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -461,6 +463,7 @@ struct CorrRing {
 
 template <class T, class S, int TX, int TY, bool ZON>
 __global__ void __launch_bounds__(TX * TY) k_correct25(CorrArgs<T, S> A, int kc) {
+  pdl_enter();
   using Ring = CorrRing<T, S, TX, TY>;
   constexpr int SW = Ring::SW;
   constexpr bool CONV = Ring::CONV;
@@ -585,7 +588,7 @@ static void predict_launch(const PredArgs<T>& a, cudaStream_t s) {
   constexpr size_t bytes = sizeof(PredRing<T, TX25, TY25>);
   static const bool attr = (allow_smem(k_predict25<T, TX25, TY25, LES, ZON>, bytes), true);
   (void)attr;
-  k_predict25<T, TX25, TY25, LES, ZON><<<grid25(a.g), dim3(TX25, TY25), bytes, s>>>(a, KC25);
+  launch_pdl(k_predict25<T, TX25, TY25, LES, ZON>, grid25(a.g), dim3(TX25, TY25), bytes, s, a, KC25);
 }
 template <class T>
 void launch_predict(const PredArgs<T>& a, cudaStream_t s) {
@@ -605,7 +608,7 @@ static void div_launch(const T* fx, const T* fy, const T* fz, O* out, const Grid
   constexpr size_t bytes = sizeof(DivRing<T, TX25, TY25>);
   static const bool attr = (allow_smem(k_div25<T, O, TX25, TY25, ZON>, bytes), true);
   (void)attr;
-  k_div25<T, O, TX25, TY25, ZON><<<grid25(g), dim3(TX25, TY25), bytes, s>>>(fx, fy, fz, out, g, cf, odd, dt,
+  launch_pdl(k_div25<T, O, TX25, TY25, ZON>, grid25(g), dim3(TX25, TY25), bytes, s, fx, fy, fz, out, g, cf, odd, dt,
                                                                               divide, part, KC25);
 }
 template <class T, class O>
@@ -620,7 +623,7 @@ static void correct_launch(const CorrArgs<T, S>& a, cudaStream_t s) {
   constexpr size_t bytes = sizeof(CorrRing<T, S, TX25, TY25>);
   static const bool attr = (allow_smem(k_correct25<T, S, TX25, TY25, ZON>, bytes), true);
   (void)attr;
-  k_correct25<T, S, TX25, TY25, ZON><<<grid25(a.g), dim3(TX25, TY25), bytes, s>>>(a, KC25);
+  launch_pdl(k_correct25<T, S, TX25, TY25, ZON>, grid25(a.g), dim3(TX25, TY25), bytes, s, a, KC25);
 }
 template <class T, class S>
 void launch_correct(const CorrArgs<T, S>& a, cudaStream_t s) {

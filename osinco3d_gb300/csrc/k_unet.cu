@@ -67,6 +67,7 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs& A, long long p, in
 
 template <int NT>
 __global__ void __launch_bounds__(128) k_conv3(ConvArgs A) {
+  pdl_enter();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int g = lane >> 2, tq = lane & 3;
   const long long nvox = (long long)A.v.nx * A.v.ny * A.v.nz;
@@ -155,6 +156,7 @@ __global__ void __launch_bounds__(128) k_conv3(ConvArgs A) {
 
 // sum of the S slices' partials in slice order, then the epilogue
 __global__ void k_conv3_reduce(ConvArgs A, int S) {
+  pdl_enter();
   const long long nvox = (long long)A.v.nx * A.v.ny * A.v.nz;
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // channel pair index
   const int half = A.N / 2;
@@ -275,6 +277,7 @@ __global__ void k_bias_grad(const __nv_bfloat16* __restrict__ dy, int dycs, int 
 // ---------------------------------------------------------------------------
 __global__ void k_pool(const __nv_bfloat16* __restrict__ x, int xcs, int xc0, Vol vf, __nv_bfloat16* __restrict__ y,
                        int ycs, int yc0, Vol vc, int C) {
+  pdl_enter();
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long nc = (long long)vc.nx * vc.ny * vc.nz * C;
   if (e >= nc) return;
@@ -307,6 +310,7 @@ __global__ void k_pool_back(const __nv_bfloat16* __restrict__ dy, int dycs, int 
 // nearest upsampling: Y[p] = X[p / 2]
 __global__ void k_upsample(const __nv_bfloat16* __restrict__ x, int xcs, int xc0, Vol vc,
                            __nv_bfloat16* __restrict__ y, int ycs, int yc0, Vol vf, int C) {
+  pdl_enter();
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long nf = (long long)vf.nx * vf.ny * vf.nz * C;
   if (e >= nf) return;
@@ -341,6 +345,7 @@ __global__ void k_upsample_back(const __nv_bfloat16* __restrict__ dy, int dycs, 
 // ---------------------------------------------------------------------------
 __global__ void k_head(const __nv_bfloat16* __restrict__ x, int xcs, int C, long long nvox, const float* __restrict__ wh,
                        const float* __restrict__ bh, float* __restrict__ out) {
+  pdl_enter();
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= nvox) return;
   float s = bh[0];
@@ -424,6 +429,7 @@ __global__ void k_adam(float* __restrict__ w, const float* __restrict__ g, float
 
 // FP32 (n, ny, nz) x `nch` inputs -> BF16 channels-last, padded to cs channels with zeros
 __global__ void k_pack_input(const float* __restrict__ in, int nch, long long nvox, __nv_bfloat16* __restrict__ x, int cs) {
+  pdl_enter();
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= nvox * cs) return;
   const int c = (int)(e % cs);
@@ -454,11 +460,11 @@ int launch_conv3(const ConvArgs& a, cudaStream_t s) {
   int S = a.ws ? conv_splits(nvox, a.K, a.N) : 1;
   while (S > 1 && (long long)S * nvox * a.N > a.ws_cap) --S;
   if (a.N <= 16) {
-    k_conv3<2><<<dim3(gx, (a.N + 15) / 16, S), 128, 0, s>>>(a);
+    launch_pdl(k_conv3<2>, dim3(gx, (a.N + 15) / 16, S), 128, 0, s, a);
   } else {
-    k_conv3<4><<<dim3(gx, (a.N + 31) / 32, S), 128, 0, s>>>(a);
+    launch_pdl(k_conv3<4>, dim3(gx, (a.N + 31) / 32, S), 128, 0, s, a);
   }
-  if (S > 1) k_conv3_reduce<<<(unsigned)((nvox * (a.N / 2) + 255) / 256), 256, 0, s>>>(a, S);
+  if (S > 1) launch_pdl(k_conv3_reduce, (unsigned)((nvox * (a.N / 2) + 255) / 256), 256, 0, s, a, S);
   return S > 1 ? 2 : 1;
 }
 
@@ -484,7 +490,7 @@ static inline unsigned nb256(long long n) { return (unsigned)((n + 255) / 256); 
 
 void launch_pool(const __nv_bfloat16* x, int xcs, int xc0, const Vol& vf, __nv_bfloat16* y, int ycs, int yc0,
                  const Vol& vc, int C, cudaStream_t s) {
-  k_pool<<<nb256((long long)vc.nx * vc.ny * vc.nz * C), 256, 0, s>>>(x, xcs, xc0, vf, y, ycs, yc0, vc, C);
+  launch_pdl(k_pool, nb256((long long)vc.nx * vc.ny * vc.nz * C), 256, 0, s, x, xcs, xc0, vf, y, ycs, yc0, vc, C);
 }
 void launch_pool_back(const __nv_bfloat16* dy, int dycs, int dyc0, const Vol& vc, __nv_bfloat16* dx, int dxcs,
                       int dxc0, const Vol& vf, int C, int accumulate, cudaStream_t s) {
@@ -493,7 +499,7 @@ void launch_pool_back(const __nv_bfloat16* dy, int dycs, int dyc0, const Vol& vc
 }
 void launch_upsample(const __nv_bfloat16* x, int xcs, int xc0, const Vol& vc, __nv_bfloat16* y, int ycs, int yc0,
                      const Vol& vf, int C, cudaStream_t s) {
-  k_upsample<<<nb256((long long)vf.nx * vf.ny * vf.nz * C), 256, 0, s>>>(x, xcs, xc0, vc, y, ycs, yc0, vf, C);
+  launch_pdl(k_upsample, nb256((long long)vf.nx * vf.ny * vf.nz * C), 256, 0, s, x, xcs, xc0, vc, y, ycs, yc0, vf, C);
 }
 void launch_upsample_back(const __nv_bfloat16* dy, int dycs, int dyc0, const Vol& vf, __nv_bfloat16* dx, int dxcs,
                           int dxc0, const Vol& vc, int C, const __nv_bfloat16* mask, int mcs, int mc0,
@@ -503,7 +509,7 @@ void launch_upsample_back(const __nv_bfloat16* dy, int dycs, int dyc0, const Vol
 }
 void launch_head(const __nv_bfloat16* x, int xcs, int C, long long nvox, const float* wh, const float* bh, float* out,
                  cudaStream_t s) {
-  k_head<<<nb256(nvox), 256, 0, s>>>(x, xcs, C, nvox, wh, bh, out);
+  launch_pdl(k_head, nb256(nvox), 256, 0, s, x, xcs, C, nvox, wh, bh, out);
 }
 void launch_head_back(const __nv_bfloat16* x, int xcs, int C, long long nvox, const float* wh, const float* dout,
                       __nv_bfloat16* dx, float* dwh, float* dbh, cudaStream_t s) {
@@ -520,7 +526,7 @@ void launch_adam(float* w, const float* g, float* m, float* v, long long n, floa
   k_adam<<<nb256(n), 256, 0, s>>>(w, g, m, v, n, lr, b1, b2, eps, c1, c2);
 }
 void launch_pack_input(const float* in, int nch, long long nvox, __nv_bfloat16* x, int cs, cudaStream_t s) {
-  k_pack_input<<<nb256(nvox * cs), 256, 0, s>>>(in, nch, nvox, x, cs);
+  launch_pdl(k_pack_input, nb256(nvox * cs), 256, 0, s, in, nch, nvox, x, cs);
 }
 
 }  // namespace o3d
