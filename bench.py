@@ -326,8 +326,11 @@ def gpu_arm(args, rank, world, local):
                          # the plain method: FP64 V(2,2) Gauss-Seidel from the previous pressure
                          ("fp64_mg", fp64),
                          # FP64 with the mixed method's smoother settings and extrapolated guess
-                         ("fp64_mg_v21_om1.15_extrapolated",
-                          dict(fp64, mg_post=1, mg_omega=1.15, guess=o3d.GUESS_EXTRAPOLATED))):
+                         ("fp64_mg_v11_om1.25_extrapolated",
+                          dict(fp64, mg_pre=1, mg_post=1, mg_omega=1.25, guess=o3d.GUESS_EXTRAPOLATED)),
+                         # the fastest configuration found: extrapolated guess, V(2,1), omega 1.3
+                         ("mixed_mg_extrapolated_v21_om1.3",
+                          dict(mixed, mg_pre=2, mg_post=1, mg_omega=1.3, guess=o3d.GUESS_EXTRAPOLATED))):
             if name in variants:
                 continue
             v, cx, _ = run_variant(o3d, name, args.steps, args.warmup, world, **kw)
@@ -352,7 +355,7 @@ def gpu_arm(args, rank, world, local):
         "vs_baseline": None,
         "dtype": "fp32 stencils/V-cycles + fp64 defect correction",
         "data": "synthetic (analytic Taylor-Green initial state)",
-        "config": {"workload": WORKLOAD, "grid": [N, N, N], "poisson": ("FP32 multigrid V(2,1), red-black smoother omega=1.15, one V-cycle per FP64 residual "
+        "config": {"workload": WORKLOAD, "grid": [N, N, N], "poisson": ("FP32 multigrid V(1,1), red-black smoother omega=1.25, one V-cycle per FP64 residual "
                                "(defect correction); initial guess: " + GUESS_DESC[head_name]),
                    "parallelism": f"replicas x{world}", "l2": "no flush: every step streams > 1 GB, far above the 129 MB L2"},
         "e2e": e2e,

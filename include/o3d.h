@@ -107,12 +107,12 @@ typedef struct o3d_params {
   int precision;          /* O3D_PREC_* */
   int solver;             /* O3D_SOLVER_* */
   int mg_levels;          /* 0 = as many as the grid allows */
-  int mg_pre, mg_post;    /* smoothing sweeps; 0 -> V(2,2) in FP64, V(2,1) mixed */
+  int mg_pre, mg_post;    /* smoothing sweeps; 0 -> V(2,2) in FP64, V(1,1) mixed */
   int guess;              /* O3D_GUESS_* */
   int diagnostics;        /* 1: per-step div/CFL/min-max reductions as the driver prints them */
   int mg_cycles;          /* V-cycles per FP64 residual; 0 -> 1 */
   double mg_omega;        /* relaxation of the red-black smoother; 0 -> 1 (Gauss-Seidel)
-                             in FP64, 1.15 mixed */
+                             in FP64, 1.25 mixed */
   int mg_kernels;         /* mixed multigrid: 0 = fused level kernels where a level allows
                              them, 1 = one kernel per pass (same results, for comparison) */
 } o3d_params;

@@ -447,15 +447,16 @@ constexpr int MG_COARSE_SWEEPS = 40;
 
 int mg_smooth_cfg(const o3d_ctx* c, int* pre, int* post) {
   // the plain FP64 method is the V(2,2) Gauss-Seidel cycle; the mixed one
-  // defaults to V(2,1) over-relaxed (fewer FP32 sweeps per FP64 residual)
-  *pre = c->P.mg_pre > 0 ? c->P.mg_pre : 2;
+  // defaults to V(1,1) over-relaxed: with omega 1.25 it needs no more cycles
+  // per step than V(2,1) or V(2,2) at 256^3 and each cycle is cheaper
+  *pre = c->P.mg_pre > 0 ? c->P.mg_pre : (c->mixed ? 1 : 2);
   *post = c->P.mg_post > 0 ? c->P.mg_post : (c->mixed ? 1 : 2);
   return 0;
 }
 
 double mg_omega_of(const o3d_ctx* c) {
   if (c->P.mg_omega > 0.0) return c->P.mg_omega;
-  return c->mixed ? 1.15 : 1.0;
+  return c->mixed ? 1.25 : 1.0;
 }
 
 int capture_mg(o3d_ctx* c) {

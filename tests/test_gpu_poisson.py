@@ -153,8 +153,8 @@ def test_mixed_precision_multigrid(oracle, o3d, shape, bcs):
 
 FUSED_CASES = [
     # shape, boundaries, multigrid options: the zero-start and from-correction
-    # fused kernels, V(2,1) and V(1,2), fused and unfused levels in one cycle
-    ((64, 64, 64), (0, 0, 0), {}),
+    # fused kernels, V(2,1), V(1,1) and V(1,2), fused and unfused levels in one cycle
+    ((64, 64, 64), (0, 0, 0), {"mg_pre": 2, "mg_post": 1}),
     ((64, 65, 32), (0, 1, 0), {"mg_cycles": 2}),
     ((33, 33, 33), (1, 1, 1), {"mg_pre": 1, "mg_post": 2}),
 ]
