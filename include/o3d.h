@@ -87,7 +87,13 @@ typedef struct o3d_params {
   int nx, ny, nz;
   double xlx, yly, zlz;   /* node-inclusive: dx = xlx/(nx-1), src/initialization.f90:182 */
   double x0, y0, z0;
-  /* &BoundaryConditions */
+  /* &BoundaryConditions: 0 periodic, 1 free-slip; on x also 2, open: inflow at
+   * x(1) (u, v, w and phi held at their values there), outflow at x(nx), the
+   * derivatives closed one-sidedly as the reference's dery1D
+   * (src/derivation.f90:950-992) and dp/dx = 0 on both faces; it needs
+   * free-slip y and z.  The reference declares code 2 but binds no scheme
+   * for it (src/initialization.f90:228-242), so this closure is this
+   * library's definition. */
   int nbcx1, nbcxn, nbcy1, nbcyn, nbcz1, nbczn, sim2d;
   /* &AdvanceTime */
   int itscheme;           /* 1 Euler, 2 AB2, 3 AB3 */

@@ -95,10 +95,38 @@ static void d2_odd(double *df, const double *f, int n, size_t s,
   D(n - 2) = -a * (F(n - 4) - F(n - 2)) + b * (F(n - 3) + F(n - 1)) - c * F(n - 2);
   D(n - 1) = -a * (F(n - 3) - F(n - 3)) + b * (F(n - 2) - F(n - 2)) - c * F(n - 1);
 }
+/* Open x axis: no reference routine (src/initialization.f90:228-242 stops on
+ * nbcx = 2).  First derivative: the one-sided closure of dery1D,
+ * src/derivation.f90:975-989, with the 6th-order interior; second
+ * derivative (this build's choice): 2nd-order one-sided at the end nodes,
+ * 2nd-order central next to them, the 4th-order interior elsewhere.  d is
+ * the node spacing. */
+static void d1_open(double *df, const double *f, int n, size_t s,
+                    double a, double b, double c, double d) {
+  D(0) = (-F(2) + 4.0 * F(1) - 3.0 * F(0)) / (2.0 * d);
+  D(1) = (F(2) - F(0)) / (2.0 * d);
+  D(2) = (-F(4) + 8.0 * F(3) - 8.0 * F(1) + F(0)) / (12.0 * d);
+  for (int i = 3; i <= n - 4; ++i)
+    D(i) = a * (F(i + 3) - F(i - 3)) - b * (F(i + 2) - F(i - 2)) + c * (F(i + 1) - F(i - 1));
+  D(n - 3) = (-F(n - 1) + 8.0 * F(n - 2) - 8.0 * F(n - 4) + F(n - 5)) / (12.0 * d);
+  D(n - 2) = (F(n - 1) - F(n - 3)) / (2.0 * d);
+  D(n - 1) = (3.0 * F(n - 1) - 4.0 * F(n - 2) + F(n - 3)) / (2.0 * d);
+}
+
+static void d2_open(double *df, const double *f, int n, size_t s,
+                    double a, double b, double c, double d) {
+  D(0) = (2.0 * F(0) - 5.0 * F(1) + 4.0 * F(2) - F(3)) / (d * d);
+  D(1) = (F(0) - 2.0 * F(1) + F(2)) / (d * d);
+  for (int i = 2; i <= n - 3; ++i)
+    D(i) = -a * (F(i - 2) + F(i + 2)) + b * (F(i - 1) + F(i + 1)) - c * F(i);
+  D(n - 2) = (F(n - 3) - 2.0 * F(n - 2) + F(n - 1)) / (d * d);
+  D(n - 1) = (2.0 * F(n - 1) - 5.0 * F(n - 2) + 4.0 * F(n - 3) - F(n - 4)) / (d * d);
+}
 #undef F
 #undef D
 
 typedef void (*line_fn)(double *, const double *, int, size_t, double, double, double);
+typedef void (*line_fn_d)(double *, const double *, int, size_t, double, double, double, double);
 
 static void apply_lines(double *df, const double *f, int nx, int ny, int nz,
                         int axis, line_fn fn, double a, double b, double c) {
@@ -119,6 +147,21 @@ static void apply_lines(double *df, const double *f, int nx, int ny, int nz,
   }
 }
 
+static void apply_lines_d(double *df, const double *f, int nx, int ny, int nz,
+                          int axis, line_fn_d fn, double a, double b, double c, double d) {
+  size_t sx = 1, sy = (size_t)nx, sz = (size_t)nx * ny;
+  for (int q = 0; q < (axis == 2 ? ny : nz); ++q)
+    for (int p = 0; p < (axis == 0 ? ny : nx); ++p) {
+      size_t base;
+      int n;
+      size_t s;
+      if (axis == 0) { base = sy * p + sz * q; n = nx; s = sx; }
+      else if (axis == 1) { base = sx * p + sz * q; n = ny; s = sy; }
+      else { base = sx * p + sy * q; n = nz; s = sz; }
+      fn(df + base, f + base, n, s, a, b, c, d);
+    }
+}
+
 void orc_der1(double *df, const double *f, int nx, int ny, int nz, int axis,
               int closure, double d) {
   size_t n = (size_t)nx * ny * nz;
@@ -129,6 +172,10 @@ void orc_der1(double *df, const double *f, int nx, int ny, int nz, int axis,
   /* coefficients, src/derivation.f90:26-30 */
   double sixtyd = 60.0 * d;
   double a = 1.0 / sixtyd, b = 9.0 / sixtyd, c = 45.0 / sixtyd;
+  if (closure == ORC_OPEN) {
+    apply_lines_d(df, f, nx, ny, nz, axis, d1_open, a, b, c, d);
+    return;
+  }
   line_fn fn = closure == ORC_PERIODIC ? d1_periodic : closure == ORC_EVEN ? d1_even : d1_odd;
   apply_lines(df, f, nx, ny, nz, axis, fn, a, b, c);
 }
@@ -143,6 +190,10 @@ void orc_der2(double *df, const double *f, int nx, int ny, int nz, int axis,
   /* coefficients, src/derivation.f90:518-522 */
   double twelved2 = 12.0 * d * d;
   double a = 1.0 / twelved2, b = 16.0 / twelved2, c = 30.0 / twelved2;
+  if (closure == ORC_OPEN) {
+    apply_lines_d(df, f, nx, ny, nz, axis, d2_open, a, b, c, d);
+    return;
+  }
   line_fn fn = closure == ORC_PERIODIC ? d2_periodic : closure == ORC_EVEN ? d2_even : d2_odd;
   apply_lines(df, f, nx, ny, nz, axis, fn, a, b, c);
 }
@@ -155,6 +206,7 @@ static int closure_of(const orc_model *m, int axis, int odd) {
   if (axis == 2 && m->sim2d) return ORC_ZERO;
   int bc = axis == 0 ? m->bcx : axis == 1 ? m->bcy : m->bcz;
   if (bc == 0) return ORC_PERIODIC;
+  if (bc == 2) return ORC_OPEN;
   return odd ? ORC_ODD : ORC_EVEN;
 }
 static double step_of(const orc_model *m, int axis) {
@@ -256,6 +308,7 @@ void orc_predict_velocity(const orc_model *m, double *upred[3], double *u[3],
       f1[q] = nu_eff[q] * (d2[0][q] + d2[1][q] + d2[2][q]) -
               (u[0][q] * d1[0][q] + u[1][q] * d1[1][q] + u[2][q] * d1[2][q]);
       up[q] = uc[q] + adu * f1[q] + bdu * f2[q] + cdu * f3[q];
+      if (m->bcx == 2 && q % (size_t)m->nx == 0) up[q] = uc[q]; /* open x: inflow held */
     }
   }
   /* history shift, src/integration.f90:176-188 */
@@ -341,6 +394,24 @@ int orc_correct_pressure(const orc_model *m, double *pp, double *const upred[3],
   double *div = fld(m), *rhs = fld(m);
   orc_divergence(m, div, upred[0], upred[1], upred[2], 1);
   for (size_t q = 0; q < n; ++q) rhs[q] = div[q] / m->dt;
+  if (m->bcx == 2) {
+    /* open x axis (this library's definition): the net flux through the
+     * inflow and outflow faces makes the all-Neumann problem incompatible;
+     * the trapezoid-weighted mean of the rhs (weight 1/2 at the end nodes of
+     * every axis) is removed before the solve */
+    double sw = 0.0, swr = 0.0;
+    for (int k = 0; k < m->nz; ++k)
+      for (int j = 0; j < m->ny; ++j)
+        for (int i = 0; i < m->nx; ++i) {
+          double w = (i == 0 || i == m->nx - 1) ? 0.5 : 1.0;
+          if (j == 0 || j == m->ny - 1) w *= 0.5;
+          if (k == 0 || k == m->nz - 1) w *= 0.5;
+          sw += w;
+          swr += w * rhs[IDX(m, i, j, k)];
+        }
+    double mean = swr / sw;
+    for (size_t q = 0; q < n; ++q) rhs[q] = rhs[q] - mean;
+  }
   int st = orc_poisson_sor(m, pp, rhs, omega, eps, kmax, idyn, iters, dmax);
   free(div); free(rhs);
   return st;
@@ -365,6 +436,8 @@ int orc_correct_velocity(const orc_model *m, double *u[3], double *const upred[3
   for (int a = 0; a < 3; ++a) {
     der1(m, g, pp, a, 0);
     for (size_t q = 0; q < n; ++q) u[a][q] = upred[a][q] - m->dt * g[q];
+    if (m->bcx == 2) /* open x: the inflow nodes keep their prescribed value */
+      for (size_t q = 0; q < n; q += (size_t)m->nx) u[a][q] = upred[a][q];
   }
   for (int a = 0; a < 3 && !bad; ++a) bad = bad_component(u[a], n);
   free(g);
@@ -388,7 +461,8 @@ void orc_transeq(const orc_model *m, double *phi, double *const u[3],
     double alpha = m->iles == 1 ? base + nu_t[q] / m->sc : base;
     fphi[0][q] = alpha * (d2[0][q] + d2[1][q] + d2[2][q]) -
                  (u[0][q] * d1[0][q] + u[1][q] * d1[1][q] + u[2][q] * d1[2][q]) + src[q];
-    phi[q] = phi[q] + adu * fphi[0][q] + bdu * fphi[1][q] + cdu * fphi[2][q];
+    if (!(m->bcx == 2 && q % (size_t)m->nx == 0)) /* open x: inflow held */
+      phi[q] = phi[q] + adu * fphi[0][q] + bdu * fphi[1][q] + cdu * fphi[2][q];
   }
   /* conservative clipping, src/integration.f90:432-450 */
   double sum_old = 0.0;
@@ -400,12 +474,15 @@ void orc_transeq(const orc_model *m, double *phi, double *const u[3],
     sum_new += phi[q];
   }
   double excess = old_avg - sum_new / (double)n;
+  /* open x: the held inflow nodes take no part of the excess */
+  const size_t held = m->bcx == 2 ? (size_t)m->nx : 0;
   double wsum = 0.0;
-  for (size_t q = 0; q < n; ++q) wsum += fmin(phi[q], 1.0 - phi[q]);
+  for (size_t q = 0; q < n; ++q) wsum += (held && q % held == 0) ? 0.0 : fmin(phi[q], 1.0 - phi[q]);
   /* All points clipped to a bound leaves no weight to spread the excess
    * over (the Fortran divides by zero there); the redistribution is skipped. */
   if (wsum != 0.0) {
     for (size_t q = 0; q < n; ++q) {
+      if (held && q % held == 0) continue;
       double w = fmin(phi[q], 1.0 - phi[q]) / wsum;
       phi[q] = fmax(0.0, fmin(1.0, phi[q] + excess * w));
     }
@@ -562,6 +639,35 @@ void orc_init_mixing_layer(const orc_model *m, double x0, double y0, double z0,
         uz[c] = 0.0;
         if (nscr == 1) phi[c] = 0.5 - 0.5 * tanh(t3);
         pp[c] = 1.0;
+      }
+    }
+}
+
+/* initialize_coplanar_jet, src/initial_conditions.f90:244-327: an inner jet
+ * of velocity u1 = u0/ratio within |y| < (h1 + h2)/2, an outer co-flow u0
+ * beyond, zero velocity outside the outer layer; tanh shear layers of
+ * momentum thickness h1/10 and h2/25; p = 0 */
+void orc_init_coplanar_jet(const orc_model *m, double y0, double u0, double l0,
+                           double ratio, int nscr, double *ux, double *uy,
+                           double *uz, double *pp, double *phi) {
+  double u2 = u0, u1 = u2 / ratio, u3 = 0.0 * u2;
+  double d1 = l0, d2 = 2.0 * d1, h1 = 0.5 * d1, h2 = 0.5 * d2;
+  double theta_1 = h1 / 10.0, theta_2 = h2 / 25.0, hm = 0.5 * (h1 + h2);
+  for (int k = 0; k < m->nz; ++k)
+    for (int j = 0; j < m->ny; ++j) {
+      double y = coord(y0, m->dy, j), ay = fabs(y);
+      for (int i = 0; i < m->nx; ++i) {
+        size_t c = IDX(m, i, j, k);
+        if (ay < hm) {
+          ux[c] = 0.5 * (u1 + u2) + 0.5 * (u2 - u1) * tanh((ay - h1) / (2.0 * theta_1));
+          if (nscr == 1) phi[c] = 0.5 * (0.0 + 1.0) + 0.5 * (1.0 - 0.0) * tanh((ay - h1) / (2.0 * theta_1));
+        } else {
+          ux[c] = 0.5 * (u2 + u3) + 0.5 * (u3 - u2) * tanh((ay - h2) / (2.0 * theta_2));
+          if (nscr == 1) phi[c] = 0.5 * (1.0 + 0.0) + 0.5 * (0.0 - 1.0) * tanh((ay - h2) / (2.0 * theta_2));
+        }
+        uy[c] = 0.0;
+        uz[c] = 0.0;
+        pp[c] = 0.0;
       }
     }
 }

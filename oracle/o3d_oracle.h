@@ -17,7 +17,7 @@ extern "C" {
 #endif
 
 /* closure codes: how a derivative treats the two ends of an axis */
-enum { ORC_PERIODIC = 0, ORC_EVEN = 1, ORC_ODD = 2, ORC_ZERO = 3 };
+enum { ORC_PERIODIC = 0, ORC_EVEN = 1, ORC_ODD = 2, ORC_ZERO = 3, ORC_OPEN = 4 };
 
 /* ---- derivation.f90 --------------------------------------------------- */
 /* 6th-order first derivative along `axis` (0=x,1=y,2=z). */
@@ -31,7 +31,7 @@ void orc_der2(double *df, const double *f, int nx, int ny, int nz,
 typedef struct orc_model {
   int nx, ny, nz;
   double dx, dy, dz;
-  int bcx, bcy, bcz;      /* 0 periodic, 1 free-slip (per axis, both ends) */
+  int bcx, bcy, bcz;      /* 0 periodic, 1 free-slip (per axis, both ends), 2 open (x only) */
   int sim2d;
   int itscheme;
   double dt, re, sc;
@@ -98,6 +98,10 @@ void orc_init_mixing_layer(const orc_model *m, double x0, double y0,
                            double z0, double u0, double l0, double ratio,
                            int nscr, double *ux, double *uy, double *uz,
                            double *pp, double *phi);
+/* initialize_coplanar_jet, src/initial_conditions.f90:244-327 (no noise) */
+void orc_init_coplanar_jet(const orc_model *m, double y0, double u0, double l0,
+                           double ratio, int nscr, double *ux, double *uy,
+                           double *uz, double *pp, double *phi);
 
 /* ---- one iteration of the time loop, osinco3d_main.f90:97-128 ---------- */
 typedef struct orc_step_info {

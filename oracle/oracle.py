@@ -19,7 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 SRC = os.path.join(HERE, "o3d_oracle.c")
 
-PERIODIC, EVEN, ODD, ZERO = 0, 1, 2, 3
+PERIODIC, EVEN, ODD, ZERO, OPEN = 0, 1, 2, 3, 4
 SOR_CONVERGED, SOR_STAGNATED, SOR_MAXIT = 0, 1, 2
 
 _dp = C.POINTER(C.c_double)
@@ -214,6 +214,15 @@ def init_mixing_layer(case: Case, state: State, omp: bool = False) -> None:
         C.c_double(case.u0), C.c_double(case.l0), C.c_double(case.ratio),
         C.c_int(case.nscr), ptr(state.u[0]), ptr(state.u[1]), ptr(state.u[2]),
         ptr(state.pp), ptr(state.phi))
+
+
+def init_coplanar_jet(case: Case, state: State, omp: bool = False) -> None:
+    """initialize_coplanar_jet (src/initial_conditions.f90:244-327), no noise."""
+    m = case.model(omp)
+    lib(omp).orc_init_coplanar_jet(
+        C.byref(m), C.c_double(case.y0), C.c_double(case.u0), C.c_double(case.l0),
+        C.c_double(case.ratio), C.c_int(case.nscr), ptr(state.u[0]), ptr(state.u[1]),
+        ptr(state.u[2]), ptr(state.pp), ptr(state.phi))
 
 
 def statistics(case: Case, state: State, t: float, omp: bool = False) -> np.ndarray:

@@ -22,7 +22,7 @@ __device__ __forceinline__ void grad9(const T* const* u, const Grid& g, const Co
       }
       T v[7];
       load_line<3>(u[c], g, a, i, j, k, a == c, v);
-      gr[c][a] = d1(v, cf.ax[a]);
+      gr[c][a] = d1c(v, cf.ax[a], a == 0 ? xclass(g, i) : 0);
     }
 }
 

@@ -25,7 +25,8 @@ __global__ void k_der(const T* __restrict__ f, T* __restrict__ df, Grid g, AxisC
   }
   T v[7];
   load_line<3>(f, g, axis, i, j, k, odd != 0, v);
-  df[q] = order == 1 ? d1(v, c) : d2(v, c);
+  const int pc = axis == 0 ? xclass(g, i) : 0;
+  df[q] = order == 1 ? d1c(v, c, pc) : d2c(v, c, pc);
 }
 
 // standalone calculate_nu_t (src/les_turbulence.f90:54-88)
@@ -47,7 +48,7 @@ __global__ void k_nu_t(const T* __restrict__ ux, const T* __restrict__ uy, const
       if (g.bc[a] == AX_ZERO) { g1[c][a] = (T)0; continue; }
       T v[7];
       load_line<3>(u[c], g, a, i, j, k, a == c, v);
-      g1[c][a] = d1(v, cf.ax[a]);
+      g1[c][a] = d1c(v, cf.ax[a], a == 0 ? xclass(g, i) : 0);
     }
   const T s11 = g1[0][0], s22 = g1[1][1], s33 = g1[2][2];
   const T s12 = (T)0.5 * (g1[0][1] + g1[1][0]);
@@ -83,8 +84,9 @@ __global__ void __launch_bounds__(256) k_stats(const T* __restrict__ ux, const T
         if (g.bc[a] == AX_ZERO) { g1[c][a] = 0.0; g2[c][a] = 0.0; continue; }
         T v[7];
         load_line<3>(u[c], g, a, i, j, k, a == c, v);
-        g1[c][a] = (double)d1(v, cf.ax[a]);
-        g2[c][a] = (double)d2(v, cf.ax[a]);
+        const int pc = a == 0 ? xclass(g, i) : 0;
+        g1[c][a] = (double)d1c(v, cf.ax[a], pc);
+        g2[c][a] = (double)d2c(v, cf.ax[a], pc);
         if (a == 0) uc[c] = (double)v[3];
       }
 #pragma unroll
@@ -129,8 +131,9 @@ __global__ void __launch_bounds__(256) k_transeq(ScalArgs<T> A) {
       if (g.bc[a] == AX_ZERO) { s1[a] = (T)0; s2[a] = (T)0; continue; }
       T v[7];
       load_line<3>(A.phi, g, a, i, j, k, false, v);
-      s1[a] = d1(v, A.cf.ax[a]);
-      s2[a] = d2(v, A.cf.ax[a]);
+      const int cls = a == 0 ? xclass(g, i) : 0;
+      s1[a] = d1c(v, A.cf.ax[a], cls);
+      s2[a] = d2c(v, A.cf.ax[a], cls);
       if (a == 0) pc = v[3];
     }
     T alpha = A.alpha0;
@@ -140,11 +143,12 @@ __global__ void __launch_bounds__(256) k_transeq(ScalArgs<T> A) {
     T ph = pc + A.adu * F;
     if (A.f2) ph = ph + A.bdu * A.f2[q];
     if (A.f3) ph = ph + A.cdu * A.f3[q];
+    if (xclass(g, i) == 1) ph = pc;  // open x axis: the inflow value is held
     A.fnew[q] = F;
     r[0] = (double)ph;
     const T cl = fmax((T)0, fmin((T)1, ph));
     r[1] = (double)cl;
-    r[2] = (double)fmin(cl, (T)1 - cl);
+    r[2] = xclass(g, i) == 1 ? 0.0 : (double)fmin(cl, (T)1 - cl);  // held inflow nodes take no excess
     A.phi_out[q] = cl;
   }
   block_reduce_store<3>(r, ops, A.part, block_linear_id());
@@ -153,10 +157,11 @@ __global__ void __launch_bounds__(256) k_transeq(ScalArgs<T> A) {
 // second clipping pass (src/integration.f90:443-450); sums[0..2] are the
 // finalized totals of k_transeq.
 template <class T>
-__global__ void k_scalar_redistribute(T* __restrict__ phi, long long n, const double* sums) {
+__global__ void k_scalar_redistribute(T* __restrict__ phi, long long n, const double* sums, int nx_inflow) {
   pdl_enter();
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
+  if (nx_inflow > 0 && q % nx_inflow == 0) return;  // open x axis: inflow nodes are held
   const double wsum = sums[2];
   if (wsum == 0.0) return;  // nothing to spread the excess over
   const double excess = sums[0] / (double)n - sums[1] / (double)n;
@@ -258,7 +263,8 @@ template <class T>
 void launch_transeq(const ScalArgs<T>& a, const double* sums, cudaStream_t s, long long* nl) {
   launch_pdl(k_transeq<T>, pt_grid(a.g), pt_block(), 0, s, a);
   launch_finalize(a.part, pt_blocks(a.g), 3, 0ull, (double*)sums, s);
-  launch_pdl(k_scalar_redistribute<T>, (unsigned)((a.g.n + 255) / 256), 256, 0, s, a.phi_out, a.g.n, sums);
+  launch_pdl(k_scalar_redistribute<T>, (unsigned)((a.g.n + 255) / 256), 256, 0, s, a.phi_out, a.g.n, sums,
+             a.g.bc[0] == AX_OPEN ? a.g.nx : 0);
   *nl += 3;
 }
 void launch_finalize(const double* part, long long nblk, int M, unsigned long long opmask,

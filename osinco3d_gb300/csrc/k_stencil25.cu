@@ -167,6 +167,7 @@ __global__ void __launch_bounds__(TX * TY, sizeof(T) == 4 ? 3 : 1) k_predict25(P
   const int np = min(kc, g.nz - k0);
   constexpr bool zon = ZON;  // z derivatives (false: 2D, derz_2dsim)
   const bool may_flip = g.bc[0] == AX_MIRROR || g.bc[1] == AX_MIRROR || g.bc[2] == AX_MIRROR;
+  const int pcx = xclass(g, i);  // open x axis: closure class; 1 = inflow node (held)
   const XYCell cc = xy_cell(g, i, j);
   const Halo<TX, TY> h = halo_cell<TX, TY>(g, i0, j0, t);
   const int sc = (ty + 3) * SW + tx + 3;
@@ -257,7 +258,7 @@ __global__ void __launch_bounds__(TX * TY, sizeof(T) == 4 ? 3 : 1) k_predict25(P
             T v[7];
 #pragma unroll
             for (int m = 0; m < 7; ++m) v[m] = sm.tile[u][c][sc - 3 + m];
-            const T g1x = d1(v, A.cf.ax[0]), g2x = d2(v, A.cf.ax[0]);
+            const T g1x = d1c(v, A.cf.ax[0], pcx), g2x = d2c(v, A.cf.ax[0], pcx);
 #pragma unroll
             for (int m = 0; m < 7; ++m) v[m] = sm.tile[u][c][sc + (m - 3) * SW];
             const T g1y = d1(v, A.cf.ax[1]), g2y = d2(v, A.cf.ax[1]);
@@ -270,7 +271,7 @@ __global__ void __launch_bounds__(TX * TY, sizeof(T) == 4 ? 3 : 1) k_predict25(P
               if (A.f2[c]) up = up + A.bdu * sm.hist[hs][c][t];
               if (A.f3[c]) up = up + A.cdu * sm.hist[hs][3 + c][t];
               A.fnew[c][p] = F;
-              A.up[c][p] = up;
+              A.up[c][p] = pcx == 1 ? v[3] : up;
             }
           }
         } else {
@@ -280,8 +281,8 @@ __global__ void __launch_bounds__(TX * TY, sizeof(T) == 4 ? 3 : 1) k_predict25(P
             T v[7];
 #pragma unroll
             for (int m = 0; m < 7; ++m) v[m] = sm.tile[u][c][sc - 3 + m];
-            g1[c][0] = d1(v, A.cf.ax[0]);
-            g2[c][0] = d2(v, A.cf.ax[0]);
+            g1[c][0] = d1c(v, A.cf.ax[0], pcx);
+            g2[c][0] = d2c(v, A.cf.ax[0], pcx);
 #pragma unroll
             for (int m = 0; m < 7; ++m) v[m] = sm.tile[u][c][sc + (m - 3) * SW];
             g1[c][1] = d1(v, A.cf.ax[1]);
@@ -308,7 +309,7 @@ __global__ void __launch_bounds__(TX * TY, sizeof(T) == 4 ? 3 : 1) k_predict25(P
               if (A.f2[c]) up = up + A.bdu * sm.hist[hs][c][t];
               if (A.f3[c]) up = up + A.cdu * sm.hist[hs][3 + c][t];
               A.fnew[c][p] = F;
-              A.up[c][p] = up;
+              A.up[c][p] = pcx == 1 ? uc[c] : up;
             }
           }
         }
@@ -356,6 +357,7 @@ __global__ void __launch_bounds__(TX * TY) k_div25(const T* __restrict__ fx, con
   const T* __restrict__ hf = h.xh ? fx : fy;  // x-halos belong to the x-lines of fx, y-halos to fy
   const int hodd = h.xh ? ox : oy;
   const int cxi = ty * SW + tx + 3, cyi = (ty + 3) * TX + tx;
+  const int pcx = xclass(g, i);
   const long long out0 = valid ? (long long)i + (long long)g.nx * j : 0;
   const long long sz = g.sz();
 
@@ -417,7 +419,7 @@ __global__ void __launch_bounds__(TX * TY) k_div25(const T* __restrict__ fx, con
         T v[7];
 #pragma unroll
         for (int m = 0; m < 7; ++m) v[m] = sm.sx[u][cxi - 3 + m];
-        const T ddx = d1(v, cf.ax[0]);
+        const T ddx = d1c(v, cf.ax[0], pcx);
 #pragma unroll
         for (int m = 0; m < 7; ++m) v[m] = sm.sy[u][cyi + (m - 3) * TX];
         const T ddy = d1(v, cf.ax[1]);
@@ -477,6 +479,7 @@ __global__ void __launch_bounds__(TX * TY) k_correct25(CorrArgs<T, S> A, int kc)
   const int k0 = blockIdx.z * kc;
   const int np = min(kc, g.nz - k0);
   constexpr bool zon = ZON;  // z derivatives (false: 2D, derz_2dsim)
+  const int pcx = xclass(g, i);  // open x axis: closure class; 1 = inflow node (held)
   const XYCell cc = xy_cell(g, i, j);
   const Halo<TX, TY> h = halo_cell<TX, TY>(g, i0, j0, t);
   const int sc = (ty + 3) * SW + tx + 3;
@@ -543,7 +546,7 @@ __global__ void __launch_bounds__(TX * TY) k_correct25(CorrArgs<T, S> A, int kc)
         T v[7], gp[3];
 #pragma unroll
         for (int m = 0; m < 7; ++m) v[m] = sm.tile[u][sc - 3 + m];
-        gp[0] = d1(v, A.cf.ax[0]);
+        gp[0] = d1c(v, A.cf.ax[0], pcx);
 #pragma unroll
         for (int m = 0; m < 7; ++m) v[m] = sm.tile[u][sc + (m - 3) * SW];
         gp[1] = d1(v, A.cf.ax[1]);
@@ -555,7 +558,7 @@ __global__ void __launch_bounds__(TX * TY) k_correct25(CorrArgs<T, S> A, int kc)
           const int us = lp & PD;
 #pragma unroll
           for (int a = 0; a < 3; ++a) {
-            const T un = sm.up[us][a][t] - A.dt * gp[a];
+            const T un = pcx == 1 ? sm.up[us][a][t] : sm.up[us][a][t] - A.dt * gp[a];  // inflow held
             A.u[a][p] = un;
             if (un != un) nan = true;
             mn[a] = fmin(mn[a], un);

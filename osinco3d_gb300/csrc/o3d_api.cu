@@ -600,7 +600,10 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
   if (st) return st;
   CK(cudaEventRecord(c->ev[2], c->s));
   const bool use_mg = c->P.solver == O3D_SOLVER_MG;
-  if (use_mg || learned || sampling) {
+  // an open x axis makes the all-Neumann problem incompatible (net flux
+  // through inflow and outflow): every solver then takes the rhs less its mean
+  const bool open_x = c->g.bc[0] == AX_OPEN;
+  if (use_mg || learned || sampling || open_x) {
     // the weighted mean of the rhs (compatibility of the singular problem):
     // removed in place, except for the mixed multigrid solve, whose FP64
     // residual kernel subtracts it as it reads the rhs
@@ -715,7 +718,12 @@ int check_params(const o3d_params* p) {
     return O3D_ERR_BADARG;
   }
   auto bc_ok = [](int a, int b) { return (a == 0 && b == 0) || (a == 1 && b == 1); };
-  if (!bc_ok(p->nbcx1, p->nbcxn)) { errf("unrecognized x boundary types nbcx1=%d nbcxn=%d", p->nbcx1, p->nbcxn); return O3D_ERR_BADARG; }
+  const bool xopen = p->nbcx1 == 2 && p->nbcxn == 2;
+  if (!xopen && !bc_ok(p->nbcx1, p->nbcxn)) { errf("unrecognized x boundary types nbcx1=%d nbcxn=%d", p->nbcx1, p->nbcxn); return O3D_ERR_BADARG; }
+  if (xopen && !(p->nbcy1 == 1 && p->nbcyn == 1 && (p->sim2d || (p->nbcz1 == 1 && p->nbczn == 1)))) {
+    errf("an open x axis (nbcx 2) needs free-slip y and z: its pressure problem is Neumann on every face");
+    return O3D_ERR_BADARG;
+  }
   if (!bc_ok(p->nbcy1, p->nbcyn)) { errf("unrecognized y boundary types nbcy1=%d nbcyn=%d", p->nbcy1, p->nbcyn); return O3D_ERR_BADARG; }
   if (!p->sim2d && !bc_ok(p->nbcz1, p->nbczn)) { errf("unrecognized z boundary types nbcz1=%d nbczn=%d", p->nbcz1, p->nbczn); return O3D_ERR_BADARG; }
   if (p->nbcx1 == 1 && p->nbcy1 == 0) {
@@ -776,11 +784,12 @@ int o3d_create(const o3d_params* p, o3d_ctx** out) {
   c->esz = c->mixed ? 4 : 8;
   c->g.nx = p->nx; c->g.ny = p->ny; c->g.nz = p->nz;
   c->g.n = (long long)p->nx * p->ny * p->nz;
-  c->g.bc[0] = p->nbcx1 == 0 ? AX_PERIODIC : AX_MIRROR;
+  c->g.bc[0] = p->nbcx1 == 0 ? AX_PERIODIC : p->nbcx1 == 1 ? AX_MIRROR : AX_OPEN;
   c->g.bc[1] = p->nbcy1 == 0 ? AX_PERIODIC : AX_MIRROR;
   c->g.bc[2] = p->sim2d ? AX_ZERO : (p->nbcz1 == 0 ? AX_PERIODIC : AX_MIRROR);
   // Poisson variant chosen from the x and y types (src/initialization.f90:283-301):
-  // 0000 all periodic, 0011 y mirror, 111111 x, y and z mirror
+  // 0000 all periodic, 0011 y mirror, 111111 x, y and z mirror; an open x
+  // axis takes dp/dx = 0 at inflow and outflow, the mirror remap
   c->gp = c->g;
   if (p->nbcx1 == 0 && p->nbcy1 == 0) { c->gp.bc[0] = c->gp.bc[1] = c->gp.bc[2] = AX_PERIODIC; }
   else if (p->nbcx1 == 0) { c->gp.bc[0] = AX_PERIODIC; c->gp.bc[1] = AX_MIRROR; c->gp.bc[2] = AX_PERIODIC; }

@@ -4,8 +4,9 @@
 // the Fortran fields).  Each axis is periodic (wrap with period n points,
 // src/derivation.f90:34-56), free-slip (mirror about the end nodes; even
 // fields reflect, odd fields reflect with a sign flip, src/derivation.f90:
-// 87-159) or collapsed (2D mode, every z-derivative is zero,
-// src/derivation.f90:481-495).
+// 87-159), collapsed (2D mode, every z-derivative is zero,
+// src/derivation.f90:481-495) or, on x only, open: inflow at x(1), outflow
+// at x(nx), with one-sided closures (d1c / d2c below).
 //
 // Every boundary row of the reference's explicit closures equals the
 // interior stencil applied to ghost values f(-m) = s f(m), f(n-1+m) =
@@ -22,7 +23,7 @@
 
 namespace o3d {
 
-enum AxisBC { AX_PERIODIC = 0, AX_MIRROR = 1, AX_ZERO = 2 };
+enum AxisBC { AX_PERIODIC = 0, AX_MIRROR = 1, AX_ZERO = 2, AX_OPEN = 3 };
 
 struct Grid {
   int nx, ny, nz;
@@ -40,6 +41,7 @@ template <class T>
 struct AxisCoef {
   T a1, b1, c1;   // 1/(60h), 9/(60h), 45/(60h)
   T a2, b2, c2;   // 1/(12h^2), 16/(12h^2), 30/(12h^2)
+  T h2, h12, hh;  // 2h, 12h, h^2: the denominators of the open-axis closures
 };
 
 template <class T>
@@ -52,6 +54,7 @@ inline void make_coef(double h, AxisCoef<double>& c) {
   c.a1 = 1.0 / sixtyd; c.b1 = 9.0 / sixtyd; c.c1 = 45.0 / sixtyd;
   double twelved2 = 12.0 * h * h;
   c.a2 = 1.0 / twelved2; c.b2 = 16.0 / twelved2; c.c2 = 30.0 / twelved2;
+  c.h2 = 2.0 * h; c.h12 = 12.0 * h; c.hh = h * h;
 }
 template <class T>
 inline Coef3<T> cast_coef(const Coef3<double>& d) {
@@ -59,6 +62,7 @@ inline Coef3<T> cast_coef(const Coef3<double>& d) {
   for (int a = 0; a < 3; ++a) {
     r.ax[a].a1 = (T)d.ax[a].a1; r.ax[a].b1 = (T)d.ax[a].b1; r.ax[a].c1 = (T)d.ax[a].c1;
     r.ax[a].a2 = (T)d.ax[a].a2; r.ax[a].b2 = (T)d.ax[a].b2; r.ax[a].c2 = (T)d.ax[a].c2;
+    r.ax[a].h2 = (T)d.ax[a].h2; r.ax[a].h12 = (T)d.ax[a].h12; r.ax[a].hh = (T)d.ax[a].hh;
   }
   return r;
 }
@@ -322,6 +326,45 @@ __device__ __forceinline__ T d1(const T* v, const AxisCoef<T>& c) {
 template <class T>
 __device__ __forceinline__ T d2(const T* v, const AxisCoef<T>& c) {
   return -c.a2 * (v[1] + v[5]) + c.b2 * (v[2] + v[4]) - c.c2 * v[3];
+}
+
+// ---- open x axis (nbcx1 = nbcxn = 2) -------------------------------------
+// The reference binds no derivative for it (src/initialization.f90:228-242
+// stops); this build defines the closure.  First derivative: the one-sided
+// scheme of dery1D (src/derivation.f90:950-992) -- 2nd order one-sided at the
+// end nodes, 2nd-order central next to them, 4th-order central at the third
+// node -- with the 6th-order interior stencil.  Second derivative: 2nd-order
+// one-sided at the end nodes, 2nd-order central next to them, the 4th-order
+// interior stencil elsewhere.  Position class of index i on an open axis of n
+// points: 0 interior, 1..3 the first three nodes, 4..6 the last three.  v is
+// the 7-point window f(i-3 .. i+3); the closures read only its in-range values.
+__device__ __forceinline__ int open_class(int i, int n) {
+  return i < 3 ? i + 1 : (i >= n - 3 ? i - (n - 3) + 4 : 0);
+}
+__device__ __forceinline__ int xclass(const Grid& g, int i) {
+  return g.bc[0] == AX_OPEN ? open_class(i, g.nx) : 0;
+}
+template <class T>
+__device__ __forceinline__ T d1c(const T* v, const AxisCoef<T>& c, int pc) {
+  switch (pc) {
+    case 0: return d1(v, c);
+    case 1: return (-v[5] + (T)4 * v[4] - (T)3 * v[3]) / c.h2;
+    case 2:
+    case 5: return (v[4] - v[2]) / c.h2;
+    case 3:
+    case 4: return (-v[5] + (T)8 * v[4] - (T)8 * v[2] + v[1]) / c.h12;
+    default: return ((T)3 * v[3] - (T)4 * v[2] + v[1]) / c.h2;
+  }
+}
+template <class T>
+__device__ __forceinline__ T d2c(const T* v, const AxisCoef<T>& c, int pc) {
+  switch (pc) {
+    case 1: return ((T)2 * v[3] - (T)5 * v[4] + (T)4 * v[5] - v[6]) / c.hh;
+    case 2:
+    case 5: return (v[2] - (T)2 * v[3] + v[4]) / c.hh;
+    case 6: return ((T)2 * v[3] - (T)5 * v[2] + (T)4 * v[1] - v[0]) / c.hh;
+    default: return d2(v, c);
+  }
 }
 
 // ---- order-preserving keys for atomic min/max of doubles ----------------

@@ -227,6 +227,60 @@ def mixing_layer_fields(params: Params, ratio: float = 0.5, u0: float = 1.0, l0:
     return ux, uy, uz, pp, phi
 
 
+def coplanar_jet_params(nx: int = 768, ny: int = 384, nz: int = 384, lx: float = 20.0, ly: float = 10.0,
+                        lz: float = 10.0, cfl: float = 0.25, ratio: float = 0.5, **kw) -> Params:
+    """Co-planar jet: x open (inflow at x = 0, outflow at x = lx), y and z
+    free-slip on [-ly/2, ly/2] and [-lz/2, lz/2] node-inclusive, Re 2200,
+    Smagorinsky c_s 0.17, passive scalar Sc 0.7, AB3; dt from the CFL number
+    on the inner jet's velocity u0 / ratio.  The domain lengths are this
+    library's choice (the reference gives none for this case)."""
+    u1 = 1.0 / ratio
+    base = dict(nx=nx, ny=ny, nz=nz, xlx=lx, yly=ly, zlz=lz, x0=0.0, y0=-0.5 * ly, z0=-0.5 * lz,
+                nbcx1=2, nbcxn=2, nbcy1=1, nbcyn=1, nbcz1=1, nbczn=1, re=2200.0, iles=1, cs=0.17,
+                nscr=1, sc=0.7, itscheme=3, dt=cfl * (lx / (nx - 1)) / u1)
+    base.update(kw)
+    return default_params(**base)
+
+
+def coplanar_jet_fields(params: Params, ratio: float = 0.5, u0: float = 1.0, l0: float = 1.0,
+                        noise: float = 0.05, seed: int = 1234):
+    """Initial state of the co-planar jet of src/initial_conditions.f90:244-327:
+    an inner jet u1 = u0 / ratio for |y| < (h1 + h2) / 2 and a co-flow u0
+    beyond, tanh layers at h1 = l0/2 (thickness h1/10) and h2 = l0 (h2/25),
+    v = w = p = 0, phi 0 in the inner jet, 1 in the co-flow, 0 beyond.  Seeded
+    uniform noise U(-1, 1) * noise * u0, scaled by the inner layer's shear
+    profile, is added to the three velocity components (the reference's
+    noise is clock-seeded); the inflow plane x = 0 keeps the noisy values it
+    starts with."""
+    nx, ny, nz = params.nx, params.ny, params.nz
+    dy = params.yly / (ny - 1)
+    u2 = u0
+    u1 = u2 / ratio
+    u3 = 0.0 * u2
+    d1 = l0
+    d2 = 2.0 * d1
+    h1, h2 = 0.5 * d1, 0.5 * d2
+    th1, th2 = h1 / 10.0, h2 / 25.0
+    hm = 0.5 * (h1 + h2)
+    ay = np.abs(params.y0 + np.arange(ny) * dy)
+    inner = ay < hm
+    prof = np.where(inner, 0.5 * (u1 + u2) + 0.5 * (u2 - u1) * np.tanh((ay - h1) / (2.0 * th1)),
+                    0.5 * (u2 + u3) + 0.5 * (u3 - u2) * np.tanh((ay - h2) / (2.0 * th2)))
+    ph = np.where(inner, 0.5 + 0.5 * np.tanh((ay - h1) / (2.0 * th1)),
+                  0.5 - 0.5 * np.tanh((ay - h2) / (2.0 * th2)))
+    shape = (nx, ny, nz)
+    ux = np.asfortranarray(np.broadcast_to(prof[None, :, None], shape).copy())
+    uy = np.zeros(shape, order="F")
+    uz = np.zeros(shape, order="F")
+    env = (1.0 / np.cosh((ay - h1) / (2.0 * th1)) ** 2)[None, :, None]
+    rng = np.random.default_rng(seed)
+    for f in (ux, uy, uz):
+        f += noise * u0 * env * rng.uniform(-1.0, 1.0, shape)
+    pp = np.zeros(shape, order="F")
+    phi = np.asfortranarray(np.broadcast_to(ph[None, :, None], shape).copy())
+    return ux, uy, uz, pp, phi
+
+
 def _ptr(a: np.ndarray):
     if a.dtype != np.float64 or not a.flags.f_contiguous:
         raise TypeError("fields must be float64 Fortran-ordered arrays")

@@ -33,6 +33,13 @@ def periodic_case(oracle, n, **kw):
     return oracle.Case(n, n, n, L, L, L, **base)
 
 
+def open_x_case(oracle, n, **kw):
+    """x open (inflow at x(1), outflow at x(nx)), y and z free-slip."""
+    base = dict(bcx=2, bcy=1, bcz=1, dt=0.1 * PI / (n - 1))
+    base.update(kw)
+    return oracle.Case(n, n, n, PI, PI, PI, **base)
+
+
 def free_slip_case(oracle, n, **kw):
     base = dict(bcx=1, bcy=1, bcz=1, dt=0.1 * PI / (n - 1))
     base.update(kw)
@@ -64,6 +71,8 @@ def perturbed(u, seed, amp=1e-2, kinds=("per", "per", "per")):
 
 def kinds_of(case, comp):
     """Parity of velocity component `comp` per axis: periodic axes stay
-    periodic; on free-slip axes the component normal to the wall is odd."""
+    periodic; on free-slip axes the component normal to the wall is odd; an
+    open axis takes any smooth mode (even)."""
     bcs = (case.bcx, case.bcy, case.bcz)
-    return tuple("per" if bcs[a] == 0 else ("odd" if a == comp else "even") for a in range(3))
+    return tuple("per" if bcs[a] == 0 else ("even" if bcs[a] == 2 else ("odd" if a == comp else "even"))
+                 for a in range(3))

@@ -5,7 +5,7 @@ kernels contract a*b+c into fused multiply-adds, the oracle does not."""
 import numpy as np
 import pytest
 
-from _util import PI, free_slip_case, params_of, perturbed, periodic_case, rel_err
+from _util import PI, free_slip_case, open_x_case, params_of, perturbed, periodic_case, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -17,6 +17,7 @@ SHAPES = [
     ((13, 17, 11), (1, 1, 1)),
     ((16, 9, 12), (0, 1, 0)),
     ((20, 33, 8), (0, 1, 1)),
+    ((17, 13, 11), (2, 1, 1)),  # open x: one-sided closures at inflow and outflow
 ]
 
 
@@ -37,7 +38,8 @@ def test_all_derivative_operators(oracle, o3d, shape, bcs):
         for axis in range(3):
             for order in (1, 2):
                 for odd in (0, 1):
-                    closure = oracle.PERIODIC if bcs[axis] == 0 else (oracle.ODD if odd else oracle.EVEN)
+                    closure = (oracle.PERIODIC if bcs[axis] == 0 else oracle.OPEN if bcs[axis] == 2
+                               else (oracle.ODD if odd else oracle.EVEN))
                     ref = (oracle.der1 if order == 1 else oracle.der2)(f, axis, closure, h[axis])
                     got = ctx.der(f, axis, order, bool(odd))
                     assert rel_err(got, ref) < TOL, (axis, order, odd)
@@ -62,7 +64,7 @@ def test_divergence(oracle, o3d, shape, bcs):
             assert rel_err(ctx.divergence(fx, fy, fz, odd), ref) < TOL
 
 
-@pytest.mark.parametrize("maker,n", [(free_slip_case, 17), (periodic_case, 16)])
+@pytest.mark.parametrize("maker,n", [(free_slip_case, 17), (periodic_case, 16), (open_x_case, 15)])
 def test_nu_t(oracle, o3d, maker, n):
     c = maker(oracle, n, iles=1, cs=0.17)
     s = oracle.State.zeros(c)
@@ -77,7 +79,7 @@ def test_nu_t(oracle, o3d, maker, n):
 
 @pytest.mark.parametrize("iles", [0, 1])
 @pytest.mark.parametrize("itscheme", [1, 2, 3])
-@pytest.mark.parametrize("maker,n", [(free_slip_case, 17), (periodic_case, 16)])
+@pytest.mark.parametrize("maker,n", [(free_slip_case, 17), (periodic_case, 16), (open_x_case, 15)])
 def test_predictor_and_history(oracle, o3d, maker, n, itscheme, iles):
     """predict_velocity over itime = 1..4 (Euler / AB2 start-up, then the
     scheme), including the flux-history shift."""
@@ -100,7 +102,7 @@ def test_predictor_and_history(oracle, o3d, maker, n, itscheme, iles):
                 assert rel_err(ctx.download("nu_t"), s.nu_t) < TOL
 
 
-@pytest.mark.parametrize("maker,n", [(free_slip_case, 33), (periodic_case, 32)])
+@pytest.mark.parametrize("maker,n", [(free_slip_case, 33), (periodic_case, 32), (open_x_case, 25)])
 def test_statistics(oracle, o3d, maker, n):
     """statistics_calc (src/utils.f90:243-375): all 16 moments."""
     c = maker(oracle, n, re=1600.0)
@@ -141,11 +143,11 @@ def test_integer_pipe_conversions_are_bit_exact(o3d):
     assert o3d.check_conversions(1 << 24, seed=7) == 0
 
 
-@pytest.mark.parametrize("maker,n", [("periodic", 16), ("free_slip", 13)])
+@pytest.mark.parametrize("maker,n", [("periodic", 16), ("free_slip", 13), ("open_x", 14)])
 def test_vorticity_and_q_criterion(oracle, o3d, maker, n):
     """rotational and calculate_Q_criterion (src/differential_operators.f90:
     40-108) against the oracle, FP64, 1e-12."""
-    c = periodic_case(oracle, n) if maker == "periodic" else free_slip_case(oracle, n)
+    c = {"periodic": periodic_case, "free_slip": free_slip_case, "open_x": open_x_case}[maker](oracle, n)
     rng = np.random.default_rng(21)
     u = [perturbed(np.asfortranarray(rng.standard_normal(c.shape)), 60 + a) for a in range(3)]
     rot = oracle.rotational(c, u)

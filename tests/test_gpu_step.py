@@ -20,6 +20,8 @@ def _run_both(oracle, o3d, c, nsteps, init="tgv", **extra):
     s = oracle.State.zeros(c)
     if init == "tgv":
         oracle.init_tgv(c, s)
+    elif init == "jet":
+        oracle.init_coplanar_jet(c, s)
     else:
         oracle.init_mixing_layer(c, s)
     # a smooth seeded perturbation (with each component's free-slip parity)
@@ -100,6 +102,33 @@ def test_mixing_layer_0011_steps(oracle, o3d):
     ctx.close()
 
 
+def _jet_case(oracle, **kw):
+    # Neumann on every face: SOR contracts slowly, so both sides solve to
+    # 1e-13 to keep the oracle's update-norm stop error below the tolerance
+    nx, ny, nz = 33, 33, 17
+    base = dict(bcx=2, bcy=1, bcz=1, y0=-2.0, z0=-1.0, ratio=0.5, re=2200.0, iles=1, cs=0.17, nscr=1,
+                sc=0.7, dt=0.02, omega=1.7, eps=1e-13, kmax=200000)
+    base.update(kw)
+    return oracle.Case(nx, ny, nz, 8.0, 4.0, 2.0, **base)
+
+
+@pytest.mark.parametrize("solver", [0, 1])
+def test_coplanar_jet_open_x_steps(oracle, o3d, solver):
+    """Open x axis (inflow held at x(1), outflow at x(nx), dery1D-style
+    one-sided closures, Neumann pressure), y/z free-slip, the co-planar jet
+    of src/initial_conditions.f90:244-327 with LES and scalar: SOR and
+    multigrid steps against the oracle's."""
+    c = _jet_case(oracle)
+    s, ctx, infos = _run_both(oracle, o3d, c, 4, init="jet", solver=solver)
+    _check_fields(s, ctx, c)
+    # the inflow plane kept its initial values
+    for a, name in enumerate(("ux", "uy", "uz")):
+        assert np.array_equal(ctx.download(name)[0], s.u[a][0])
+    for ri, gi in infos:
+        assert gi.diverged == 0
+    ctx.close()
+
+
 def test_mixing_layer_odd_periodic_steps(oracle, o3d):
     """The layout of the reference's mixing-layer example (odd point counts
     on the periodic x and z axes, src/../examples/mixing_layer_re3000_les:
@@ -137,6 +166,24 @@ def test_mixed_precision_step_error(oracle, o3d):
                               kmax=200, eps=1e-8)
     for a, name in enumerate(("ux", "uy", "uz")):
         assert rel_err(ctx.download(name), s.u[a]) < 1e-5, name
+    ctx.close()
+
+
+def test_mixed_precision_open_x_jet(oracle, o3d):
+    """The mixed method on the open-x co-planar jet (FP32 stencils with the
+    one-sided closures, FP32 V-cycles in FP64 defect correction): error
+    against the FP64 oracle after 6 steps at FP32 rounding level of the jet
+    velocity (the cross-stream components start at the 1e-2 perturbation),
+    and the inflow plane held to FP32 rounding."""
+    c = _jet_case(oracle)
+    s, ctx, infos = _run_both(oracle, o3d, c, 6, init="jet", solver=o3d.SOLVER_MG,
+                              precision=o3d.PREC_MIXED, kmax=200, eps=1e-8)
+    U = np.abs(s.u[0]).max()
+    for a, name in enumerate(("ux", "uy", "uz")):
+        got = ctx.download(name)
+        assert np.abs(got - s.u[a]).max() < 1e-5 * U, name
+        assert np.abs(got[0] - s.u[a][0]).max() <= 1e-7 * U
+    assert rel_err(ctx.download("phi"), s.phi) < 1e-5
     ctx.close()
 
 

@@ -165,3 +165,36 @@ def test_mixing_layer_initial_state_matches_oracle(oracle, o3d):
     assert np.abs(ux - s.u[0]).max() < 1e-14
     assert np.abs(phi - s.phi).max() < 1e-14
     assert np.abs(pp - s.pp).max() == 0.0 and np.abs(uy).max() == 0.0
+
+
+@pytest.mark.parametrize("n", [9, 16, 23])
+def test_open_axis_closures_are_exact_on_polynomials(oracle, n):
+    """The open x axis (this library's closure; the reference binds none):
+    every row of the first derivative (2nd-order one-sided, 2nd/4th/6th
+    central) is exact on quadratics, every row of the second derivative
+    (2nd-order one-sided, 3-point and 5-point central) on cubics."""
+    d = 0.37
+    x = np.arange(n) * d
+    shape = (n, 5, 4)
+    quad = np.asfortranarray(np.broadcast_to((1.0 + 2.0 * x - 0.7 * x ** 2)[:, None, None], shape).copy())
+    cub = np.asfortranarray(np.broadcast_to((1.0 + 2.0 * x - 0.7 * x ** 2 + 0.3 * x ** 3)[:, None, None],
+                                            shape).copy())
+    d1 = oracle.der1(quad, 0, oracle.OPEN, d)[:, 0, 0]
+    d2 = oracle.der2(cub, 0, oracle.OPEN, d)[:, 0, 0]
+    assert np.abs(d1 - (2.0 - 1.4 * x)).max() < 1e-12
+    assert np.abs(d2 - (-1.4 + 1.8 * x)).max() < 1e-11
+
+
+def test_coplanar_jet_initial_state_matches_oracle(oracle, o3d):
+    """The product's co-planar jet initial state (without noise) equals the
+    oracle's restatement of src/initial_conditions.f90:244-327."""
+    p = o3d.coplanar_jet_params(17, 21, 9, ratio=0.5)
+    ux, uy, uz, pp, phi = o3d.coplanar_jet_fields(p, ratio=0.5, noise=0.0)
+    c = oracle.Case(17, 21, 9, p.xlx, p.yly, p.zlz, bcx=2, bcy=1, bcz=1, dt=p.dt, y0=p.y0, z0=p.z0, nscr=1,
+                    ratio=0.5)
+    s = oracle.State.zeros(c)
+    oracle.init_coplanar_jet(c, s)
+    assert np.abs(ux - s.u[0]).max() < 1e-14
+    assert np.abs(phi - s.phi).max() < 1e-14
+    assert np.abs(pp).max() == 0.0 and np.abs(uy).max() == 0.0 and np.abs(s.pp).max() == 0.0
+    assert abs(ux.max() - 2.0) < 1e-3  # the inner jet, u0 / ratio
