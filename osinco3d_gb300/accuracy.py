@@ -4,6 +4,7 @@ plain FP64 method on the same run, field by field.
 
   python -m osinco3d_gb300.accuracy --case mixing --steps 20
   python -m osinco3d_gb300.accuracy --case tgv --n 256 --steps 20
+  python -m osinco3d_gb300.accuracy --case jet --nx 385 --ny 193 --nz 193 --steps 20
 
 Both runs start from the same host fields and solve every Poisson problem to
 the same eps with the multigrid solver; one JSON line reports, per field,
@@ -53,7 +54,7 @@ def compare(params64, params_mixed, fields, names, steps: int) -> dict:
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--case", choices=["mixing", "tgv"], default="mixing")
+    ap.add_argument("--case", choices=["mixing", "tgv", "jet"], default="mixing")
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--nx", type=int, default=512)
     ap.add_argument("--ny", type=int, default=256)
@@ -69,6 +70,13 @@ def main():
         names = ("ux", "uy", "uz", "pp", "phi")
         workload = (f"temporal mixing layer {args.nx}x{args.ny}x{args.nz}, 60x30x30, Re 3000, LES c_s 0.17, "
                     f"scalar Sc 1, AB3, CFL 0.2, seeded noise 0.05")
+    elif args.case == "jet":
+        p64 = o3d.coplanar_jet_params(args.nx, args.ny, args.nz, precision=o3d.PREC_FP64, **mg)
+        pmx = o3d.coplanar_jet_params(args.nx, args.ny, args.nz, precision=o3d.PREC_MIXED, **mg)
+        fields = o3d.coplanar_jet_fields(p64)
+        names = ("ux", "uy", "uz", "pp", "phi")
+        workload = (f"co-planar jet {args.nx}x{args.ny}x{args.nz}, 20x10x10, x open, y/z free-slip, Re 2200, "
+                    f"LES c_s 0.17, scalar Sc 0.7, AB3, CFL 0.25, seeded noise 0.05")
     else:
         p64 = o3d.tgv_params(args.n, precision=o3d.PREC_FP64, **mg)
         pmx = o3d.tgv_params(args.n, precision=o3d.PREC_MIXED, **mg)

@@ -151,7 +151,7 @@ struct PredRing {
   T hist[PD + 1][6][NC];  // f2 of u, v, w then f3 of u, v, w at the centre cells
 };
 
-template <class T, int TX, int TY, bool LES, bool ZON>
+template <class T, int TX, int TY, bool LES, bool ZON, bool XO>
 __global__ void __launch_bounds__(TX * TY, sizeof(T) == 4 ? 3 : 1) k_predict25(PredArgs<T> A, int kc) {
   pdl_enter();
   using Ring = PredRing<T, TX, TY>;
@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(TX * TY, sizeof(T) == 4 ? 3 : 1) k_predict25(P
   const int np = min(kc, g.nz - k0);
   constexpr bool zon = ZON;  // z derivatives (false: 2D, derz_2dsim)
   const bool may_flip = g.bc[0] == AX_MIRROR || g.bc[1] == AX_MIRROR || g.bc[2] == AX_MIRROR;
-  const int pcx = xclass(g, i);  // open x axis: closure class; 1 = inflow node (held)
+  const int pcx = XO ? xclass(g, i) : 0;  // open x axis: closure class; 1 = inflow node (held)
   const XYCell cc = xy_cell(g, i, j);
   const Halo<TX, TY> h = halo_cell<TX, TY>(g, i0, j0, t);
   const int sc = (ty + 3) * SW + tx + 3;
@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(TX * TY, sizeof(T) == 4 ? 3 : 1) k_predict25(P
             T v[7];
 #pragma unroll
             for (int m = 0; m < 7; ++m) v[m] = sm.tile[u][c][sc - 3 + m];
-            const T g1x = d1c(v, A.cf.ax[0], pcx), g2x = d2c(v, A.cf.ax[0], pcx);
+            const T g1x = d1x<XO>(v, A.cf.ax[0], pcx), g2x = d2x<XO>(v, A.cf.ax[0], pcx);
 #pragma unroll
             for (int m = 0; m < 7; ++m) v[m] = sm.tile[u][c][sc + (m - 3) * SW];
             const T g1y = d1(v, A.cf.ax[1]), g2y = d2(v, A.cf.ax[1]);
@@ -281,8 +281,8 @@ __global__ void __launch_bounds__(TX * TY, sizeof(T) == 4 ? 3 : 1) k_predict25(P
             T v[7];
 #pragma unroll
             for (int m = 0; m < 7; ++m) v[m] = sm.tile[u][c][sc - 3 + m];
-            g1[c][0] = d1c(v, A.cf.ax[0], pcx);
-            g2[c][0] = d2c(v, A.cf.ax[0], pcx);
+            g1[c][0] = d1x<XO>(v, A.cf.ax[0], pcx);
+            g2[c][0] = d2x<XO>(v, A.cf.ax[0], pcx);
 #pragma unroll
             for (int m = 0; m < 7; ++m) v[m] = sm.tile[u][c][sc + (m - 3) * SW];
             g1[c][1] = d1(v, A.cf.ax[1]);
@@ -333,7 +333,7 @@ struct DivRing {
   T sz[ZQ][NC];
 };
 
-template <class T, class O, int TX, int TY, bool ZON>
+template <class T, class O, int TX, int TY, bool ZON, bool XO>
 __global__ void __launch_bounds__(TX * TY) k_div25(const T* __restrict__ fx, const T* __restrict__ fy,
                                                    const T* __restrict__ fz, O* __restrict__ out, Grid g,
                                                    Coef3<T> cf, int odd, T dt, int divide, StatPart* part,
@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(TX * TY) k_div25(const T* __restrict__ fx, con
   const T* __restrict__ hf = h.xh ? fx : fy;  // x-halos belong to the x-lines of fx, y-halos to fy
   const int hodd = h.xh ? ox : oy;
   const int cxi = ty * SW + tx + 3, cyi = (ty + 3) * TX + tx;
-  const int pcx = xclass(g, i);
+  const int pcx = XO ? xclass(g, i) : 0;
   const long long out0 = valid ? (long long)i + (long long)g.nx * j : 0;
   const long long sz = g.sz();
 
@@ -419,7 +419,7 @@ __global__ void __launch_bounds__(TX * TY) k_div25(const T* __restrict__ fx, con
         T v[7];
 #pragma unroll
         for (int m = 0; m < 7; ++m) v[m] = sm.sx[u][cxi - 3 + m];
-        const T ddx = d1c(v, cf.ax[0], pcx);
+        const T ddx = d1x<XO>(v, cf.ax[0], pcx);
 #pragma unroll
         for (int m = 0; m < 7; ++m) v[m] = sm.sy[u][cyi + (m - 3) * TX];
         const T ddy = d1(v, cf.ax[1]);
@@ -463,7 +463,7 @@ struct CorrRing {
   T up[PD + 1][3][NC];
 };
 
-template <class T, class S, int TX, int TY, bool ZON>
+template <class T, class S, int TX, int TY, bool ZON, bool XO>
 __global__ void __launch_bounds__(TX * TY) k_correct25(CorrArgs<T, S> A, int kc) {
   pdl_enter();
   using Ring = CorrRing<T, S, TX, TY>;
@@ -479,7 +479,7 @@ __global__ void __launch_bounds__(TX * TY) k_correct25(CorrArgs<T, S> A, int kc)
   const int k0 = blockIdx.z * kc;
   const int np = min(kc, g.nz - k0);
   constexpr bool zon = ZON;  // z derivatives (false: 2D, derz_2dsim)
-  const int pcx = xclass(g, i);  // open x axis: closure class; 1 = inflow node (held)
+  const int pcx = XO ? xclass(g, i) : 0;  // open x axis: closure class; 1 = inflow node (held)
   const XYCell cc = xy_cell(g, i, j);
   const Halo<TX, TY> h = halo_cell<TX, TY>(g, i0, j0, t);
   const int sc = (ty + 3) * SW + tx + 3;
@@ -546,7 +546,7 @@ __global__ void __launch_bounds__(TX * TY) k_correct25(CorrArgs<T, S> A, int kc)
         T v[7], gp[3];
 #pragma unroll
         for (int m = 0; m < 7; ++m) v[m] = sm.tile[u][sc - 3 + m];
-        gp[0] = d1c(v, A.cf.ax[0], pcx);
+        gp[0] = d1x<XO>(v, A.cf.ax[0], pcx);
 #pragma unroll
         for (int m = 0; m < 7; ++m) v[m] = sm.tile[u][sc + (m - 3) * SW];
         gp[1] = d1(v, A.cf.ax[1]);
@@ -586,52 +586,70 @@ __global__ void __launch_bounds__(TX * TY) k_correct25(CorrArgs<T, S> A, int kc)
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
-template <class T, bool LES, bool ZON>
+template <class T, bool LES, bool ZON, bool XO>
 static void predict_launch(const PredArgs<T>& a, cudaStream_t s) {
   constexpr size_t bytes = sizeof(PredRing<T, TX25, TY25>);
-  static const bool attr = (allow_smem(k_predict25<T, TX25, TY25, LES, ZON>, bytes), true);
+  static const bool attr = (allow_smem(k_predict25<T, TX25, TY25, LES, ZON, XO>, bytes), true);
   (void)attr;
-  launch_pdl(k_predict25<T, TX25, TY25, LES, ZON>, grid25(a.g), dim3(TX25, TY25), bytes, s, a, KC25);
+  launch_pdl(k_predict25<T, TX25, TY25, LES, ZON, XO>, grid25(a.g), dim3(TX25, TY25), bytes, s, a, KC25);
 }
-template <class T>
-void launch_predict(const PredArgs<T>& a, cudaStream_t s) {
+template <class T, bool XO>
+static void predict_launch_xo(const PredArgs<T>& a, cudaStream_t s) {
   const bool zon = a.g.bc[2] != AX_ZERO;
   if (a.les) {
-    if (zon) predict_launch<T, true, true>(a, s);
-    else predict_launch<T, true, false>(a, s);
+    if (zon) predict_launch<T, true, true, XO>(a, s);
+    else predict_launch<T, true, false, XO>(a, s);
   } else {
-    if (zon) predict_launch<T, false, true>(a, s);
-    else predict_launch<T, false, false>(a, s);
+    if (zon) predict_launch<T, false, true, XO>(a, s);
+    else predict_launch<T, false, false, XO>(a, s);
   }
 }
+// the open-x closures are compiled in only for grids with an open x axis
+template <class T>
+void launch_predict(const PredArgs<T>& a, cudaStream_t s) {
+  if (a.g.bc[0] == AX_OPEN) predict_launch_xo<T, true>(a, s);
+  else predict_launch_xo<T, false>(a, s);
+}
 
-template <class T, class O, bool ZON>
+template <class T, class O, bool ZON, bool XO>
 static void div_launch(const T* fx, const T* fy, const T* fz, O* out, const Grid& g, const Coef3<T>& cf, int odd,
                        T dt, int divide, StatPart* part, cudaStream_t s) {
   constexpr size_t bytes = sizeof(DivRing<T, TX25, TY25>);
-  static const bool attr = (allow_smem(k_div25<T, O, TX25, TY25, ZON>, bytes), true);
+  static const bool attr = (allow_smem(k_div25<T, O, TX25, TY25, ZON, XO>, bytes), true);
   (void)attr;
-  launch_pdl(k_div25<T, O, TX25, TY25, ZON>, grid25(g), dim3(TX25, TY25), bytes, s, fx, fy, fz, out, g, cf, odd, dt,
-                                                                              divide, part, KC25);
+  launch_pdl(k_div25<T, O, TX25, TY25, ZON, XO>, grid25(g), dim3(TX25, TY25), bytes, s, fx, fy, fz, out, g, cf, odd,
+             dt, divide, part, KC25);
 }
 template <class T, class O>
 void launch_div(const T* fx, const T* fy, const T* fz, O* out, const Grid& g, const Coef3<T>& cf,
                 int odd, T dt, int divide, StatPart* part, cudaStream_t s) {
-  if (g.bc[2] != AX_ZERO) div_launch<T, O, true>(fx, fy, fz, out, g, cf, odd, dt, divide, part, s);
-  else div_launch<T, O, false>(fx, fy, fz, out, g, cf, odd, dt, divide, part, s);
+  const bool zon = g.bc[2] != AX_ZERO;
+  if (g.bc[0] == AX_OPEN) {
+    if (zon) div_launch<T, O, true, true>(fx, fy, fz, out, g, cf, odd, dt, divide, part, s);
+    else div_launch<T, O, false, true>(fx, fy, fz, out, g, cf, odd, dt, divide, part, s);
+  } else {
+    if (zon) div_launch<T, O, true, false>(fx, fy, fz, out, g, cf, odd, dt, divide, part, s);
+    else div_launch<T, O, false, false>(fx, fy, fz, out, g, cf, odd, dt, divide, part, s);
+  }
 }
 
-template <class T, class S, bool ZON>
+template <class T, class S, bool ZON, bool XO>
 static void correct_launch(const CorrArgs<T, S>& a, cudaStream_t s) {
   constexpr size_t bytes = sizeof(CorrRing<T, S, TX25, TY25>);
-  static const bool attr = (allow_smem(k_correct25<T, S, TX25, TY25, ZON>, bytes), true);
+  static const bool attr = (allow_smem(k_correct25<T, S, TX25, TY25, ZON, XO>, bytes), true);
   (void)attr;
-  launch_pdl(k_correct25<T, S, TX25, TY25, ZON>, grid25(a.g), dim3(TX25, TY25), bytes, s, a, KC25);
+  launch_pdl(k_correct25<T, S, TX25, TY25, ZON, XO>, grid25(a.g), dim3(TX25, TY25), bytes, s, a, KC25);
 }
 template <class T, class S>
 void launch_correct(const CorrArgs<T, S>& a, cudaStream_t s) {
-  if (a.g.bc[2] != AX_ZERO) correct_launch<T, S, true>(a, s);
-  else correct_launch<T, S, false>(a, s);
+  const bool zon = a.g.bc[2] != AX_ZERO;
+  if (a.g.bc[0] == AX_OPEN) {
+    if (zon) correct_launch<T, S, true, true>(a, s);
+    else correct_launch<T, S, false, true>(a, s);
+  } else {
+    if (zon) correct_launch<T, S, true, false>(a, s);
+    else correct_launch<T, S, false, false>(a, s);
+  }
 }
 
 template void launch_predict<double>(const PredArgs<double>&, cudaStream_t);

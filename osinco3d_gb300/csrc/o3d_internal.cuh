@@ -366,6 +366,18 @@ __device__ __forceinline__ T d2c(const T* v, const AxisCoef<T>& c, int pc) {
     default: return d2(v, c);
   }
 }
+// x-derivatives of a kernel compiled with (XO) or without the open-axis
+// closures: without them the plain stencil, no class test
+template <bool XO, class T>
+__device__ __forceinline__ T d1x(const T* v, const AxisCoef<T>& c, int pc) {
+  if constexpr (XO) return d1c(v, c, pc);
+  else return d1(v, c);
+}
+template <bool XO, class T>
+__device__ __forceinline__ T d2x(const T* v, const AxisCoef<T>& c, int pc) {
+  if constexpr (XO) return d2c(v, c, pc);
+  else return d2(v, c);
+}
 
 // ---- order-preserving keys for atomic min/max of doubles ----------------
 __device__ __forceinline__ unsigned long long dkey(double x) {
