@@ -120,6 +120,12 @@ struct o3d_ctx {
   long long learn_nodes;
 
   cudaEvent_t ev[4];
+  // host transfers of o3d_step_host: a copy stream beside the context's, so
+  // that the FP64 <-> FP32 conversions overlap the copies of other fields
+  cudaStream_t xs;
+  cudaEvent_t xev[8];
+  cudaEvent_t p_in_wait;  // set by o3d_step_host: the pressure's upload, awaited when the solve starts
+  double* p_out_host;     // set by o3d_step_host: the pressure's host copy, issued when the solve ends
   long long launches;
 };
 
@@ -443,7 +449,7 @@ int capture_sor(o3d_ctx* c) {
 
 // red-black sweeps of the coarsest multigrid level when it is too large
 // for the one-block shared-memory solve
-constexpr int MG_COARSE_SWEEPS = 40;
+constexpr int MG_COARSE_SWEEPS = 16;
 
 int mg_smooth_cfg(const o3d_ctx* c, int* pre, int* post) {
   // the plain FP64 method is the V(2,2) Gauss-Seidel cycle; the mixed one
@@ -575,6 +581,10 @@ int enqueue_learned_first(o3d_ctx* c, bool learned, bool sampling, bool use_mg, 
 
 // Solves A pp = rhs with the context's solver; pp holds the initial guess.
 int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step_info* info) {
+  if (c->p_in_wait) {  // o3d_step_host: the pressure upload overlapped the predictor and the rhs
+    CK(cudaStreamWaitEvent(c->s, c->p_in_wait, 0));
+    c->p_in_wait = nullptr;
+  }
   const int guess = c->P.guess;
   const bool learned = guess == O3D_GUESS_LEARNED;
   const bool sampling = c->sample_feat != nullptr;
@@ -870,6 +880,8 @@ int o3d_destroy(o3d_ctx* c) {
   if (c->mg_exec) cudaGraphExecDestroy(c->mg_exec);
   if (c->learn_exec) cudaGraphExecDestroy(c->learn_exec);
   for (int q = 0; q < 4; ++q) if (c->ev[q]) cudaEventDestroy(c->ev[q]);
+  for (int q = 0; q < 8; ++q) if (c->xev[q]) cudaEventDestroy(c->xev[q]);
+  if (c->xs) cudaStreamDestroy(c->xs);
   if (c->s) cudaStreamDestroy(c->s);
   delete c;
   return O3D_OK;
@@ -1031,6 +1043,12 @@ int o3d_step(o3d_ctx* c, int itime, o3d_step_info* info) {
   if (st) return st;
   const int ps = solve(c, &c->omega, c->P.eps, c->P.kmax, c->P.idyn, info);
   if (ps < 0) return ps;
+  if (c->p_out_host) {  // o3d_step_host: the final pressure goes out while the step finishes
+    CK(cudaEventRecord(c->xev[5], c->s));
+    CK(cudaStreamWaitEvent(c->xs, c->xev[5], 0));
+    CK(cudaMemcpyAsync(c->p_out_host, c->pp, (size_t)c->g.n * 8, cudaMemcpyDeviceToHost, c->xs));
+    c->p_out_host = nullptr;
+  }
   st = c->mixed ? correct_t<float>(c) : correct_t<double>(c);
   if (st) return st;
   if (c->P.nscr) {
@@ -1070,17 +1088,62 @@ int o3d_step_host(o3d_ctx* c, int itime, double* ux, double* uy, double* uz, dou
                   o3d_step_info* info) {
   if (!c || !ux || !uy || !uz || !pp) return O3D_ERR_BADARG;
   int st;
-  if ((st = put_field(c, c->u[0], ux))) return st;
-  if ((st = put_field(c, c->u[1], uy))) return st;
-  if ((st = put_field(c, c->u[2], uz))) return st;
-  CK(cudaMemcpyAsync(c->pp, pp, (size_t)c->g.n * 8, cudaMemcpyHostToDevice, c->s));
+  if (!c->xs) {
+    CK(cudaStreamCreateWithFlags(&c->xs, cudaStreamNonBlocking));
+    for (int q = 0; q < 8; ++q) CK(cudaEventCreateWithFlags(&c->xev[q], cudaEventDisableTiming));
+  }
+  if (c->mixed && (st = stage_ready(c, 2))) return st;
+  double* const hu[3] = {ux, uy, uz};
+  const size_t bytes = (size_t)c->g.n * 8;
+  // inputs: copied on the copy stream (after earlier work of the context
+  // stream), each velocity converted on the context stream once it landed
+  CK(cudaEventRecord(c->xev[7], c->s));
+  CK(cudaStreamWaitEvent(c->xs, c->xev[7], 0));
+  for (int k = 0; k < 3; ++k) {
+    if (c->mixed) {
+      CK(cudaMemcpyAsync(c->stage[k], hu[k], bytes, cudaMemcpyHostToDevice, c->xs));
+      CK(cudaEventRecord(c->xev[k], c->xs));
+      CK(cudaStreamWaitEvent(c->s, c->xev[k], 0));
+      launch_convert<double, float>(c->stage[k], (float*)c->u[k], c->g.n, c->s);
+      c->launches++;
+    } else {
+      CK(cudaMemcpyAsync(c->u[k], hu[k], bytes, cudaMemcpyHostToDevice, c->xs));
+    }
+  }
+  if (!c->mixed) {
+    CK(cudaEventRecord(c->xev[2], c->xs));
+    CK(cudaStreamWaitEvent(c->s, c->xev[2], 0));
+  }
+  // the pressure lands while the predictor and the rhs run (the solve waits
+  // for it) and leaves as soon as the solve ends (o3d_step issues the copy)
+  CK(cudaMemcpyAsync(c->pp, pp, bytes, cudaMemcpyHostToDevice, c->xs));
+  CK(cudaEventRecord(c->xev[3], c->xs));
+  c->p_in_wait = c->xev[3];
+  c->p_out_host = pp;
+  CKL();
   const int rs = o3d_step(c, itime, info);
-  if (rs < 0) return rs;
-  if ((st = get_field(c, c->u[0], ux))) return st;
-  if ((st = get_field(c, c->u[1], uy))) return st;
-  if ((st = get_field(c, c->u[2], uz))) return st;
-  CK(cudaMemcpyAsync(pp, c->pp, (size_t)c->g.n * 8, cudaMemcpyDeviceToHost, c->s));
-  CK(cudaStreamSynchronize(c->s));
+  c->p_in_wait = nullptr;
+  c->p_out_host = nullptr;
+  if (rs < 0) {
+    cudaStreamSynchronize(c->xs);
+    return rs;
+  }
+  // outputs: each velocity as soon as it is converted
+  CK(cudaEventRecord(c->xev[4], c->s));
+  CK(cudaStreamWaitEvent(c->xs, c->xev[4], 0));
+  for (int k = 0; k < 3; ++k) {
+    if (c->mixed) {
+      launch_convert<float, double>((const float*)c->u[k], c->stage[k], c->g.n, c->s);
+      c->launches++;
+      CK(cudaEventRecord(c->xev[k], c->s));
+      CK(cudaStreamWaitEvent(c->xs, c->xev[k], 0));
+      CK(cudaMemcpyAsync(hu[k], c->stage[k], bytes, cudaMemcpyDeviceToHost, c->xs));
+    } else {
+      CK(cudaMemcpyAsync(hu[k], c->u[k], bytes, cudaMemcpyDeviceToHost, c->xs));
+    }
+  }
+  CKL();
+  CK(cudaStreamSynchronize(c->xs));
   return rs;
 }
 
