@@ -200,7 +200,7 @@ constexpr int down_d() {
 }
 
 template <int S, bool ZERO>
-__global__ void __launch_bounds__(MF_NT, 3)
+__global__ void __launch_bounds__(MF_NT, S == 2 ? 4 : 3)
     k_mg_down(const float* __restrict__ r, const float* __restrict__ ein, float* __restrict__ eout,
               float* __restrict__ rc, Grid gf, Grid gc, PoiCoef<float> c, float om, int kc, const SolveCtrl* ctrl) {
   pdl_enter();
@@ -354,13 +354,15 @@ template <int S2>
 struct UpGeom {
   using X = Ext<MF_FX + 2 * S2, MF_FY + 2 * S2>;
   static constexpr int CX = MF_FX / 2 + S2 + 1, CY = MF_FY / 2 + S2 + 1, CPL = CX * CY;
-  static constexpr int NE = S2 + 2 + MF_D, NR = S2 + 1 + MF_D, NC = 5, NP = MF_D + 1;
+  // planes in flight: 2 for the 2-stage kernel (its rings then fit 4 blocks per SM)
+  static constexpr int D = S2 == 2 ? 2 : MF_D;
+  static constexpr int NE = S2 + 2 + D, NR = S2 + 1 + D, NC = 5, NP = D + 1;
   static constexpr size_t floats = (size_t)(NE + NR) * X::PL + NC * CPL + 2;  // + 2: pad before the p ring
   static constexpr size_t bytes = ((floats * 4 + 15) / 16) * 16 + (size_t)NP * MF_OWN * 8;
 };
 
 template <int S2, bool UPD>
-__global__ void __launch_bounds__(MF_NT, 3)
+__global__ void __launch_bounds__(MF_NT, S2 == 2 ? 4 : 3)
     k_mg_up(const float* __restrict__ epre, const float* __restrict__ ecrs, const float* __restrict__ r,
             float* __restrict__ eout, double* __restrict__ p, Grid gf, Grid gc, PoiCoef<float> c, float om, int kc,
             SolveCtrl* ctrl) {
@@ -368,7 +370,7 @@ __global__ void __launch_bounds__(MF_NT, 3)
   if (ctrl->done) return;
   using G = UpGeom<S2>;
   using X = typename G::X;
-  constexpr int PL = X::PL, D = MF_D, NE = G::NE, NR = G::NR, NC = G::NC, NP = G::NP;
+  constexpr int PL = X::PL, D = G::D, NE = G::NE, NR = G::NR, NC = G::NC, NP = G::NP;
   constexpr int CX = G::CX, CPL = G::CPL;
   extern __shared__ float4 mf_smem[];
   float* const E = (float*)mf_smem;
@@ -538,10 +540,10 @@ static size_t up_smem() {
 }
 
 // planes per block: split z into as many chunks as keep the whole grid
-// resident at three blocks per SM (152 SMs), at least 32 planes each
-static int mf_chunk(const Grid& g) {
+// resident at `per_sm` blocks per SM (152 SMs), at least 32 planes each
+static int mf_chunk(const Grid& g, int per_sm = 3) {
   const long long tiles = (long long)((g.nx + MF_FX - 1) / MF_FX) * ((g.ny + MF_FY - 1) / MF_FY);
-  long long nch = (3 * 152) / (tiles > 0 ? tiles : 1);
+  long long nch = (per_sm * 152) / (tiles > 0 ? tiles : 1);
   if (nch < 1) nch = 1;
   const long long most = (g.nz + 31) / 32;
   if (nch > most) nch = most;
@@ -588,7 +590,7 @@ bool mg_fusable(const MGLevel& L, int pre, int post) {
 void launch_mg_down(const MGLevel& L, const MGLevel& C, float om, int pre, bool zero, const SolveCtrl* ctrl,
                     cudaStream_t s) {
   const PoiCoef<float> c = make_poi<float>(L.h[0], L.h[1], L.h[2]);
-  const int kc = mf_chunk(L.g);
+  const int kc = mf_chunk(L.g, pre == 1 ? 4 : 3);  // the 2-stage kernel fits 4 blocks per SM
   const dim3 grid((L.g.nx + MF_FX - 1) / MF_FX, (L.g.ny + MF_FY - 1) / MF_FY, (L.g.nz + kc - 1) / kc);
   const float* r = (const float*)L.r;
   const float* ein = (const float*)L.e;
@@ -609,7 +611,7 @@ void launch_mg_down(const MGLevel& L, const MGLevel& C, float om, int pre, bool 
 void launch_mg_up(const MGLevel& L, const MGLevel& C, float om, int post, double* p, SolveCtrl* ctrl,
                   cudaStream_t s) {
   const PoiCoef<float> c = make_poi<float>(L.h[0], L.h[1], L.h[2]);
-  const int kc = mf_chunk(L.g);
+  const int kc = mf_chunk(L.g, post == 1 ? 4 : 3);
   const dim3 grid((L.g.nx + MF_FX - 1) / MF_FX, (L.g.ny + MF_FY - 1) / MF_FY, (L.g.nz + kc - 1) / kc);
   const float* epre = (const float*)L.t;
   const float* ec = (const float*)C.e;
