@@ -41,8 +41,8 @@ PRED_BYTES_PER_PT = 15 * 4   # read u,v,w + 6 history, write 3 u* + 3 fluxes
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
 # 256^3 launches, from the ncu captures summarised in profiles/
 TRAFFIC_PER_LAUNCH: dict = {
-    "mg_down": (74.900736 + 31.665664) * 1e6,     # k_mg_down_tgv256.md
-    "mg_up": (286.49984 + 151.700992) * 1e6,      # k_mg_up_tgv256.md
+    "mg_down": (73.19936 + 32.406016) * 1e6,      # k_mg_down_tgv256.md
+    "mg_up": (288.510464 + 152.460032) * 1e6,     # k_mg_up_tgv256.md
     "predict": (623.436032 + 365.83552) * 1e6,    # k_predict25_tgv256.md
     "rhs": (202.962432 + 3.673088) * 1e6,         # k_div25_tgv256.md (statistics pass, no rhs write)
     "correct": (339.60832 + 169.290496) * 1e6,    # k_correct25_tgv256.md
@@ -234,7 +234,7 @@ def measure_e2e(o3d, steps: int, warmup: int, world: int, weights=None, **kw) ->
 KERNEL_BYTES = {
     "predict": (PRED_BYTES_PER_PT, "k_predict25<float>"),
     # read r, write e and the coarse rhs (1/8)
-    "mg_down": (4 + 4 + 0.5, "k_mg_down<4,zero> (pre-smoothing + residual + restriction, finest level)"),
+    "mg_down": (4 + 4 + 0.5, "k_mg_down<2,zero> (pre-smoothing + residual + restriction, finest level)"),
     # read e, r, p and the coarse correction (1/8), write e and p
     "mg_up": (4 + 4 + 8 + 0.5 + 4 + 8, "k_mg_up<2,update> (prolongation + post-smoothing + p += e, finest)"),
     "rhs": (4 * 3 + 8, "k_div25<float,double>"),  # read u* (3 x FP32), write the FP64 rhs
