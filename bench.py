@@ -205,9 +205,44 @@ def run_variant(o3d, name: str, steps: int, warmup: int, world: int, weights=Non
     return out, ctx, it
 
 
-def measure_e2e(o3d, steps: int, warmup: int, world: int, weights=None, **kw) -> dict:
+def gpu_local_cpus(local: int):
+    """CPUs attached to the GPU's PCI device (its NUMA neighbourhood), from
+    sysfs; None when they cannot be found."""
+    try:
+        out = subprocess.run(["nvidia-smi", "-i", str(local), "--query-gpu=pci.bus_id", "--format=csv,noheader"],
+                             capture_output=True, text=True, timeout=30).stdout.strip()
+        dom, bus, rest = out.split(":")
+        path = f"/sys/bus/pci/devices/{int(dom, 16):04x}:{bus.lower()}:{rest.lower()}/local_cpulist"
+        cpus = set()
+        for part in open(path).read().strip().split(","):
+            a, _, b = part.partition("-")
+            cpus.update(range(int(a), int(b or a) + 1))
+        return cpus or None
+    except Exception:
+        return None
+
+
+def measure_e2e(o3d, steps: int, warmup: int, world: int, weights=None, local: int = 0, **kw) -> dict:
     """Same steps through o3d_step_host: the driver's host arrays (page-locked)
-    are copied in before and out after every step."""
+    are copied in before and out after every step.  The host thread runs on
+    the GPU's local CPUs while the arrays are allocated and copied, so that
+    they sit in the memory next to the GPU (as a driver process bound to its
+    GPU's NUMA node would have them)."""
+    saved = os.sched_getaffinity(0) if hasattr(os, "sched_getaffinity") else None
+    cpus = gpu_local_cpus(local)
+    if cpus and saved is not None:
+        try:
+            os.sched_setaffinity(0, cpus & set(range(os.cpu_count() or 1)) or cpus)
+        except OSError:
+            cpus = None
+    try:
+        return _measure_e2e(o3d, steps, warmup, world, weights, **kw)
+    finally:
+        if cpus and saved is not None:
+            os.sched_setaffinity(0, saved)
+
+
+def _measure_e2e(o3d, steps: int, warmup: int, world: int, weights=None, **kw) -> dict:
     p, ctx = make_context(o3d, weights, **kw)
     ux0, uy0, uz0, pp0 = o3d.tgv_fields(p)
     bufs = [pinned_field(ux0.shape) for _ in range(4)]
@@ -317,6 +352,9 @@ def gpu_arm(args, rank, world, local):
     roof = None if args.no_roofline else kernel_roofline(o3d, ctx, peaks)
     ctx.close()
     variants[head_name] = head
+    # end to end right after the headline, on the same configuration
+    e2e = None if args.no_e2e else measure_e2e(o3d, max(3, args.steps // 2), 3, world, weights=weights, local=local,
+                                                **head_kw)
     if not args.quick:
         fp64 = dict(precision=o3d.PREC_FP64, solver=o3d.SOLVER_MG, kmax=100)
         for name, kw in (("mixed_mg", mixed), ("mixed_mg_extrapolated", dict(mixed, guess=o3d.GUESS_EXTRAPOLATED)),
@@ -341,7 +379,6 @@ def gpu_arm(args, rank, world, local):
                                precision=o3d.PREC_FP64, solver=o3d.SOLVER_SOR, kmax=20000)
         c3.close()
         variants["fp64_rbsor"] = v
-    e2e = None if args.no_e2e else measure_e2e(o3d, max(3, args.steps // 2), 3, world, weights=weights, **head_kw)
     line = {
         "metric": METRIC,
         "value": head["mpts_per_s"],
