@@ -119,8 +119,10 @@ typedef struct o3d_params {
   int mg_cycles;          /* V-cycles per FP64 residual; 0 -> 1 */
   double mg_omega;        /* relaxation of the red-black smoother; 0 -> 1 (Gauss-Seidel)
                              in FP64, 1.25 mixed */
-  int mg_kernels;         /* mixed multigrid: 0 = fused level kernels where a level allows
-                             them, 1 = one kernel per pass (same results, for comparison) */
+  int mg_kernels;         /* mixed multigrid: 0 = fused level kernels on the levels large
+                             enough to fill the GPU (at least 152 blocks), 1 = one kernel
+                             per pass, 2 = fused on every level they can serve (same
+                             results in all three; 1 and 2 are for comparison and tests) */
 } o3d_params;
 
 /* Fills *p with the defaults of the reference's namelists (periodic 64^3). */

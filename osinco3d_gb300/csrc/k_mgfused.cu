@@ -574,14 +574,15 @@ int mg_fused_setup() {
   return st;
 }
 
-bool mg_fusable(const MGLevel& L, int pre, int post) {
-  if (!(L.coarsen[0] && L.coarsen[1] && L.coarsen[2])) return false;
+bool mg_fusable(const MGLevel& L, int pre, int post, bool any_size) {
+  if (!(L.coarsen[0] == 1 && L.coarsen[1] == 1 && L.coarsen[2] == 1)) return false;
   if (pre < 1 || pre > 2 || post < 1 || post > 2) return false;
   // the ghost cells of the extended tile stay within one wrap or reflection
   if (L.g.nx < 16 || L.g.ny < 16 || L.g.nz < 16) return false;
   // a level too small to give every SM a block runs faster as one-pass
   // kernels (their blocks are short; a fused block is a long chain of
-  // dependent plane steps)
+  // dependent plane steps); any_size fuses it all the same
+  if (any_size) return true;
   const long long blocks = (long long)((L.g.nx + MF_FX - 1) / MF_FX) * ((L.g.ny + MF_FY - 1) / MF_FY) *
                            ((L.g.nz + mf_chunk(L.g) - 1) / mf_chunk(L.g));
   return blocks >= 152;

@@ -652,6 +652,183 @@ __global__ void __launch_bounds__(256) k_prolong_cell(T* __restrict__ ef, const 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Non-nested coarsening (MGLevel::coarsen mode 2) of an axis that cannot be
+// halved onto a subset of its nodes: an even free-slip axis (n nodes, the
+// ends on the walls) goes to m = (n/2) | 1 nodes spanning the same length,
+// an odd periodic axis (period n) to m = ((n+1)/2) & ~1 nodes per period.
+// With rho = H/h = (n-1)/(m-1) (free-slip) or n/m (periodic), fine node j
+// lies at coarse coordinate s_j = j / rho.  The prolongation interpolates
+// linearly there; the restriction is its transpose over the mirror- or
+// wrap-extended fine grid, scaled by 1/rho (for rho = 2 that is full
+// weighting with the same ghost rule).  Levels below are nested again.
+// 1/rho = num/den; rho <= 2.5, so a coarse node takes at most 5 fine nodes.
+// ---------------------------------------------------------------------------
+constexpr int NN_MAXT = 5;
+
+// Per-axis constants of a non-nested transfer, computed on the host so that
+// no kernel divides: the mode of each axis and, for mode 2, the weight scale
+// num / den^2 of the restriction and 1 / den of the prolongation.
+template <class T>
+struct NNXfer {
+  int c[3];
+  T wsc[3], invden[3];
+};
+
+__host__ __device__ __forceinline__ void nn_ratio(int nf, int nc, int bc, int* num, int* den) {
+  if (bc == AX_PERIODIC) { *num = nc; *den = nf; }
+  else { *num = nc - 1; *den = nf - 1; }
+}
+
+__device__ __forceinline__ int floor_div(int a, int b) { return a >= 0 ? a / b : -((-a + b - 1) / b); }
+
+// restriction taps of coarse index J along one axis: fine indices and weights
+template <class T>
+__device__ __forceinline__ int restrict_taps(int J, int nf, int nc, int bc, int mode, T wsc, int* idx, T* w) {
+  if (mode == 0) { idx[0] = J; w[0] = (T)1; return 1; }
+  if (mode == 1) {
+#pragma unroll
+    for (int o = 0; o < 3; ++o) {
+      idx[o] = fine_of(J, o - 1, nf, bc, 1);
+      w[o] = o == 1 ? (T)0.5 : (T)0.25;
+    }
+    return 3;
+  }
+  int num, den;
+  nn_ratio(nf, nc, bc, &num, &den);
+  // fine je with |je num - J den| < den, weight (den - d) num / den^2,
+  // mapped back by the ghost rule
+  const int lo = floor_div(J * den - den, num) + 1, hi = floor_div(J * den + den - 1, num);
+  int t = 0;
+  for (int je = lo; je <= hi && t < NN_MAXT; ++je) {
+    const int d = abs(je * num - J * den);
+    if (d >= den) continue;
+    int j = je;
+    if (bc == AX_PERIODIC) j = j < 0 ? j + nf : (j >= nf ? j - nf : j);
+    else if (j < 0) j = -j;
+    else if (j > nf - 1) j = 2 * (nf - 1) - j;
+    idx[t] = j;
+    w[t] = (T)(den - d) * wsc;
+    ++t;
+  }
+  return t;
+}
+
+// One thread per coarse point; the taps are summed along x, then y, then z.
+template <class T>
+__global__ void __launch_bounds__(256) k_restrict_nn(const T* __restrict__ tf, T* __restrict__ rc, Grid gf, Grid gc,
+                                                     NNXfer<T> nn, const SolveCtrl* ctrl) {
+  pdl_enter();
+  if (ctrl->done) return;
+  const int I = blockIdx.x * blockDim.x + threadIdx.x;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y;
+  const int K = blockIdx.z;
+  if (I >= gc.nx || J >= gc.ny) return;
+  int xi[NN_MAXT], yi[NN_MAXT], zi[NN_MAXT];
+  T xw[NN_MAXT], yw[NN_MAXT], zw[NN_MAXT];
+  const int nxt = restrict_taps<T>(I, gf.nx, gc.nx, gf.bc[0], nn.c[0], nn.wsc[0], xi, xw);
+  const int nyt = restrict_taps<T>(J, gf.ny, gc.ny, gf.bc[1], nn.c[1], nn.wsc[1], yi, yw);
+  const int nzt = restrict_taps<T>(K, gf.nz, gc.nz, gf.bc[2], nn.c[2], nn.wsc[2], zi, zw);
+  T acc = (T)0;
+  for (int a = 0; a < nzt; ++a) {
+    T accy = (T)0;
+    for (int b = 0; b < nyt; ++b) {
+      const T* row = tf + gf.sz() * zi[a] + gf.sy() * yi[b];
+      T accx = (T)0;
+      for (int q = 0; q < nxt; ++q) accx += xw[q] * __ldg(row + xi[q]);
+      accy += yw[b] * accx;
+    }
+    acc += zw[a] * accy;
+  }
+  rc[idx3(gc, I, J, K)] = acc;
+}
+
+// Prolongation unit of one axis: a coarse cell (fine 2u and 2u + 1) on a
+// halved axis, one fine point otherwise; its two coarse corners and, per
+// fine point, the weight of the second corner.
+template <class T>
+struct PUnit {
+  int f0, nf, c0, c1;
+  T w[2];
+};
+
+template <class T>
+__device__ __forceinline__ PUnit<T> prol_unit(int u, int nfine, int nc, int bc, int mode, T invden) {
+  PUnit<T> r;
+  r.w[0] = r.w[1] = (T)0;
+  if (mode == 1) {
+    r.f0 = 2 * u;
+    r.nf = 2 * u + 1 < nfine ? 2 : 1;
+    r.c0 = u;
+    r.c1 = prol_hi(u, nc, bc);
+    r.w[1] = (T)0.5;
+  } else if (mode == 0) {
+    r.f0 = u;
+    r.nf = 1;
+    r.c0 = r.c1 = u;
+  } else {
+    int num, den;
+    nn_ratio(nfine, nc, bc, &num, &den);
+    const int q = u * num;  // < 2^31: n^2 / 2 for n < 65536
+    r.f0 = u;
+    r.nf = 1;
+    r.c0 = q / den;
+    r.c1 = prol_hi(r.c0, nc, bc);
+    r.w[0] = (T)(q - r.c0 * den) * invden;
+  }
+  return r;
+}
+
+__host__ __device__ __forceinline__ int prol_units(int nfine, int nc, int mode) { return mode == 1 ? nc : nfine; }
+
+// One thread per prolongation unit (up to 2 x 2 x 2 fine points): the 8
+// coarse corners are read once and interpolated along x, then y, then z.
+template <class T>
+__global__ void __launch_bounds__(256) k_prolong_nn(T* __restrict__ ef, const T* __restrict__ ec, Grid gf, Grid gc,
+                                                    NNXfer<T> nn, const SolveCtrl* ctrl) {
+  pdl_enter();
+  if (ctrl->done) return;
+  const int ux = blockIdx.x * blockDim.x + threadIdx.x;
+  const int uy = blockIdx.y * blockDim.y + threadIdx.y;
+  const int uz = blockIdx.z;
+  if (ux >= prol_units(gf.nx, gc.nx, nn.c[0]) || uy >= prol_units(gf.ny, gc.ny, nn.c[1])) return;
+  const PUnit<T> ax = prol_unit<T>(ux, gf.nx, gc.nx, gf.bc[0], nn.c[0], nn.invden[0]);
+  const PUnit<T> ay = prol_unit<T>(uy, gf.ny, gc.ny, gf.bc[1], nn.c[1], nn.invden[1]);
+  const PUnit<T> az = prol_unit<T>(uz, gf.nz, gc.nz, gf.bc[2], nn.c[2], nn.invden[2]);
+  auto at = [&](int a, int b, int c) { return __ldg(ec + (long long)a + gc.sy() * b + gc.sz() * c); };
+  T c[2][2][2];  // [z][y][x] corner
+#pragma unroll
+  for (int zc = 0; zc < 2; ++zc)
+#pragma unroll
+    for (int yc = 0; yc < 2; ++yc) {
+      const int cz = zc ? az.c1 : az.c0, cy = yc ? ay.c1 : ay.c0;
+      c[zc][yc][0] = at(ax.c0, cy, cz);
+      c[zc][yc][1] = at(ax.c1, cy, cz);
+    }
+#pragma unroll
+  for (int px = 0; px < 2; ++px) {
+    if (px >= ax.nf) break;
+    T vy[2][2];  // [y point][z corner]
+#pragma unroll
+    for (int zc = 0; zc < 2; ++zc) {
+      const T v0 = c[zc][0][0] + ax.w[px] * (c[zc][0][1] - c[zc][0][0]);
+      const T v1 = c[zc][1][0] + ax.w[px] * (c[zc][1][1] - c[zc][1][0]);
+#pragma unroll
+      for (int py = 0; py < 2; ++py) vy[py][zc] = v0 + ay.w[py] * (v1 - v0);
+    }
+#pragma unroll
+    for (int py = 0; py < 2; ++py) {
+      if (py >= ay.nf) break;
+#pragma unroll
+      for (int pz = 0; pz < 2; ++pz) {
+        if (pz >= az.nf) break;
+        const T v = vy[py][0] + az.w[pz] * (vy[py][1] - vy[py][0]);
+        ef[(long long)(ax.f0 + px) + gf.sy() * (ay.f0 + py) + gf.sz() * (az.f0 + pz)] += v;
+      }
+    }
+  }
+}
+
 // Coarsest level: one block, shared memory, weighted mean of r removed,
 // `sweeps` red-black Gauss-Seidel sweeps from e = 0.  Each thread resolves
 // once the cells it updates in each colour (the colour's cells of a (j, k)
@@ -791,6 +968,55 @@ __global__ void k_mg_control(SolveCtrl* c) {
 static inline dim3 g3(const Grid& g) { return dim3((g.nx + 31) / 32, (g.ny + 7) / 8, g.nz); }
 static inline dim3 g3rb(const Grid& g) { return dim3((unsigned)(((g.nx + 1) / 2 + 31) / 32), (g.ny + 7) / 8, g.nz); }
 
+// the host constants of a level's non-nested transfer
+template <class T>
+static NNXfer<T> nn_xfer(const MGLevel& L, const MGLevel& C) {
+  NNXfer<T> x;
+  for (int a = 0; a < 3; ++a) {
+    x.c[a] = L.coarsen[a];
+    int num = 1, den = 1;
+    if (L.coarsen[a] == 2) nn_ratio(L.g.len(a), C.g.len(a), L.g.bc[a], &num, &den);
+    x.wsc[a] = (T)((double)num / ((double)den * den));
+    x.invden[a] = (T)(1.0 / den);
+  }
+  return x;
+}
+
+// Restriction of the fine level's tf into the coarse level's rc, and
+// prolongation of the coarse ec added into the fine ef, with the kernel the
+// level's coarsening calls for: every axis halved (one thread per coarse
+// point or cell), some axes kept (generic), or a non-nested axis.
+template <class T>
+static void launch_restrict(const MGLevel& L, const MGLevel& C, const T* tf, T* rc, const SolveCtrl* ctrl,
+                            cudaStream_t s) {
+  Coarsen cz;
+  for (int a = 0; a < 3; ++a) cz.c[a] = L.coarsen[a];
+  const dim3 b(32, 8);
+  if (cz.c[0] == 2 || cz.c[1] == 2 || cz.c[2] == 2)
+    launch_pdl(k_restrict_nn<T>, g3(C.g), b, 0, s, tf, rc, L.g, C.g, nn_xfer<T>(L, C), ctrl);
+  else if (cz.c[0] && cz.c[1] && cz.c[2])
+    launch_pdl(k_restrict_full<T>, g3(C.g), b, 0, s, tf, rc, L.g, C.g, ctrl);
+  else
+    launch_pdl(k_restrict<T>, g3(C.g), b, 0, s, tf, rc, L.g, C.g, cz, ctrl);
+}
+
+template <class T>
+static void launch_prolong_add(const MGLevel& L, const MGLevel& C, T* ef, const T* ec, const SolveCtrl* ctrl,
+                               cudaStream_t s) {
+  Coarsen cz;
+  for (int a = 0; a < 3; ++a) cz.c[a] = L.coarsen[a];
+  const dim3 b(32, 8);
+  if (cz.c[0] == 2 || cz.c[1] == 2 || cz.c[2] == 2) {
+    const dim3 gu((unsigned)((prol_units(L.g.nx, C.g.nx, cz.c[0]) + 31) / 32),
+                  (unsigned)((prol_units(L.g.ny, C.g.ny, cz.c[1]) + 7) / 8), (unsigned)prol_units(L.g.nz, C.g.nz, cz.c[2]));
+    launch_pdl(k_prolong_nn<T>, gu, b, 0, s, ef, ec, L.g, C.g, nn_xfer<T>(L, C), ctrl);
+  }
+  else if (cz.c[0] && cz.c[1] && cz.c[2])
+    launch_pdl(k_prolong_cell<T>, g3(C.g), b, 0, s, ef, ec, L.g, C.g, ctrl);
+  else
+    launch_pdl(k_prolong<T>, g3(L.g), b, 0, s, ef, ec, L.g, C.g, cz, ctrl);
+}
+
 // One V-cycle on level l for A e = r, from e = 0 (zero_init: the first
 // sweep in one pass from r) or from the current e.
 // On a fused level (FP32 only) k_mg_down and k_mg_up do the level's work;
@@ -833,18 +1059,10 @@ static bool vcycle(MGLevel* lv, int l, int nlev, int pre, int post, int coarse_s
   smooth_sweeps<T>(L, e, r, c, om, sweeps, ctrl, s, nl);
   launch_pdl(k_resid<T>, g3(L.g), b, 0, s, e, r, (T*)L.t, L.g, c, ctrl);
   const MGLevel& C = lv[l + 1];
-  Coarsen cz;
-  for (int a = 0; a < 3; ++a) cz.c[a] = L.coarsen[a];
-  if (cz.c[0] && cz.c[1] && cz.c[2])
-    launch_pdl(k_restrict_full<T>, g3(C.g), b, 0, s, (const T*)L.t, (T*)C.r, L.g, C.g, ctrl);
-  else
-    launch_pdl(k_restrict<T>, g3(C.g), b, 0, s, (const T*)L.t, (T*)C.r, L.g, C.g, cz, ctrl);
+  launch_restrict<T>(L, C, (const T*)L.t, (T*)C.r, ctrl, s);
   *nl += 2;
   vcycle<T>(lv, l + 1, nlev, pre, post, coarse_sweeps, om, ctrl, s, nl, true);
-  if (cz.c[0] && cz.c[1] && cz.c[2])
-    launch_pdl(k_prolong_cell<T>, g3(C.g), b, 0, s, e, (const T*)C.e, L.g, C.g, ctrl);
-  else
-    launch_pdl(k_prolong<T>, g3(L.g), b, 0, s, e, (const T*)C.e, L.g, C.g, cz, ctrl);
+  launch_prolong_add<T>(L, C, e, (const T*)C.e, ctrl, s);
   *nl += 1;
   smooth_sweeps<T>(L, e, r, c, om, post, ctrl, s, nl);
   return false;
@@ -1027,13 +1245,8 @@ static T* restrict_to(MGLevel* lv, int ll, const T* f0, int which, SolveCtrl* ct
   const T* src = f0;
   T* dst = nullptr;
   for (int l = 0; l < ll; ++l) {
-    Coarsen cz;
-    for (int a = 0; a < 3; ++a) cz.c[a] = lv[l].coarsen[a];
     dst = (T*)(which ? lv[l + 1].t : lv[l + 1].e);
-    if (cz.c[0] && cz.c[1] && cz.c[2])
-      launch_pdl(k_restrict_full<T>, g3(lv[l + 1].g), dim3(32, 8), 0, s, src, dst, lv[l].g, lv[l + 1].g, ctrl);
-    else
-      launch_pdl(k_restrict<T>, g3(lv[l + 1].g), dim3(32, 8), 0, s, src, dst, lv[l].g, lv[l + 1].g, cz, ctrl);
+    launch_restrict<T>(lv[l], lv[l + 1], src, dst, ctrl, s);
     src = dst;
     *nl += 1;
   }
@@ -1071,14 +1284,7 @@ void launch_learn_apply(double* p, const float* y, MGLevel* lv, int ll, bool add
   *nl += 1;
   for (int l = ll - 1; l >= 0; --l) {
     cudaMemsetAsync(lv[l].e, 0, (size_t)lv[l].g.n * sizeof(T), s);
-    Coarsen cz;
-    for (int a = 0; a < 3; ++a) cz.c[a] = lv[l].coarsen[a];
-    if (cz.c[0] && cz.c[1] && cz.c[2])
-      launch_pdl(k_prolong_cell<T>, g3(lv[l + 1].g), dim3(32, 8), 0, s, (T*)lv[l].e, (const T*)lv[l + 1].e, lv[l].g,
-                                                                lv[l + 1].g, ctrl);
-    else
-      launch_pdl(k_prolong<T>, g3(lv[l].g), dim3(32, 8), 0, s, (T*)lv[l].e, (const T*)lv[l + 1].e, lv[l].g, lv[l + 1].g,
-                                                       cz, ctrl);
+    launch_prolong_add<T>(lv[l], lv[l + 1], (T*)lv[l].e, (const T*)lv[l + 1].e, ctrl, s);
     *nl += 1;
   }
   if (add_to_p) {

@@ -358,17 +358,26 @@ int build_mg(o3d_ctx* c) {
     for (int a = 0; a < 3; ++a) L.h[a] = h[a];
     int any = 0;
     Grid ng = g;
+    double nh[3] = {h[0], h[1], h[2]};
     for (int a = 0; a < 3; ++a) {
       const int n = g.len(a);
-      int cn = 0;
-      if (g.bc[a] == AX_PERIODIC && n % 2 == 0 && n / 2 >= 4) cn = n / 2;
-      if (g.bc[a] == AX_MIRROR && n % 2 == 1 && (n + 1) / 2 >= 3) cn = (n + 1) / 2;
-      L.coarsen[a] = cn > 0;
-      if (cn) {
+      int cn = 0, mode = 0;
+      // halved onto every other node: even periodic, odd free-slip
+      if (g.bc[a] == AX_PERIODIC && n % 2 == 0 && n / 2 >= 4) { cn = n / 2; mode = 1; }
+      if (g.bc[a] == AX_MIRROR && n % 2 == 1 && (n + 1) / 2 >= 3) { cn = (n + 1) / 2; mode = 1; }
+      // non-nested onto about half the nodes (k_restrict_nn / k_prolong_nn):
+      // even free-slip to an odd count, odd periodic to an even count, so
+      // that the next level is nested again; H/h stays <= 2.5
+      if (!mode && g.bc[a] == AX_MIRROR && n >= 6 && n % 2 == 0) { cn = (n / 2) | 1; mode = 2; }
+      if (!mode && g.bc[a] == AX_PERIODIC && n >= 9 && n % 2 == 1) { cn = ((n + 1) / 2) & ~1; mode = 2; }
+      L.coarsen[a] = mode;
+      if (mode) {
         any = 1;
         if (a == 0) ng.nx = cn;
         if (a == 1) ng.ny = cn;
         if (a == 2) ng.nz = cn;
+        if (mode == 1) nh[a] = 2.0 * h[a];
+        else nh[a] = g.bc[a] == AX_PERIODIC ? h[a] * n / cn : h[a] * (n - 1) / (cn - 1);
       }
     }
     ng.n = (long long)ng.nx * ng.ny * ng.nz;
@@ -376,20 +385,20 @@ int build_mg(o3d_ctx* c) {
     if (last) for (int a = 0; a < 3; ++a) L.coarsen[a] = 0;
     c->mg.push_back(L);
     if (last) break;
-    for (int a = 0; a < 3; ++a)
-      if (c->mg.back().coarsen[a]) h[a] *= 2.0;
+    for (int a = 0; a < 3; ++a) h[a] = nh[a];
     g = ng;
   }
   // fused level kernels (FP32): every level that coarsens on all axes and is
   // large enough, unless the caller asked for one kernel per pass
   int pre, post;
   mg_smooth_cfg(c, &pre, &post);
-  const bool fuse = c->mixed && c->P.mg_kernels == 0;
+  const bool fuse = c->mixed && c->P.mg_kernels != 1;
   if (fuse && mg_fused_setup()) {
     errf("fused multigrid kernels: %s", cudaGetErrorString(cudaGetLastError()));
     return O3D_ERR_CUDA;
   }
-  for (size_t l = 0; l + 1 < c->mg.size(); ++l) c->mg[l].fused = fuse && mg_fusable(c->mg[l], pre, post);
+  for (size_t l = 0; l + 1 < c->mg.size(); ++l)
+    c->mg[l].fused = fuse && mg_fusable(c->mg[l], pre, post, c->P.mg_kernels == 2);
   const size_t tsz = c->mixed ? 4 : 8;
   for (auto& L : c->mg) {
     int st;
@@ -508,7 +517,7 @@ int learn_ready(o3d_ctx* c) {
   int ll = 0;
   while (ll < 3 && ll + 1 < (int)c->mg.size()) {
     const MGLevel& L = c->mg[ll];
-    if (!(L.coarsen[0] && L.coarsen[1] && L.coarsen[2])) break;
+    if (!(L.coarsen[0] == 1 && L.coarsen[1] == 1 && L.coarsen[2] == 1)) break;
     const Grid& g = c->mg[ll + 1].g;
     if (g.nx < 16 || g.ny < 16 || g.nz < 16) break;
     ++ll;
@@ -743,8 +752,9 @@ int check_params(const o3d_params* p) {
   if (p->itscheme < 1 || p->itscheme > 3) { errf("itscheme %d unrecognized", p->itscheme); return O3D_ERR_BADARG; }
   if (p->precision != O3D_PREC_FP64 && p->precision != O3D_PREC_MIXED) { errf("precision %d unknown", p->precision); return O3D_ERR_BADARG; }
   if (p->solver != O3D_SOLVER_SOR && p->solver != O3D_SOLVER_MG) { errf("solver %d unknown", p->solver); return O3D_ERR_BADARG; }
-  if (p->mg_omega < 0.0 || p->mg_omega >= 2.0 || p->mg_pre < 0 || p->mg_post < 0 || p->mg_cycles < 0) {
-    errf("multigrid options out of range (mg_omega in [0, 2), sweep and cycle counts >= 0)");
+  if (p->mg_omega < 0.0 || p->mg_omega >= 2.0 || p->mg_pre < 0 || p->mg_post < 0 || p->mg_cycles < 0 ||
+      p->mg_kernels < 0 || p->mg_kernels > 2) {
+    errf("multigrid options out of range (mg_omega in [0, 2), sweep and cycle counts >= 0, mg_kernels 0..2)");
     return O3D_ERR_BADARG;
   }
   if (!(p->dt > 0.0) || !(p->re > 0.0) || !(p->xlx > 0.0) || !(p->yly > 0.0) || !(p->zlz > 0.0)) {

@@ -112,7 +112,7 @@ constexpr int coarse_max() { return (int)(16384 / sizeof(T)); }
 struct MGLevel {
   Grid g;
   double h[3];
-  int coarsen[3];   // axis coarsened towards the next level
+  int coarsen[3];   // per axis towards the next level: 0 kept, 1 halved onto every other node, 2 non-nested
   void* e;          // correction (T)
   void* r;          // right-hand side (T)
   void* t;          // residual scratch (T); the smoothed e between the fused kernels
@@ -121,7 +121,7 @@ struct MGLevel {
 
 // fused FP32 level kernels (k_mgfused.cu)
 int mg_fused_setup();
-bool mg_fusable(const MGLevel& L, int pre, int post);
+bool mg_fusable(const MGLevel& L, int pre, int post, bool any_size);
 void launch_mg_down(const MGLevel& L, const MGLevel& C, float om, int pre, bool zero, const SolveCtrl* ctrl,
                     cudaStream_t s);
 void launch_mg_up(const MGLevel& L, const MGLevel& C, float om, int post, double* p, SolveCtrl* ctrl,

@@ -54,6 +54,7 @@ def test_default_params(o3d):
     (dict(itscheme=4), "itscheme"),               # src/integration.f90:99-104
     (dict(nx=5), "too small"),
     (dict(solver=7), "solver"),
+    (dict(mg_kernels=3), "mg_kernels"),
 ])
 def test_bad_params_rejected_before_any_device_work(o3d, kw, msg):
     p = o3d.default_params(**kw)

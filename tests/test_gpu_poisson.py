@@ -117,22 +117,47 @@ def test_odd_periodic_sor_fixed_point(oracle, o3d, shape, bcs):
     assert err < 200 * eps, (err, it)
 
 
-def test_even_free_slip_axis_multigrid(oracle, o3d):
-    """An even free-slip axis cannot be coarsened vertex-centred: the
-    hierarchy keeps it (semi-coarsening) and the multigrid still reaches the
-    lexicographic SOR fixed point, with more V-cycles."""
-    eps = 1e-9
-    c = _case(oracle, (32, 32, 16), (0, 1, 0))
+NON_NESTED = [
+    # (shape, boundaries, the neighbouring shape whose axes all halve onto
+    # every other node): an even free-slip axis, an odd periodic axis, and
+    # the reference's mixing-layer layout (odd periodic x and z) with an even
+    # free-slip y
+    ((32, 32, 16), (0, 1, 0), (32, 33, 16)),
+    ((33, 32, 32), (0, 0, 0), (32, 32, 32)),
+    ((31, 32, 17), (0, 1, 0), (32, 33, 16)),
+]
+
+
+def _mg_solve(oracle, o3d, shape, bcs, eps, **kw):
+    c = _case(oracle, shape, bcs)
     rhs = _compatible_rhs(c, 5)
+    with o3d.Context(params_of(o3d, c, solver=o3d.SOLVER_MG, **kw)) as ctx:
+        got = ctx.field()
+        st, it, dm, om = ctx.poisson_solve(got, rhs, 1.0, eps, 400, 0)
+    assert st == o3d.OK, (st, it, dm)
+    return c, rhs, got, it
+
+
+@pytest.mark.parametrize("shape,bcs,nested", NON_NESTED)
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_non_nested_coarsening_multigrid(oracle, o3d, shape, bcs, nested, precision):
+    """An axis that cannot be halved onto every other node (even free-slip,
+    odd periodic) is coarsened onto a non-nested grid of about half the
+    nodes, with linear interpolation and its transpose: the multigrid reaches
+    the lexicographic SOR fixed point, in about as many V-cycles as on the
+    neighbouring size (keeping the axis instead, semi-coarsening, takes 5 to
+    20 more at these sizes)."""
+    eps = 1e-9
+    kw = {} if precision == "fp64" else {"precision": o3d.PREC_MIXED}
+    c, rhs, got, it = _mg_solve(oracle, o3d, shape, bcs, eps, **kw)
     ref = oracle.field3(c.shape)
     st, _, _, _ = oracle.poisson_sor(c, ref, rhs, 1.8, eps * 1e-3, 200000)
     assert st == oracle.SOR_CONVERGED
-    with o3d.Context(params_of(o3d, c, solver=o3d.SOLVER_MG)) as ctx:
-        got = ctx.field()
-        st, it, dm, om = ctx.poisson_solve(got, rhs, 1.8, eps, 400, 0)
-    assert st == o3d.OK, (st, it, dm)
     err = np.abs(_demean(got) - _demean(ref)).max()
-    assert err < 5 * eps, (err, it)
+    tol = 5 * eps if precision == "fp64" else 1e-6 * np.abs(ref).max() + 5 * eps
+    assert err < tol, (err, it)
+    _, _, _, it_nested = _mg_solve(oracle, o3d, nested, bcs, eps, **kw)
+    assert it <= it_nested + 2, (it, it_nested)
 
 
 @pytest.mark.parametrize("shape,bcs", VARIANTS)
@@ -152,30 +177,41 @@ def test_mixed_precision_multigrid(oracle, o3d, shape, bcs):
 
 
 FUSED_CASES = [
-    # shape, boundaries, multigrid options: the zero-start and from-correction
-    # fused kernels, V(2,1), V(1,1) and V(1,2), fused and unfused levels in one cycle
-    ((64, 64, 64), (0, 0, 0), {"mg_pre": 2, "mg_post": 1}),
-    ((64, 65, 32), (0, 1, 0), {"mg_cycles": 2}),
-    ((33, 33, 33), (1, 1, 1), {"mg_pre": 1, "mg_post": 2}),
+    # shape, boundaries, multigrid options, the mg_kernels mode compared with
+    # one kernel per pass (1): 2 fuses every level the kernels can serve (at
+    # these sizes all but the coarsest, with partial tiles), 0 only the levels
+    # of at least 152 blocks.  The zero-start and from-correction kernels,
+    # V(2,1), V(1,1) and V(1,2), odd free-slip sizes, and fused levels below a
+    # non-nested one.
+    ((64, 64, 64), (0, 0, 0), {"mg_pre": 2, "mg_post": 1}, 2),
+    ((64, 65, 32), (0, 1, 0), {"mg_cycles": 2}, 2),
+    ((33, 33, 33), (1, 1, 1), {"mg_pre": 1, "mg_post": 2}, 2),
+    ((64, 64, 32), (0, 1, 0), {}, 2),
+    ((256, 256, 64), (0, 0, 0), {}, 0),
 ]
 
 
-@pytest.mark.parametrize("shape,bcs,kw", FUSED_CASES)
-def test_fused_level_kernels_match_unfused(oracle, o3d, shape, bcs, kw):
+@pytest.mark.parametrize("shape,bcs,kw,mode", FUSED_CASES)
+def test_fused_level_kernels_match_unfused(oracle, o3d, shape, bcs, kw, mode):
     """The fused level kernels (pre-smoothing + residual + restriction, and
     prolongation + post-smoothing + update) evaluate the expressions of the
     one-pass kernels in the same order: both solves agree bit for bit."""
     c = _case(oracle, shape, bcs)
     rhs = _compatible_rhs(c, 13)
     out = []
-    for mk in (0, 1):
+    for mk in (mode, 1):
         prm = params_of(o3d, c, solver=o3d.SOLVER_MG, precision=o3d.PREC_MIXED, mg_kernels=mk, **kw)
         with o3d.Context(prm) as ctx:
             got = ctx.field()
+            n0 = ctx.launches
             st, it, dm, om = ctx.poisson_solve(got, rhs, 1.0, 1e-9, 100, 0)
-        out.append((st, it, dm, got))
+            per_cycle = (ctx.launches - n0) / it
+        out.append((st, it, dm, got, per_cycle))
+    assert out[0][0] == o3d.OK
     assert out[0][:3] == out[1][:3]
     np.testing.assert_array_equal(out[0][3], out[1][3])
+    # the fused levels ran: fewer launches per outer iteration
+    assert out[0][4] < out[1][4], (out[0][4], out[1][4])
 
 
 def test_dynamic_omega_follows_reference_rule(oracle, o3d):

@@ -129,16 +129,19 @@ def test_coplanar_jet_open_x_steps(oracle, o3d, solver):
     ctx.close()
 
 
-def test_mixing_layer_odd_periodic_steps(oracle, o3d):
+@pytest.mark.parametrize("solver", ["sor", "mg"])
+def test_mixing_layer_odd_periodic_steps(oracle, o3d, solver):
     """The layout of the reference's mixing-layer example (odd point counts
     on the periodic x and z axes, src/../examples/mixing_layer_re3000_les:
     241 x 241 x 81), scaled down: red-black SOR with the seam classes of the
-    odd periodic axes reaches the lexicographic solver's fixed point."""
+    odd periodic axes, and the multigrid with those axes coarsened onto
+    non-nested grids, reach the lexicographic solver's fixed point."""
     nx, ny, nz = 31, 33, 17
     c = oracle.Case(nx, ny, nz, 12.0 * (nx - 1) / nx, 12.0, 4.0 * (nz - 1) / nz, bcx=0, bcy=1, bcz=0,
                     y0=-6.0, z0=-2.0, ratio=0.5, re=3000.0, iles=1, cs=0.17, nscr=1, sc=1.0,
                     dt=0.01, omega=1.7, eps=EPS, kmax=100000)
-    s, ctx, infos = _run_both(oracle, o3d, c, 3, init="ml")
+    kw = {} if solver == "sor" else {"solver": o3d.SOLVER_MG, "kmax": 200}
+    s, ctx, infos = _run_both(oracle, o3d, c, 3, init="ml", **kw)
     _check_fields(s, ctx, c)
     ctx.close()
 
