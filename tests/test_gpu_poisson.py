@@ -125,6 +125,11 @@ NON_NESTED = [
     ((32, 32, 16), (0, 1, 0), (32, 33, 16)),
     ((33, 32, 32), (0, 0, 0), (32, 32, 32)),
     ((31, 32, 17), (0, 1, 0), (32, 33, 16)),
+    # a non-nested transfer between the last two levels: y 19 -> 10 -> 5
+    # (even free-slip at 16 x 10 x 16), z 36 -> 18 -> 9 -> 4 (odd periodic
+    # at 8 x 8 x 9)
+    ((32, 19, 32), (0, 1, 0), (32, 17, 32)),
+    ((32, 32, 36), (0, 0, 0), (32, 32, 32)),
 ]
 
 
