@@ -58,6 +58,29 @@ def test_unet_forward_and_gradients_match_oracle(o3d, dims, per, levels):
     net.close()
 
 
+def test_unet_forward_unsplit_matches_oracle(o3d):
+    """The guess grid of a 256^3 run (32^3): its level-0 convolutions fill
+    the GPU without splitting the (tap, channel) reduction, so they take the
+    fused-epilogue path that the small grids above do not reach; the output
+    agrees with the BF16 oracle as on the small grids."""
+    torch = pytest.importorskip("torch")
+    from oracle import unet_oracle as U
+    dims, per, levels = (32, 32, 32), (1, 1, 1), 2
+    nvox = dims[0] * dims[1] * dims[2]
+    net = o3d.UNet(dims, periodic=per, base=16, levels=levels, in_channels=2, seed=11)
+    p = net.get_params()
+    rng = np.random.default_rng(5)
+    inp = rng.standard_normal((2, nvox)).astype(np.float32)
+    d_in = _dev(inp.reshape(-1))
+    d_out = torch.zeros(nvox, dtype=torch.float32, device="cuda")
+    net.forward(d_in.data_ptr(), d_out.data_ptr())
+    torch.cuda.synchronize()
+    out_ref, _, _ = U.forward_backward(p.astype(np.float64), inp.astype(np.float64), np.zeros(nvox), dims, per, 16,
+                                       levels)
+    assert rel_err(d_out.cpu().numpy(), out_ref) < 1e-2
+    net.close()
+
+
 def test_unet_training_reduces_loss(o3d):
     """A few hundred Adam steps on a fixed smooth sample fit it."""
     torch = pytest.importorskip("torch")
