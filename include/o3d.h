@@ -125,7 +125,8 @@ typedef struct o3d_params {
                              results in all three; 1 and 2 are for comparison and tests) */
 } o3d_params;
 
-/* Fills *p with the defaults of the reference's namelists (periodic 64^3). */
+/* Fills *p with the defaults of the reference's namelists (periodic 64^3);
+ * the namelists are read by parameters(), src/initialization.f90:114-126. */
 O3D_API void o3d_default_params(o3d_params *p);
 
 /* What one time step reports (the values the reference prints each step). */
@@ -159,7 +160,9 @@ O3D_API long long o3d_launch_count(const o3d_ctx *ctx);
 /* The context's CUDA stream (a cudaStream_t) for callers that enqueue work. */
 O3D_API void *o3d_stream(o3d_ctx *ctx);
 
-/* Field transfer, host buffers of nx*ny*nz doubles. */
+/* Field transfer, host buffers of nx*ny*nz doubles: the module arrays that
+ * src/initialization.f90:158-160 allocates (ux, uy, uz, pp, ...) live on the
+ * device instead, and the driver copies them only at output. */
 O3D_API int o3d_upload(o3d_ctx *ctx, int field, const double *host);
 O3D_API int o3d_download(o3d_ctx *ctx, int field, double *host);
 
@@ -326,7 +329,8 @@ O3D_API int o3d_divergence_stats_noalloc(const double *d_fx, const double *d_fy,
                                          double dz, int bcx, int bcy, int bcz, int odd, void *stream,
                                          double stats[6]);
 
-/* Red-black SOR sweep(s) alone on device buffers: for tests of the kernel. */
+/* Red-black SOR sweep(s) alone on device buffers: for tests of the kernel
+ * that replaces the lexicographic sweeps of src/poisson.f90:6-130. */
 O3D_API int o3d_rbsor_sweeps_dev(o3d_ctx *ctx, double *d_pp, const double *d_rhs, double omega,
                          int nsweeps, double *dmax_last);
 
