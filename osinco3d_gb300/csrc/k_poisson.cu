@@ -1323,12 +1323,20 @@ template <class R>
 void launch_rhs_wmean(const R* rhs, const Grid& g, double* part, SolveCtrl* ctrl, cudaStream_t s,
                       long long* nl) {
   const dim3 grid((g.nx + 31) / 32, (g.ny + 7) / 8, (g.nz + WM_KC - 1) / WM_KC);
+  launch_pdl(k_wmean_part<R>, grid, dim3(32, 8), 0, s, rhs, g, part);
+  *nl += 1;
+  launch_rhs_wmean_final(part, (long long)grid.x * grid.y * grid.z, g, ctrl, s, nl);
+}
+
+// the mean from per-block weighted sums already in part (nblk records, e.g.
+// written by the divergence kernel that produced the rhs)
+void launch_rhs_wmean_final(const double* part, long long nblk, const Grid& g, SolveCtrl* ctrl, cudaStream_t s,
+                            long long* nl) {
   // sum of the weights: per axis n (periodic) or n - 1 (mirror: halves at both ends)
   double wsum = 1.0;
   for (int a = 0; a < 3; ++a) wsum *= g.bc[a] == AX_MIRROR ? (double)(g.len(a) - 1) : (double)g.len(a);
-  launch_pdl(k_wmean_part<R>, grid, dim3(32, 8), 0, s, rhs, g, part);
-  launch_pdl(k_wmean_final, 1, 1024, 0, s, part, (long long)grid.x * grid.y * grid.z, wsum, ctrl);
-  *nl += 2;
+  launch_pdl(k_wmean_final, 1, 1024, 0, s, part, nblk, wsum, ctrl);
+  *nl += 1;
 }
 
 template <class R>

@@ -337,7 +337,7 @@ template <class T, class O, int TX, int TY, bool ZON, bool XO>
 __global__ void __launch_bounds__(TX * TY) k_div25(const T* __restrict__ fx, const T* __restrict__ fy,
                                                    const T* __restrict__ fz, O* __restrict__ out, Grid g,
                                                    Coef3<T> cf, int odd, T dt, int divide, StatPart* part,
-                                                   int kc) {
+                                                   int kc, double* wpart, int wmask) {
   pdl_enter();
   using Ring = DivRing<T, TX, TY>;
   constexpr int SW = Ring::SW;
@@ -406,6 +406,13 @@ __global__ void __launch_bounds__(TX * TY) k_div25(const T* __restrict__ fx, con
   // T = float (exact to ~2^-48 over the chunk), widened once at the end
   double sum = 0.0;
   float sum_hi = 0.f, sum_lo = 0.f;
+  // with wpart (T = float): the trapezoid-weighted sum of the values written,
+  // weight 1/2 at each end of an axis whose bit is set in wmask (the mirror
+  // axes of the pressure grid), in a TwoSum pair; the weights are powers of
+  // two, so each weighted term is exact
+  float wsum_hi = 0.f, wsum_lo = 0.f;
+  const float wxy = (((wmask & 1) && (i == 0 || i == g.nx - 1)) ? 0.5f : 1.f) *
+                    (((wmask & 2) && (j == 0 || j == g.ny - 1)) ? 0.5f : 1.f);
   for (int lb = 0; lb < np; lb += ZQ) {
 #pragma unroll
     for (int u = 0; u < ZQ; ++u) {
@@ -429,9 +436,18 @@ __global__ void __launch_bounds__(TX * TY) k_div25(const T* __restrict__ fx, con
         const T div = ddx + ddy + ddz;
         if (valid) {
           const long long p = out0 + sz * (k0 + lp);
-          if (out) out[p] = to_t<O>(divide ? div / dt : div);
-          if constexpr (sizeof(T) == 4) two_sum_acc(sum_hi, sum_lo, (float)div);
-          else sum += (double)div;
+          const T ov = divide ? div / dt : div;
+          if (out) out[p] = to_t<O>(ov);
+          if constexpr (sizeof(T) == 4) {
+            two_sum_acc(sum_hi, sum_lo, (float)div);
+            if (wpart) {
+              const int k = k0 + lp;
+              const float wz = ((wmask & 4) && (k == 0 || k == g.nz - 1)) ? 0.5f : 1.f;
+              two_sum_acc(wsum_hi, wsum_lo, (wxy * wz) * (float)ov);
+            }
+          } else {
+            sum += (double)div;
+          }
           if (div < mn) mn = div;
           if (div > mx) { mx = div; imx = p; }  // k ascends: the first max of the column is kept
         }
@@ -443,6 +459,11 @@ __global__ void __launch_bounds__(TX * TY) k_div25(const T* __restrict__ fx, con
   if (part) {
     if (!(mx >= mn)) { mn = (T)INFINITY; mx = (T)-INFINITY; imx = 0x7fffffffffffffffll; }
     block_stat_t<T>(mn, mx, sum, imx, part, block_linear_id());
+  }
+  if (wpart) {
+    double r[1] = {to_t<double>(wsum_hi) + to_t<double>(wsum_lo)};
+    const int ops[1] = {RED_SUM};
+    block_reduce_store<1>(r, ops, wpart, block_linear_id());
   }
 }
 
@@ -613,23 +634,23 @@ void launch_predict(const PredArgs<T>& a, cudaStream_t s) {
 
 template <class T, class O, bool ZON, bool XO>
 static void div_launch(const T* fx, const T* fy, const T* fz, O* out, const Grid& g, const Coef3<T>& cf, int odd,
-                       T dt, int divide, StatPart* part, cudaStream_t s) {
+                       T dt, int divide, StatPart* part, cudaStream_t s, double* wpart, int wmask) {
   constexpr size_t bytes = sizeof(DivRing<T, TX25, TY25>);
   static const bool attr = (allow_smem(k_div25<T, O, TX25, TY25, ZON, XO>, bytes), true);
   (void)attr;
   launch_pdl(k_div25<T, O, TX25, TY25, ZON, XO>, grid25(g), dim3(TX25, TY25), bytes, s, fx, fy, fz, out, g, cf, odd,
-             dt, divide, part, KC25);
+             dt, divide, part, KC25, wpart, wmask);
 }
 template <class T, class O>
 void launch_div(const T* fx, const T* fy, const T* fz, O* out, const Grid& g, const Coef3<T>& cf,
-                int odd, T dt, int divide, StatPart* part, cudaStream_t s) {
+                int odd, T dt, int divide, StatPart* part, cudaStream_t s, double* wpart, int wmask) {
   const bool zon = g.bc[2] != AX_ZERO;
   if (g.bc[0] == AX_OPEN) {
-    if (zon) div_launch<T, O, true, true>(fx, fy, fz, out, g, cf, odd, dt, divide, part, s);
-    else div_launch<T, O, false, true>(fx, fy, fz, out, g, cf, odd, dt, divide, part, s);
+    if (zon) div_launch<T, O, true, true>(fx, fy, fz, out, g, cf, odd, dt, divide, part, s, wpart, wmask);
+    else div_launch<T, O, false, true>(fx, fy, fz, out, g, cf, odd, dt, divide, part, s, wpart, wmask);
   } else {
-    if (zon) div_launch<T, O, true, false>(fx, fy, fz, out, g, cf, odd, dt, divide, part, s);
-    else div_launch<T, O, false, false>(fx, fy, fz, out, g, cf, odd, dt, divide, part, s);
+    if (zon) div_launch<T, O, true, false>(fx, fy, fz, out, g, cf, odd, dt, divide, part, s, wpart, wmask);
+    else div_launch<T, O, false, false>(fx, fy, fz, out, g, cf, odd, dt, divide, part, s, wpart, wmask);
   }
 }
 
@@ -655,11 +676,12 @@ void launch_correct(const CorrArgs<T, S>& a, cudaStream_t s) {
 template void launch_predict<double>(const PredArgs<double>&, cudaStream_t);
 template void launch_predict<float>(const PredArgs<float>&, cudaStream_t);
 template void launch_div<double, double>(const double*, const double*, const double*, double*, const Grid&,
-                                         const Coef3<double>&, int, double, int, StatPart*, cudaStream_t);
+                                         const Coef3<double>&, int, double, int, StatPart*, cudaStream_t, double*,
+                                         int);
 template void launch_div<float, float>(const float*, const float*, const float*, float*, const Grid&,
-                                       const Coef3<float>&, int, float, int, StatPart*, cudaStream_t);
+                                       const Coef3<float>&, int, float, int, StatPart*, cudaStream_t, double*, int);
 template void launch_div<float, double>(const float*, const float*, const float*, double*, const Grid&,
-                                        const Coef3<float>&, int, float, int, StatPart*, cudaStream_t);
+                                        const Coef3<float>&, int, float, int, StatPart*, cudaStream_t, double*, int);
 template void launch_correct<double, double>(const CorrArgs<double, double>&, cudaStream_t);
 template void launch_correct<float, double>(const CorrArgs<float, double>&, cudaStream_t);
 

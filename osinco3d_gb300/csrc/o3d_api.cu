@@ -103,6 +103,8 @@ struct o3d_ctx {
 
   double* part;      // per-block reduction records
   StatPart* spart;
+  double* wpart;     // weighted rhs sums per divergence block (mixed method)
+  int rhs_wsum;      // wpart holds the sums of the current rhs
   DevDiag* diag;
   DevDiag* diag_h;   // pinned
   SolveCtrl* ctrl;
@@ -271,8 +273,15 @@ int rhs_t(o3d_ctx* c) {
   // the Poisson rhs is FP64 in both methods (the mixed method's FP32
   // divergence widened exactly), so that removing its weighted mean leaves a
   // compatible problem to FP64 rounding
+  // the mixed method's kernel also sums the rhs with the trapezoid weights of
+  // the pressure grid, for the compatibility mean of the solve
+  const bool fuse_wsum = sizeof(T) == 4;
+  int wmask = 0;
+  for (int a = 0; a < 3; ++a)
+    if (c->gp.bc[a] == AX_MIRROR) wmask |= 1 << a;
   launch_div<T, double>((const T*)c->up[0], (const T*)c->up[1], (const T*)c->up[2], (double*)c->rhs, c->g, cf,
-                        1, (T)c->P.dt, 1, c->spart, c->s);
+                        1, (T)c->P.dt, 1, c->spart, c->s, fuse_wsum ? c->wpart : nullptr, wmask);
+  c->rhs_wsum = fuse_wsum ? 1 : 0;
   launch_finalize_stats(c->spart, z_blocks(c->g), c->g, c->diag->divp, c->s);
   c->launches += 2;
   CKL();
@@ -626,7 +635,8 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
     // the weighted mean of the rhs (compatibility of the singular problem):
     // removed in place, except for the mixed multigrid solve, whose FP64
     // residual kernel subtracts it as it reads the rhs
-    launch_rhs_wmean<double>((const double*)c->rhs, c->gp, c->part, c->ctrl, c->s, &c->launches);
+    if (c->rhs_wsum) launch_rhs_wmean_final(c->wpart, z_blocks(c->g), c->gp, c->ctrl, c->s, &c->launches);
+    else launch_rhs_wmean<double>((const double*)c->rhs, c->gp, c->part, c->ctrl, c->s, &c->launches);
     if (!(c->mixed && use_mg)) {
       launch_rhs_shift<double>((double*)c->rhs, c->g.n, c->ctrl, c->s);
       c->launches++;
@@ -853,6 +863,7 @@ int o3d_create(const o3d_params* p, o3d_ctx** out) {
   const long long nb = pt_blocks(c->g) + 1;
   st = st ? st : dalloc(c->s, (void**)&c->part, (size_t)nb * 16 * sizeof(double));
   st = st ? st : dalloc(c->s, (void**)&c->spart, (size_t)nb * sizeof(StatPart));
+  st = st ? st : dalloc(c->s, (void**)&c->wpart, (size_t)z_blocks(c->g) * sizeof(double));
   st = st ? st : dalloc(c->s, (void**)&c->diag, sizeof(DevDiag));
   st = st ? st : dalloc(c->s, (void**)&c->ctrl, sizeof(SolveCtrl));
   if (!st && cudaMallocHost((void**)&c->diag_h, sizeof(DevDiag)) != cudaSuccess) st = O3D_ERR_NOMEM;
@@ -882,7 +893,7 @@ int o3d_destroy(o3d_ctx* c) {
   for (int q = 0; q < 3; ++q) cudaFree(c->uold[q]);
   for (int q = 0; q < 4; ++q) cudaFree(c->vout[q]);
   cudaFree(c->rscratch);
-  cudaFree(c->part); cudaFree(c->spart); cudaFree(c->diag); cudaFree(c->ctrl);
+  cudaFree(c->part); cudaFree(c->spart); cudaFree(c->wpart); cudaFree(c->diag); cudaFree(c->ctrl);
   if (c->diag_h) cudaFreeHost(c->diag_h);
   if (c->ctrl_h) cudaFreeHost(c->ctrl_h);
   for (auto& L : c->mg) { cudaFree(L.e); cudaFree(L.r); cudaFree(L.t); }
@@ -905,6 +916,7 @@ int o3d_upload(o3d_ctx* c, int field, const double* host) {
   bool is_pp;
   void* d = field_ptr(c, field, &is_pp);
   if (!d) { errf("field %d not allocated or unknown", field); return O3D_ERR_BADARG; }
+  if (field == O3D_FIELD_RHS) c->rhs_wsum = 0;
   if (is_pp) {
     CK(cudaMemcpyAsync(d, host, (size_t)c->g.n * 8, cudaMemcpyHostToDevice, c->s));
   } else {
@@ -1026,6 +1038,7 @@ int o3d_poisson_solve(o3d_ctx* c, double* pp, const double* rhs, double* omega, 
   if (!c || !pp || !rhs || !omega) return O3D_ERR_BADARG;
   CK(cudaMemcpyAsync(c->pp, pp, (size_t)c->g.n * 8, cudaMemcpyHostToDevice, c->s));
   CK(cudaMemcpyAsync(c->rhs, rhs, (size_t)c->g.n * 8, cudaMemcpyHostToDevice, c->s));
+  c->rhs_wsum = 0;  // a caller's rhs: its mean takes the separate pass
   int st = O3D_OK;
   o3d_step_info info;
   memset(&info, 0, sizeof info);

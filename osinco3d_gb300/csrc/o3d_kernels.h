@@ -71,7 +71,8 @@ void launch_nu_t(const T* ux, const T* uy, const T* uz, T* nu, const Grid& g, co
                  T csd2, cudaStream_t s);
 template <class T, class O>
 void launch_div(const T* fx, const T* fy, const T* fz, O* out, const Grid& g, const Coef3<T>& cf,
-                int odd, T dt, int divide, StatPart* part, cudaStream_t s);
+                int odd, T dt, int divide, StatPart* part, cudaStream_t s, double* wpart = nullptr,
+                int wmask = 0);
 template <class T, class P>
 void launch_correct(const CorrArgs<T, P>& a, cudaStream_t s);
 template <class T>
@@ -185,6 +186,8 @@ void launch_level_kernel(int which, double* p, const R* rhs, const MGLevel& L, S
 template <class R>
 void launch_rhs_wmean(const R* rhs, const Grid& g, double* part, SolveCtrl* ctrl, cudaStream_t s,
                       long long* nl);
+void launch_rhs_wmean_final(const double* part, long long nblk, const Grid& g, SolveCtrl* ctrl, cudaStream_t s,
+                            long long* nl);
 template <class R>
 void launch_residual_inf(const double* p, const R* rhs, const Grid& g, const PoiCoef<double>& c, SolveCtrl* ctrl,
                          bool shift,
