@@ -635,8 +635,11 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
     // the weighted mean of the rhs (compatibility of the singular problem):
     // removed in place, except for the mixed multigrid solve, whose FP64
     // residual kernel subtracts it as it reads the rhs
+    // (from the divergence kernel's sums once per rhs: a later solve of the
+    // same, possibly shifted, rhs sums it again)
     if (c->rhs_wsum) launch_rhs_wmean_final(c->wpart, z_blocks(c->g), c->gp, c->ctrl, c->s, &c->launches);
     else launch_rhs_wmean<double>((const double*)c->rhs, c->gp, c->part, c->ctrl, c->s, &c->launches);
+    c->rhs_wsum = 0;
     if (!(c->mixed && use_mg)) {
       launch_rhs_shift<double>((double*)c->rhs, c->g.n, c->ctrl, c->s);
       c->launches++;
