@@ -319,11 +319,15 @@ O3D_API int o3d_check_conversions(long long n, unsigned long long seed, long lon
  * node spacings, bc* the O3D_BC_* code of each axis, odd selects the "i"
  * closures; the work runs on `stream` (a cudaStream_t, NULL = default) and the
  * call returns after stats = min, max, mean, imax, jmax, kmax (1-based) are in
- * host memory.  Scratch: a fixed 512 KiB array in device memory, shared by
- * every call: grids needing more than 16384 reduction blocks (beyond 512^3 or
- * 768 x 384 x 384 points) are rejected with O3D_ERR_BADARG, and calls that
- * overlap on the GPU race.  The first call on each device looks up the
- * array's device address; make that first call before any stream capture. */
+ * host memory.  Scratch: a fixed 768 KiB array in device memory, shared by
+ * every call, of O3D_NOALLOC_MAX_RECORDS block records.  A grid needs
+ * ceil(nx/32) * ceil(ny/8) * ceil(nz/28) of them (19456 for 512^3, 16128 for
+ * 768 x 384 x 384); a grid needing more is rejected with O3D_ERR_BADARG before
+ * any device work.  Calls that overlap on the GPU race on the array.  The
+ * first call on each device looks up the array's device address.  Every call
+ * synchronizes `stream` and copies the statistics into pageable host memory,
+ * so it must not be called while `stream` is being captured into a graph. */
+#define O3D_NOALLOC_MAX_RECORDS 24576
 O3D_API int o3d_divergence_stats_noalloc(const double *d_fx, const double *d_fy, const double *d_fz,
                                          double *d_div, int nx, int ny, int nz, double dx, double dy,
                                          double dz, int bcx, int bcy, int bcz, int odd, void *stream,

@@ -30,6 +30,7 @@
 //                group(lp + 3 + P) into the stage of plane lp - 1 (free:
 //                every thread passed the barrier after computing it), take
 //                the queue head from plane lp + 3, compute plane lp.
+#include <atomic>
 #include "o3d_internal.cuh"
 #include "o3d_kernels.h"
 
@@ -110,9 +111,19 @@ __device__ __forceinline__ Halo<TX, TY> halo_cell(const Grid& g, int i0, int j0,
   return h;
 }
 
+// Raises a kernel's dynamic shared-memory limit above 48 KB.  The attribute
+// belongs to the current device, so it is applied once per device (one flag
+// per device and kernel instantiation); devices beyond the table get it on
+// every launch.
+constexpr int SMEM_MAX_DEVICES = 64;
 template <class K>
-static void allow_smem(K* kernel, size_t bytes) {
-  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+static void allow_smem(K* kernel, size_t bytes, std::atomic<bool>* done) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) dev = -1;
+  if (dev >= 0 && dev < SMEM_MAX_DEVICES && done[dev].load(std::memory_order_acquire)) return;
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess &&
+      dev >= 0 && dev < SMEM_MAX_DEVICES)
+    done[dev].store(true, std::memory_order_release);
 }
 
 constexpr int TX25 = 32, TY25 = 8, KC25 = 28;  // planes per block: a multiple of the unroll (7)
@@ -610,8 +621,8 @@ __global__ void __launch_bounds__(TX * TY) k_correct25(CorrArgs<T, S> A, int kc)
 template <class T, bool LES, bool ZON, bool XO>
 static void predict_launch(const PredArgs<T>& a, cudaStream_t s) {
   constexpr size_t bytes = sizeof(PredRing<T, TX25, TY25>);
-  static const bool attr = (allow_smem(k_predict25<T, TX25, TY25, LES, ZON, XO>, bytes), true);
-  (void)attr;
+  static std::atomic<bool> attr[SMEM_MAX_DEVICES];
+  allow_smem(k_predict25<T, TX25, TY25, LES, ZON, XO>, bytes, attr);
   launch_pdl(k_predict25<T, TX25, TY25, LES, ZON, XO>, grid25(a.g), dim3(TX25, TY25), bytes, s, a, KC25);
 }
 template <class T, bool XO>
@@ -636,8 +647,8 @@ template <class T, class O, bool ZON, bool XO>
 static void div_launch(const T* fx, const T* fy, const T* fz, O* out, const Grid& g, const Coef3<T>& cf, int odd,
                        T dt, int divide, StatPart* part, cudaStream_t s, double* wpart, int wmask) {
   constexpr size_t bytes = sizeof(DivRing<T, TX25, TY25>);
-  static const bool attr = (allow_smem(k_div25<T, O, TX25, TY25, ZON, XO>, bytes), true);
-  (void)attr;
+  static std::atomic<bool> attr[SMEM_MAX_DEVICES];
+  allow_smem(k_div25<T, O, TX25, TY25, ZON, XO>, bytes, attr);
   launch_pdl(k_div25<T, O, TX25, TY25, ZON, XO>, grid25(g), dim3(TX25, TY25), bytes, s, fx, fy, fz, out, g, cf, odd,
              dt, divide, part, KC25, wpart, wmask);
 }
@@ -657,8 +668,8 @@ void launch_div(const T* fx, const T* fy, const T* fz, O* out, const Grid& g, co
 template <class T, class S, bool ZON, bool XO>
 static void correct_launch(const CorrArgs<T, S>& a, cudaStream_t s) {
   constexpr size_t bytes = sizeof(CorrRing<T, S, TX25, TY25>);
-  static const bool attr = (allow_smem(k_correct25<T, S, TX25, TY25, ZON, XO>, bytes), true);
-  (void)attr;
+  static std::atomic<bool> attr[SMEM_MAX_DEVICES];
+  allow_smem(k_correct25<T, S, TX25, TY25, ZON, XO>, bytes, attr);
   launch_pdl(k_correct25<T, S, TX25, TY25, ZON, XO>, grid25(a.g), dim3(TX25, TY25), bytes, s, a, KC25);
 }
 template <class T, class S>

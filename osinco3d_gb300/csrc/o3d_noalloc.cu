@@ -16,11 +16,15 @@
 
 namespace o3d {
 
-// Most thread blocks the divergence kernel may use: one block per 32 x 8
-// columns of 32 planes, so 16384 blocks cover 512^3 or 768 x 384 x 384.
-constexpr long long NOALLOC_MAX_BLOCKS = 16384;
+// Most thread blocks the divergence kernel may use.  The kernel tiles the
+// grid into columns of 32 x 8 points that march over 28 planes each
+// (z_blocks), so a grid needs ceil(nx/32) * ceil(ny/8) * ceil(nz/28) block
+// records: 16 * 64 * 19 = 19456 for 512^3, 24 * 48 * 14 = 16128 for
+// 768 x 384 x 384.  Both fit.
+constexpr long long NOALLOC_MAX_BLOCKS = O3D_NOALLOC_MAX_RECORDS;
+static_assert(NOALLOC_MAX_BLOCKS >= 19456, "the scratch must serve a 512^3 grid");
 
-// Scratch of the entry point (512 KiB of block records plus the six
+// Scratch of the entry point (768 KiB of 32-byte block records plus the six
 // finalized statistics).  Every device that loads the library holds it until
 // the process exits.  Each call writes every record it reads, so nothing has
 // to start at zero; all calls share it, so calls that overlap on the GPU
@@ -106,8 +110,8 @@ extern "C" int o3d_divergence_stats_noalloc(const double* d_fx, const double* d_
   for (int a = 0; a < 3; ++a) g.bc[a] = bcs[a] == O3D_BC_PERIODIC ? AX_PERIODIC : AX_MIRROR;
   const long long blocks = z_blocks(g);
   if (blocks > NOALLOC_MAX_BLOCKS) {
-    set_error("o3d_divergence_stats_noalloc: a %d x %d x %d grid needs %lld reduction records, more than "
-              "the %lld this entry point holds (at most 512^3 or 768 x 384 x 384 points)",
+    set_error("o3d_divergence_stats_noalloc: a %d x %d x %d grid needs %lld reduction records "
+              "(ceil(nx/32) * ceil(ny/8) * ceil(nz/28)), more than the %lld this entry point holds",
               nx, ny, nz, blocks, NOALLOC_MAX_BLOCKS);
     return O3D_ERR_BADARG;
   }

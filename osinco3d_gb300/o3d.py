@@ -537,6 +537,19 @@ def check_conversions(n: int = 1 << 24, seed: int = 1) -> int:
     return bad.value
 
 
+# block records held by the scratch of o3d_divergence_stats_noalloc
+# (O3D_NOALLOC_MAX_RECORDS in include/o3d.h); a grid needs
+# noalloc_records(shape) of them
+NOALLOC_MAX_RECORDS = 24576
+
+
+def noalloc_records(shape) -> int:
+    """Block records o3d_divergence_stats_noalloc needs for a grid: one per
+    32 x 8 column of 28 planes."""
+    nx, ny, nz = shape
+    return -(-nx // 32) * -(-ny // 8) * -(-nz // 28)
+
+
 def divergence_stats_noalloc(d_fx: int, d_fy: int, d_fz: int, d_div: int | None, shape, spacing, bcs,
                              odd: int = 1, stream: int | None = None):
     """o3d_divergence_stats_noalloc on the caller's device buffers (raw device
