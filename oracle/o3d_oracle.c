@@ -787,3 +787,38 @@ double orc_rbsor_sweep(const orc_model *m, double *pp, const double *rhs, double
     }
   return dmax;
 }
+
+/* poisson.f90:52-123's control loop (same tests, same order, same factors
+ * as orc_poisson_sor above) around one red-black sweep per iteration */
+int orc_poisson_rbsor(const orc_model *m, double *pp, const double *rhs,
+                      double *omega_io, double eps, int kmax, int idyn,
+                      int *iters, double *dmax_out, double *omega_trace,
+                      double *dmax_trace) {
+  double factor;
+  if (m->bcx == 0 && m->bcy == 0) factor = 1.05;       /* poisson.f90:35 */
+  else if (m->bcx == 0 && m->bcy == 1) factor = 1.01;  /* poisson.f90:162 */
+  else factor = 1.05;                                  /* poisson.f90:288 */
+  double omega = *omega_io;
+  double dmax_old = 1609.0, dmax = 0.0;
+  int status = ORC_SOR_MAXIT, iter;
+  for (iter = 1; iter <= kmax; ++iter) {
+    dmax = orc_rbsor_sweep(m, pp, rhs, omega);
+    int stop = 0;
+    if (dmax < eps) { status = ORC_SOR_CONVERGED; stop = 1; }
+    else if (fabs(dmax_old - dmax) < eps / 1000.0) { status = ORC_SOR_STAGNATED; stop = 1; }
+    else {
+      if (iter > 1 && idyn == 1) {
+        if (dmax > dmax_old) omega = omega * (2.0 - factor);
+        else if (dmax < 0.1 * dmax_old) omega = fmin(omega * factor, 2.0);
+      }
+      dmax_old = dmax;
+    }
+    if (omega_trace) omega_trace[iter - 1] = omega;
+    if (dmax_trace) dmax_trace[iter - 1] = dmax;
+    if (stop) break;
+  }
+  *iters = iter > kmax ? kmax : iter;
+  *dmax_out = dmax;
+  *omega_io = omega;
+  return status;
+}

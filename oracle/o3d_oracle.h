@@ -127,6 +127,17 @@ void orc_step(const orc_model *m, orc_state *s, int itime, orc_step_info *info);
 double orc_rbsor_sweep(const orc_model *m, double *pp, const double *rhs,
                        double omega);
 
+/* The reference's SOR control loop (poisson.f90:52-123: stop on dmax < eps,
+ * stagnation on |dmax_old - dmax| < eps/1000, dynamic omega with the
+ * variant's factor, kmax) driving orc_rbsor_sweep instead of the
+ * lexicographic sweep: the solve the GPU red-black SOR performs.  If
+ * omega_trace is not NULL, omega_trace[iter-1] and dmax_trace[iter-1] hold
+ * omega and dmax after the control step of each sweep. */
+int orc_poisson_rbsor(const orc_model *m, double *pp, const double *rhs,
+                      double *omega_io, double eps, int kmax, int idyn,
+                      int *iters, double *dmax_out, double *omega_trace,
+                      double *dmax_trace);
+
 #ifdef __cplusplus
 }
 #endif

@@ -82,7 +82,7 @@ def lib(omp: bool = False):
             build()
         L = C.CDLL(path)
         L.orc_rbsor_sweep.restype = C.c_double
-        for fn in ("orc_poisson_sor", "orc_correct_pressure", "orc_correct_velocity"):
+        for fn in ("orc_poisson_sor", "orc_poisson_rbsor", "orc_correct_pressure", "orc_correct_velocity"):
             getattr(L, fn).restype = C.c_int
         _LIBS[name] = L
     return _LIBS[name]
@@ -286,6 +286,22 @@ def poisson_sor(case: Case, pp: np.ndarray, rhs: np.ndarray, omega: float, eps: 
     st = lib().orc_poisson_sor(C.byref(m), ptr(pp), ptr(rhs), C.byref(om), C.c_double(eps),
                                C.c_int(kmax), C.c_int(idyn), C.byref(it), C.byref(dm))
     return st, it.value, dm.value, om.value
+
+
+def poisson_rbsor(case: Case, pp: np.ndarray, rhs: np.ndarray, omega: float, eps: float, kmax: int,
+                  idyn: int = 0):
+    """The reference's SOR control loop around red-black sweeps; returns
+    (status, iters, dmax, omega, omega after each sweep, dmax of each sweep)."""
+    m = case.model()
+    om = C.c_double(omega)
+    it = C.c_int(0)
+    dm = C.c_double(0)
+    otr = np.zeros(kmax)
+    dtr = np.zeros(kmax)
+    st = lib().orc_poisson_rbsor(C.byref(m), ptr(pp), ptr(rhs), C.byref(om), C.c_double(eps), C.c_int(kmax),
+                                 C.c_int(idyn), C.byref(it), C.byref(dm), otr.ctypes.data_as(_dp),
+                                 dtr.ctypes.data_as(_dp))
+    return st, it.value, dm.value, om.value, otr[:it.value], dtr[:it.value]
 
 
 def rbsor_sweep(case: Case, pp: np.ndarray, rhs: np.ndarray, omega: float) -> float:

@@ -219,16 +219,52 @@ def test_fused_level_kernels_match_unfused(oracle, o3d, shape, bcs, kw, mode):
     assert out[0][4] < out[1][4], (out[0][4], out[1][4])
 
 
-def test_dynamic_omega_follows_reference_rule(oracle, o3d):
-    """idyn = 1: same omega trajectory rule (src/poisson.f90:115-121); the final
-    omega of a long solve stays within the rule's bounds."""
-    c = _case(oracle, (32, 32, 32), (0, 0, 0))
-    rhs = _compatible_rhs(c, 11)
+OMEGA_CASES = [
+    # shape, boundaries (solver variant and its factor), initial omega, rhs:
+    # 0000 and 111111 use factor 1.05 (src/poisson.f90:35,288), 0011 1.01
+    # (:162); the constant rhs on the all-mirror grid has no solution and
+    # ends on the stagnation test
+    ((32, 32, 32), (0, 0, 0), 1.8, "smooth"),
+    ((32, 33, 16), (0, 1, 0), 1.8, "smooth"),
+    ((33, 33, 33), (1, 1, 1), 1.8, "smooth"),
+    ((32, 32, 32), (0, 0, 0), 1.5, "smooth"),
+    ((17, 17, 17), (1, 1, 1), 1.9, "constant"),
+]
+
+
+@pytest.mark.parametrize("shape,bcs,om0,kind", OMEGA_CASES)
+def test_dynamic_omega_trajectory_and_exit_match_oracle(oracle, o3d, shape, bcs, om0, kind):
+    """idyn = 1: the GPU red-black SOR applies src/poisson.f90:110-122 after
+    every sweep.  The oracle drives its red-black sweep with the same rule
+    (orc_poisson_rbsor); omega after k sweeps (a solve capped at kmax = k),
+    the exit iteration, the exit status and the final omega are identical,
+    and the last update norm agrees to rounding."""
+    c = _case(oracle, shape, bcs)
+    rhs = _compatible_rhs(c, 11) if kind == "smooth" else np.asfortranarray(np.ones(c.shape))
+    eps = 1e-8
+    st_ref, it_ref, dm_ref, om_ref, otr, dtr = oracle.poisson_rbsor(c, oracle.field3(c.shape), rhs, om0, eps,
+                                                                    20000, 1)
+    want = oracle.SOR_CONVERGED if kind == "smooth" else oracle.SOR_STAGNATED
+    assert st_ref == want
+    assert np.count_nonzero(np.diff(otr)) >= 1  # the rule changed omega at least once
+    code = {oracle.SOR_CONVERGED: o3d.OK, oracle.SOR_STAGNATED: o3d.WARN_STAGNATION}[st_ref]
     with o3d.Context(params_of(o3d, c)) as ctx:
         got = ctx.field()
-        st, it, dm, om = ctx.poisson_solve(got, rhs, 1.5, 1e-8, 5000, 1)
-    assert 0.0 < om <= 2.0
-    assert st in (o3d.OK, o3d.WARN_STAGNATION)
+        st, it, dm, om = ctx.poisson_solve(got, rhs, om0, eps, 20000, 1)
+        assert (st, it) == (code, it_ref)
+        assert om == om_ref  # bit-identical: same factors applied in the same order
+        assert dm == pytest.approx(dm_ref, rel=1e-6)
+        # the trajectory: every sweep where omega changed, its neighbours, and
+        # points across the 16-sweep batches
+        ks = {1, 2, 3, 15, 16, 17, 31, 32, 33, it_ref - 1}
+        for q in np.flatnonzero(np.diff(otr)):
+            ks |= {int(q) + 1, int(q) + 2, int(q) + 3}
+        for k in sorted(x for x in ks if 1 <= x < it_ref):
+            got = ctx.field()
+            st_k, it_k, dm_k, om_k = ctx.poisson_solve(got, rhs, om0, eps, k, 1)
+            assert (st_k, it_k) == (o3d.WARN_POISSON_MAXIT, k), k
+            assert om_k == otr[k - 1], (k, om_k, otr[k - 1])
+            assert dm_k == pytest.approx(dtr[k - 1], rel=1e-6), k
 
 
 def test_incompatible_rhs_stagnates_like_reference(oracle, o3d):
