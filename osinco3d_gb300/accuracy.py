@@ -9,7 +9,9 @@ plain FP64 method on the same run, field by field.
 Both runs start from the same host fields and solve every Poisson problem to
 the same eps with the multigrid solver; one JSON line reports, per field,
 max|mixed - fp64| / max|fp64| and the rms ratio, with each run's ms per step
-and V-cycles per step.
+and V-cycles per step.  For the pressure (mean removed) it also reports the
+absolute error, the largest pressure fluctuation and the error relative to
+the dynamic pressure max |u|^2.
 """
 from __future__ import annotations
 
@@ -48,6 +50,13 @@ def compare(params64, params_mixed, fields, names, steps: int) -> dict:
         d = a - b
         errs[nm] = {"max_rel": float(np.abs(d).max() / max(np.abs(b).max(), 1e-300)),
                     "rms_rel": float(np.sqrt((d * d).mean()) / max(np.sqrt((b * b).mean()), 1e-300))}
+        if nm == "pp":
+            # the pressure's scales: its own fluctuation, and the dynamic
+            # pressure max |u|^2 of the run
+            u2 = max(float(np.abs(ref[c]).max()) for c in ("ux", "uy", "uz")) ** 2
+            errs[nm]["max_abs"] = float(np.abs(d).max())
+            errs[nm]["p_fluct_max"] = float(np.abs(b).max())
+            errs[nm]["max_rel_u2"] = float(np.abs(d).max() / u2)
     return {"steps": steps, "errors": errs, "fp64": {"ms_per_step": ms64, "vcycles_per_step": c64},
             "mixed": {"ms_per_step": msm, "vcycles_per_step": cm}}
 
