@@ -216,6 +216,21 @@ O3D_API int o3d_statistics_calc(o3d_ctx *ctx, double t, double out[17]);
  * (src/differential_operators.f90:40-108) of the current velocity into host
  * arrays of nx*ny*nz doubles; any pointer may be NULL. */
 O3D_API int o3d_vorticity(o3d_ctx *ctx, double *rotx, double *roty, double *rotz, double *q_criterion);
+
+/* write_all_data(...) + write_xdmf(...), src/visualization.f90:242-341, as
+ * called every nfre steps by src/osinco3d_main.f90:147-150: writes
+ * <dir>/ux_<num>.bin, uy, uz, pp, vort (|curl u|), qcrit, and phi (nscr = 1)
+ * and nu_t (iles = 1) -- raw FP64 column-major nx*ny*nz arrays, no record
+ * markers -- and <dir>/output_<num>.xdmf describing them, in the reference's
+ * layouts.  Asynchronous: the call snapshots the fields on the device and
+ * returns; the device->host copies run on a separate stream and a host
+ * thread writes the files while later steps run.  The next call,
+ * o3d_output_wait or o3d_destroy waits for it.  The driver keeps num
+ * (write_xdmf's counter) and time. */
+O3D_API int o3d_write_output(o3d_ctx *ctx, const char *dir, int num, double time);
+/* Waits until the files of the last o3d_write_output are written; returns
+ * O3D_ERR_BADARG (with o3d_last_error) if a file could not be written. */
+O3D_API int o3d_output_wait(o3d_ctx *ctx);
 /* old_values (src/utils.f90:209-218): keep the current velocity on the
  * device for o3d_velocity_residuals. */
 O3D_API int o3d_save_old_velocity(o3d_ctx *ctx);

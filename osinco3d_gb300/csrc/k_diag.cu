@@ -49,6 +49,34 @@ __global__ void __launch_bounds__(256) k_vort(const T* __restrict__ u0, const T*
            gr[0][2] * gr[2][0] - gr[1][2] * gr[2][1];
 }
 
+// The output snapshot of write_all_data (src/visualization.f90:242-274) in
+// one pass: u, v, w widened to FP64, the vorticity magnitude
+// sqrt(rotx^2 + roty^2 + rotz^2) of the curl (src/differential_operators.f90:
+// 63-74, the magnitude formed as write_all_data forms it) and the
+// Q-criterion (:104-105), computed in the field type T
+template <class T>
+__global__ void __launch_bounds__(256) k_out_snapshot(const T* __restrict__ u0, const T* __restrict__ u1,
+                                                      const T* __restrict__ u2, double* __restrict__ ux,
+                                                      double* __restrict__ uy, double* __restrict__ uz,
+                                                      double* __restrict__ vort, double* __restrict__ q, Grid g,
+                                                      Coef3<T> cf) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= g.nx || j >= g.ny) return;
+  const T* u[3] = {u0, u1, u2};
+  T gr[3][3];
+  grad9<T>(u, g, cf, i, j, k, gr);
+  const long long p = (long long)i + g.sy() * j + g.sz() * k;
+  ux[p] = to_t<double>(u0[p]);
+  uy[p] = to_t<double>(u1[p]);
+  uz[p] = to_t<double>(u2[p]);
+  const T rx = gr[2][1] - gr[1][2], ry = gr[0][2] - gr[2][0], rz = gr[1][0] - gr[0][1];
+  vort[p] = to_t<double>((T)sqrt(rx * rx + ry * ry + rz * rz));
+  q[p] = to_t<double>((T)-0.5 * (gr[0][0] * gr[0][0] + gr[1][1] * gr[1][1] + gr[2][2] * gr[2][2]) -
+                      gr[0][1] * gr[1][0] - gr[0][2] * gr[2][0] - gr[1][2] * gr[2][1]);
+}
+
 // per block and component: sum of a^2 and max of a, a = |old - u| / (2 dt)
 // over the interior points; on equal maxima the larger index (the last in
 // the reference's loop order, i fastest) wins
@@ -134,6 +162,17 @@ void launch_vorticity(const T* const u[3], T* rx, T* ry, T* rz, T* q, const Grid
                       cudaStream_t s) {
   k_vort<T><<<dg_grid(g), dim3(32, 8), 0, s>>>(u[0], u[1], u[2], rx, ry, rz, q, g, cf);
 }
+
+template <class T>
+void launch_out_snapshot(const T* const u[3], double* const out[5], const Grid& g, const Coef3<T>& cf,
+                         cudaStream_t s) {
+  k_out_snapshot<T><<<dg_grid(g), dim3(32, 8), 0, s>>>(u[0], u[1], u[2], out[0], out[1], out[2], out[3], out[4], g,
+                                                       cf);
+}
+template void launch_out_snapshot<double>(const double* const*, double* const*, const Grid&, const Coef3<double>&,
+                                          cudaStream_t);
+template void launch_out_snapshot<float>(const float* const*, double* const*, const Grid&, const Coef3<float>&,
+                                         cudaStream_t);
 
 // scratch: 3 * blocks ResPart records, then 3 final records
 template <class T>

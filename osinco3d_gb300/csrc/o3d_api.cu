@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "o3d_internal.cuh"
+#include "o3d_output.h"
 #include "o3d_kernels.h"
 
 using namespace o3d;
@@ -100,6 +101,7 @@ struct o3d_ctx {
   void* uold[3];     // velocity kept by o3d_save_old_velocity (lazy)
   void* vout[4];     // curl and Q-criterion outputs (lazy)
   void* rscratch;    // velocity residual block records (lazy)
+  OutWriter* out;    // asynchronous output writer (lazy)
 
   double* part;      // per-block reduction records
   StatPart* spart;
@@ -882,6 +884,7 @@ int o3d_create(const o3d_params* p, o3d_ctx** out) {
 
 int o3d_destroy(o3d_ctx* c) {
   if (!c) return O3D_OK;
+  out_destroy(c->out);
   if (c->s) cudaStreamSynchronize(c->s);
   for (int q = 0; q < 3; ++q) {
     cudaFree(c->u[q]);
@@ -1465,3 +1468,57 @@ int o3d_time_kernel(o3d_ctx* c, int kernel, int reps, double* ms_per_launch) {
 }
 
 }  // extern "C"
+
+int o3d_write_output(o3d_ctx* c, const char* dir, int num, double time) {
+  if (!c || !dir) return O3D_ERR_BADARG;
+  const char* names[8] = {"ux", "uy", "uz", "pp", "vort", "qcrit", nullptr, nullptr};
+  int nf = 6;
+  if (c->P.nscr == 1) names[nf++] = "phi";
+  if (c->P.iles == 1) names[nf++] = "nu_t";
+  double* snap = nullptr;
+  int st = out_prepare(&c->out, c->g.n, nf, &snap);
+  if (st) return st;
+  const long long n = c->g.n;
+  double* outs[5] = {snap, snap + n, snap + 2 * n, snap + 4 * n, snap + 5 * n};
+  if (c->mixed) {
+    const float* u[3] = {(const float*)c->u[0], (const float*)c->u[1], (const float*)c->u[2]};
+    launch_out_snapshot<float>(u, outs, c->g, cast_coef<float>(c->cf), c->s);
+  } else {
+    const double* u[3] = {(const double*)c->u[0], (const double*)c->u[1], (const double*)c->u[2]};
+    launch_out_snapshot<double>(u, outs, c->g, c->cf, c->s);
+  }
+  c->launches++;
+  CKL();
+  CK(cudaMemcpyAsync(snap + 3 * n, c->pp, (size_t)n * 8, cudaMemcpyDeviceToDevice, c->s));
+  int q = 6;
+  for (void* f : {c->P.nscr == 1 ? c->phi : nullptr, c->P.iles == 1 ? c->nu_t : nullptr}) {
+    if (!f) continue;
+    if (c->mixed) {
+      launch_convert<float, double>((const float*)f, snap + (size_t)q * n, n, c->s);
+      c->launches++;
+      CKL();
+    } else {
+      CK(cudaMemcpyAsync(snap + (size_t)q * n, f, (size_t)n * 8, cudaMemcpyDeviceToDevice, c->s));
+    }
+    ++q;
+  }
+  OutRequest r;
+  r.dir = dir;
+  r.num = num;
+  r.time = time;
+  r.nx = c->g.nx;
+  r.ny = c->g.ny;
+  r.nz = c->g.nz;
+  r.dx = c->dx;
+  r.dy = c->dy;
+  r.dz = c->dz;
+  r.x0 = c->P.x0;
+  r.y0 = c->P.y0;
+  r.z0 = c->P.z0;
+  return out_submit(c->out, r, names, nf, c->s);
+}
+
+int o3d_output_wait(o3d_ctx* c) {
+  if (!c) return O3D_ERR_BADARG;
+  return out_wait(c->out);
+}

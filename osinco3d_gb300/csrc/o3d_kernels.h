@@ -64,6 +64,10 @@ long long z_blocks(const Grid& g);
 template <class T>
 void launch_der(const T* f, T* df, const Grid& g, const AxisCoef<T>& c, int axis, int order,
                 int odd, cudaStream_t s);
+// output snapshot: u, v, w in FP64, |curl u| and Q into out[0..4]
+template <class T>
+void launch_out_snapshot(const T* const u[3], double* const out[5], const Grid& g, const Coef3<T>& cf,
+                         cudaStream_t s);
 template <class T>
 void launch_predict(const PredArgs<T>& a, cudaStream_t s);
 template <class T>

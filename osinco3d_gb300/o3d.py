@@ -125,6 +125,8 @@ def lib(build_if_missing: bool = True):
             "o3d_step_host": (C.c_int, [vp, C.c_int, _dp, _dp, _dp, _dp, C.POINTER(StepInfo)]),
             "o3d_statistics_calc": (C.c_int, [vp, C.c_double, _dp]),
             "o3d_vorticity": (C.c_int, [vp, _dp, _dp, _dp, _dp]),
+            "o3d_write_output": (C.c_int, [vp, C.c_char_p, C.c_int, C.c_double]),
+            "o3d_output_wait": (C.c_int, [vp]),
             "o3d_save_fields": (C.c_int, [vp, C.c_char_p, C.c_double]),
             "o3d_load_fields": (C.c_int, [vp, C.c_char_p, _dp]),
             "o3d_save_history": (C.c_int, [vp, C.c_char_p]),
@@ -401,6 +403,14 @@ class Context:
         out = (C.c_double * 17)()
         self._check(self.L.o3d_statistics_calc(self.h, t, out))
         return np.array(out[:])
+
+    def write_output(self, directory: str, num: int, time: float) -> None:
+        """write_all_data + write_xdmf: the raw FP64 fields and the XDMF file
+        of output `num`, written asynchronously (see output_wait)."""
+        self._check(self.L.o3d_write_output(self.h, os.fsencode(directory), num, time))
+
+    def output_wait(self) -> None:
+        self._check(self.L.o3d_output_wait(self.h))
 
     # -- checkpoint and restart ------------------------------------------------
     def save_fields(self, path: str, time: float) -> None:
