@@ -13,6 +13,7 @@ Adam (o3d_unet_train_step); PyTorch only holds the device buffers.
 from __future__ import annotations
 
 import argparse
+import json
 import math
 import os
 import time
@@ -142,23 +143,29 @@ def inference_ms(net: "o3d.UNet", reps: int = 20) -> float:
 
 
 def compare_guesses(n: int, steps: int, warmup: int, weights: str | None, precision=o3d.PREC_MIXED, re=1600.0,
-                    seed: int = 17):
+                    seed: int = 17, t0: float = 0.0, cycle: dict | None = None, guesses=None, amp: float = 0.02):
     """Poisson V-cycles and time per step on the n^3 Taylor-Green run for the
     zero, previous, extrapolated and (with weights) learned initial guesses,
-    all iterating to eps = 1e-8."""
+    all iterating to eps = 1e-8.  The measured steps start at time t0 (the
+    run gets there first); `cycle` sets mg_pre, mg_post and mg_omega; `amp`
+    is the amplitude of the seeded smooth perturbation of the initial state."""
     results = {}
-    guesses = [("zero", o3d.GUESS_ZERO), ("previous", o3d.GUESS_PREVIOUS), ("extrapolated", o3d.GUESS_EXTRAPOLATED)]
+    all_guesses = [("zero", o3d.GUESS_ZERO), ("previous", o3d.GUESS_PREVIOUS),
+                   ("extrapolated", o3d.GUESS_EXTRAPOLATED)]
     if weights and os.path.exists(weights):
-        guesses.append(("learned", o3d.GUESS_LEARNED))
+        all_guesses.append(("learned", o3d.GUESS_LEARNED))
+    guesses = [gg for gg in all_guesses if guesses is None or gg[0] in guesses]
     for name, g in guesses:
-        p = o3d.tgv_params(n, re=re, precision=precision, solver=o3d.SOLVER_MG, eps=1e-8, kmax=100, guess=g)
+        p = o3d.tgv_params(n, re=re, precision=precision, solver=o3d.SOLVER_MG, eps=1e-8, kmax=100, guess=g,
+                           **(cycle or {}))
+        warmup = max(warmup, int(round(t0 / p.dt)))
         with o3d.Context(p) as ctx:
             net = None
             if g == o3d.GUESS_LEARNED:
                 net = load(weights, ctx.guess_grid())
                 ctx.attach_unet(net)
             ux, uy, uz, pp = o3d.tgv_fields(p)
-            du = _perturbation(ux.shape, seed, 0.02)
+            du = _perturbation(ux.shape, seed, amp)
             for nm, f in zip(("ux", "uy", "uz"), (ux + du[0], uy + du[1], uz + du[2])):
                 ctx.upload(nm, np.asfortranarray(f))
             ctx.upload("pp", pp)
@@ -170,7 +177,7 @@ def compare_guesses(n: int, steps: int, warmup: int, weights: str | None, precis
                     pms.append(info.poisson_ms)
                     sms.append(info.step_ms)
             results[name] = {"vcycles_per_step": float(np.mean(cyc)), "poisson_ms": float(np.mean(pms)),
-                             "step_ms": float(np.mean(sms))}
+                             "step_ms": float(np.mean(sms)), "t_first": (warmup + 1) * p.dt}
             if net:
                 results[name]["inference_ms"] = inference_ms(net)
                 results[name]["grid"] = list(net.dims)
@@ -193,6 +200,12 @@ def main():
     e.add_argument("--n", type=int, default=256)
     e.add_argument("--steps", type=int, default=10)
     e.add_argument("--weights", default=WEIGHTS)
+    e.add_argument("--t0", type=float, default=0.0, help="time at which the measured steps start")
+    e.add_argument("--pre", type=int, default=0)
+    e.add_argument("--post", type=int, default=0)
+    e.add_argument("--omega", type=float, default=0.0)
+    e.add_argument("--amp", type=float, default=0.02, help="initial perturbation amplitude")
+    e.add_argument("--guesses", default="", help="comma-separated subset of zero,previous,extrapolated,learned")
     args = ap.parse_args()
     if args.cmd == "train":
         t0 = time.time()
@@ -204,7 +217,10 @@ def main():
         print(f"training {time.time() - t1:.1f} s, loss {hist[0]:.4e} -> {hist[-1]:.4e}", flush=True)
         save(net, args.out)
     elif args.cmd == "eval":
-        print(compare_guesses(args.n, args.steps, 3, args.weights))
+        cyc = {k: v for k, v in (("mg_pre", args.pre), ("mg_post", args.post), ("mg_omega", args.omega)) if v}
+        sel = [x for x in args.guesses.split(",") if x] or None
+        res = compare_guesses(args.n, args.steps, 3, args.weights, t0=args.t0, cycle=cyc, guesses=sel, amp=args.amp)
+        print(json.dumps({"n": args.n, "t0": args.t0, "cycle": cyc, "amp": args.amp, "guesses": res}))
 
 
 if __name__ == "__main__":
