@@ -267,18 +267,20 @@ def _measure_e2e(o3d, steps: int, warmup: int, world: int, weights=None, **kw) -
 
 # algorithmic bytes per grid point of the hot kernels (float32 storage)
 KERNEL_BYTES = {
-    "predict": (PRED_BYTES_PER_PT, "k_predict25<float>"),
+    "predict": (PRED_BYTES_PER_PT, "k_predict25v<float> (two x-adjacent points per thread)"),
     # read r, write e and the coarse rhs (1/8)
     "mg_down": (4 + 4 + 0.5, "k_mg_down<2,zero> (pre-smoothing + residual + restriction, finest level)"),
     # read e, r, p and the coarse correction (1/8), write e and p
     "mg_up": (4 + 4 + 8 + 0.5 + 4 + 8, "k_mg_up<2,update> (prolongation + post-smoothing + p += e, finest)"),
-    "rhs": (4 * 3 + 8, "k_div25<float,double>"),  # read u* (3 x FP32), write the FP64 rhs
-    "correct": (4 * 6 + 8, "k_correct25<float,double>"),
+    # read u* (3 x FP32), write the FP64 rhs (its trapezoid-weighted sums ride along)
+    "rhs": (4 * 3 + 8, "k_div25v<double> (Poisson rhs with its weighted sums)"),
+    # read u* (3 x FP32) and the FP64 pressure, write u (3 x FP32)
+    "correct": (4 * 6 + 8, "k_correct25v (FP64 pressure, FP32 velocity)"),
     "resid64": (8 + 8 + 4, "k_resid25<float,double> (double-float residual, finest level)"),  # read p, rhs; write r
 }
 # the kernel the roofline entry describes: the finest level's fused
-# pre-smoothing kernel, the largest share of the step
-ROOF_KERNEL = "mg_down"
+# post-smoothing kernel, the largest single share of the step
+ROOF_KERNEL = "mg_up"
 
 
 def kernel_roofline(o3d, ctx, peaks: dict) -> dict:
@@ -297,28 +299,88 @@ def kernel_roofline(o3d, ctx, peaks: dict) -> dict:
     return out
 
 
-def cpu_baseline_oracle(seconds_budget: float = 20.0, omp: bool = False, sweeps: int = 30) -> dict:
-    """FP64 oracle (serial restatement of the reference) on one bounded
-    sample of the workload: one time step at 256^3 with the lexicographic SOR
-    capped at `sweeps` sweeps (the GPU needs more, so this overstates the CPU
-    rate)."""
+# Lexicographic SOR sweeps the reference's solver takes per step of this
+# workload at eps = 1e-8 (omega = 2/(1 + sin(2 pi^2 / 256)), starting from the
+# previous pressure): the oracle's exit iterations on steps 1-5 were 338,
+# 346, 243, 236 and 240; the AB3 steps settle at about 240.
+# `python bench.py --cpu-full-steps 5` runs those steps to convergence again.
+K_LEX = 240
+
+
+def _cpu_case(orc, kmax):
+    L = 2 * math.pi * (N - 1) / N
+    return orc.Case(N, N, N, L, L, L, dt=0.2 * 2 * math.pi / N,
+                    omega=2.0 / (1.0 + math.sin(math.pi * 2 * math.pi / N)), eps=EPS, kmax=kmax)
+
+
+def cpu_sweep_seconds(sweeps: int = 10) -> float:
+    """Seconds per lexicographic SOR sweep of the oracle at 256^3 (the
+    reference's poisson_solver_0000 loop; serial as in the reference)."""
+    import numpy as np
+
     from oracle import oracle as orc
 
     orc.build()
-    L = 2 * math.pi * (N - 1) / N
-    case = orc.Case(N, N, N, L, L, L, dt=0.2 * 2 * math.pi / N, omega=2.0 / (1.0 + math.sin(math.pi * 2 * math.pi / N)),
-                    eps=EPS, kmax=sweeps)
+    case = _cpu_case(orc, sweeps)
+    rng = np.random.default_rng(0)
+    rhs = np.asfortranarray(rng.standard_normal(case.shape))
+    pp = orc.field3(case.shape)
+    t0 = time.perf_counter()
+    orc.poisson_sor(case, pp, rhs, case.omega, 0.0, sweeps)  # eps = 0: exactly `sweeps` sweeps
+    return (time.perf_counter() - t0) / sweeps
+
+
+def cpu_step_seconds(omp: bool, sweeps: int = 10) -> float:
+    """Seconds of one 256^3 step of the oracle (predictor, divergence,
+    correction, diagnostics) with its SOR capped at `sweeps` sweeps."""
+    from oracle import oracle as orc
+
+    orc.build()
+    case = _cpu_case(orc, sweeps)
     st = orc.State.zeros(case)
     orc.init_tgv(case, st, omp=omp)
     r = orc.Runner(case, st, omp=omp)
     t0 = time.perf_counter()
     r.step(1)
-    dt = time.perf_counter() - t0
+    return time.perf_counter() - t0
+
+
+def cpu_baseline_oracle(omp: bool = False, sweeps: int = 10) -> dict:
+    """The FP64 oracle (the C restatement of the reference) on a bounded
+    sample of the workload, extrapolated to a full step: one 256^3 step with
+    the lexicographic SOR capped at `sweeps` sweeps, plus `sweeps` sweeps of
+    the solver timed alone; a full step is that step plus K_LEX - sweeps more
+    sweeps."""
+    t_cap = cpu_step_seconds(omp, sweeps)
+    t_sweep = cpu_sweep_seconds(sweeps)
+    t_step = t_cap + (K_LEX - sweeps) * t_sweep
     cores = (os.cpu_count() or 1) if omp else 1
-    return {"value": N ** 3 / dt / 1e6, "unit": "Mpt-steps/s", "cores": cores, "kind": "port",
-            "sample": f"1 time step of the 256^3 workload in FP64 on the oracle (C restatement), "
-                      f"lexicographic SOR capped at {sweeps} sweeps; {dt:.1f} s",
-            "seconds": dt}
+    return {"value": N ** 3 / t_step / 1e6, "unit": "Mpt-steps/s", "cores": cores, "kind": "port",
+            "sample": (f"extrapolated full step: 1 step of the 256^3 workload in FP64 on the oracle (C restatement) "
+                       f"with the lexicographic SOR capped at {sweeps} sweeps ({t_cap:.2f} s), plus {sweeps} "
+                       f"sweeps timed alone ({t_sweep:.3f} s each), scaled to {K_LEX} sweeps per step (the "
+                       f"reference solver's exit iteration on this workload) = {t_step:.1f} s per step"),
+            "seconds_sampled": t_cap + sweeps * t_sweep, "seconds_per_step": t_step, "sweep_s": t_sweep,
+            "sweeps_per_step": K_LEX}
+
+
+def cpu_full_steps(nsteps: int, omp: bool) -> dict:
+    """Full steps of the oracle with the SOR to convergence: the exit
+    iteration and the time of each (about a minute per step at 256^3)."""
+    from oracle import oracle as orc
+
+    orc.build()
+    case = _cpu_case(orc, 100000)
+    st = orc.State.zeros(case)
+    orc.init_tgv(case, st, omp=omp)
+    r = orc.Runner(case, st, omp=omp)
+    out = []
+    for it in range(1, nsteps + 1):
+        t0 = time.perf_counter()
+        info = r.step(it)
+        out.append({"step": it, "sor_status": info.sor_status, "sweeps": info.sor_iters,
+                    "seconds": time.perf_counter() - t0})
+    return {"workload": WORKLOAD, "omp_cores": (os.cpu_count() or 1) if omp else 1, "steps": out}
 
 
 GUESS_DESC = {"mixed_mg_learned": "learned (U-Net correction of the previous pressure)",
@@ -417,21 +479,27 @@ def gpu_arm(args, rank, world, local):
 
 
 def reference_arm(args, rank, world):
+    """The reference's CPU implementation of the path on the host cores: the
+    oracle with OpenMP on its stencil passes (the lexicographic SOR stays
+    serial, as in the reference), each step a bounded sample extrapolated to
+    a full step (cpu_baseline_oracle)."""
     if rank != 0:
         return None
-    samples = []
+    t_sweep = cpu_sweep_seconds()
+    caps = []
     for k in range(args.warmup + args.steps):
-        r = cpu_baseline_oracle(omp=True, sweeps=10)
+        t = cpu_step_seconds(True)
         if k >= args.warmup:
-            samples.append(r)
-    sec = sum(s["seconds"] for s in samples)
-    val = N ** 3 * len(samples) / sec / 1e6
-    cb = {"value": val, "unit": "Mpt-steps/s", "cores": samples[0]["cores"], "kind": "port",
-          "sample": "per step: 1 time step of the 256^3 workload in FP64 on the oracle (C restatement, "
-                    "OpenMP on the stencil passes, lexicographic SOR serial as in the reference) with the "
-                    "SOR capped at 10 sweeps"}
+            caps.append(t)
+    t_step = sum(caps) / len(caps) + (K_LEX - 10) * t_sweep
+    val = N ** 3 / t_step / 1e6
+    cb = {"value": val, "unit": "Mpt-steps/s", "cores": os.cpu_count() or 1, "kind": "port",
+          "sample": (f"per step: 1 time step of the 256^3 workload in FP64 on the oracle (C restatement, OpenMP on "
+                     f"the stencil passes, lexicographic SOR serial as in the reference) with the SOR capped at 10 "
+                     f"sweeps (mean {sum(caps) / len(caps):.2f} s), extrapolated to {K_LEX} sweeps per step with "
+                     f"{t_sweep:.3f} s per sweep timed alone = {t_step:.1f} s per step")}
     return {"metric": METRIC, "value": val, "unit": "Mpt-steps/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * sec / len(samples), "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "grid": [N, N, N]}, "impl": "reference",
             "cpu_baseline": cb, "e2e": {"value": val, "unit": "Mpt-steps/s", "h2d_bytes_per_step": 0,
@@ -447,11 +515,16 @@ def main():
     ap.add_argument("--quick", action="store_true", help="headline variant only")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end run")
+    ap.add_argument("--cpu-full-steps", type=int, default=0,
+                    help="run this many full 256^3 steps of the oracle (SOR to convergence) and print them")
     ap.add_argument("--no-roofline", action="store_true",
                     help="skip the per-kernel timing launches (for a launch list of the steps alone)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.cpu_full_steps:
+        print(json.dumps(cpu_full_steps(args.cpu_full_steps, omp=True)), flush=True)
+        return
     rank, world, local = dist_setup()
     if args.impl == "reference":
         line = reference_arm(args, rank, world)

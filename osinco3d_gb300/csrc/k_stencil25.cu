@@ -47,18 +47,6 @@ __device__ __forceinline__ XYCell xy_cell(const Grid& g, int i, int j) {
   return c;
 }
 
-// plane k, ghost-mapped along z: element offset of the plane and its flip
-struct ZPlane {
-  long long off;
-  bool fz;
-};
-__device__ __forceinline__ ZPlane z_plane(const Grid& g, int k) {
-  ZPlane z;
-  const int kk = ghost(k, g.nz, g.bc[2] == AX_ZERO ? AX_PERIODIC : g.bc[2], &z.fz);
-  z.off = g.sz() * kk;
-  return z;
-}
-
 // whether a field odd along odd_axis (0/1/2; -1 = even) flips at a cell
 __device__ __forceinline__ bool flips(const XYCell& x, bool fz, int odd_axis) {
   return odd_axis == 0 ? x.fx : odd_axis == 1 ? x.fy : odd_axis == 2 ? fz : false;
@@ -134,6 +122,20 @@ long long z_blocks(const Grid& g) {
   const dim3 b = grid25(g);
   return (long long)b.x * b.y * b.z;
 }
+template <class T>
+long long div_blocks(const Grid& g) {
+  if (sizeof(T) == 4 && stencil_v_ok(g)) return div_v_blocks(g);
+  return z_blocks(g);
+}
+template <class T>
+long long corr_blocks(const Grid& g) {
+  if (sizeof(T) == 4 && stencil_v_ok(g)) return corr_v_blocks(g);
+  return z_blocks(g);
+}
+template long long div_blocks<float>(const Grid&);
+template long long div_blocks<double>(const Grid&);
+template long long corr_blocks<float>(const Grid&);
+template long long corr_blocks<double>(const Grid&);
 
 // The plane loop runs in rounds of 7 fully unrolled iterations (the chunk of
 // planes is a multiple of 7 and the ring has R = 7 stages, P = 3): the ring
@@ -639,6 +641,12 @@ static void predict_launch_xo(const PredArgs<T>& a, cudaStream_t s) {
 // the open-x closures are compiled in only for grids with an open x axis
 template <class T>
 void launch_predict(const PredArgs<T>& a, cudaStream_t s) {
+  if constexpr (sizeof(T) == 4) {
+    if (stencil_v_ok(a.g)) {
+      launch_predict_v(a, s);
+      return;
+    }
+  }
   if (a.g.bc[0] == AX_OPEN) predict_launch_xo<T, true>(a, s);
   else predict_launch_xo<T, false>(a, s);
 }
@@ -655,6 +663,12 @@ static void div_launch(const T* fx, const T* fy, const T* fz, O* out, const Grid
 template <class T, class O>
 void launch_div(const T* fx, const T* fy, const T* fz, O* out, const Grid& g, const Coef3<T>& cf,
                 int odd, T dt, int divide, StatPart* part, cudaStream_t s, double* wpart, int wmask) {
+  if constexpr (sizeof(T) == 4) {
+    if (stencil_v_ok(g)) {
+      launch_div_v<O>(fx, fy, fz, out, g, cf, odd, dt, divide, part, s, wpart, wmask);
+      return;
+    }
+  }
   const bool zon = g.bc[2] != AX_ZERO;
   if (g.bc[0] == AX_OPEN) {
     if (zon) div_launch<T, O, true, true>(fx, fy, fz, out, g, cf, odd, dt, divide, part, s, wpart, wmask);
@@ -674,6 +688,12 @@ static void correct_launch(const CorrArgs<T, S>& a, cudaStream_t s) {
 }
 template <class T, class S>
 void launch_correct(const CorrArgs<T, S>& a, cudaStream_t s) {
+  if constexpr (sizeof(T) == 4 && sizeof(S) == 8) {
+    if (stencil_v_ok(a.g)) {
+      launch_correct_v(a, s);
+      return;
+    }
+  }
   const bool zon = a.g.bc[2] != AX_ZERO;
   if (a.g.bc[0] == AX_OPEN) {
     if (zon) correct_launch<T, S, true, true>(a, s);

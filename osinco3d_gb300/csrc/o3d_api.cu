@@ -284,7 +284,7 @@ int rhs_t(o3d_ctx* c) {
   launch_div<T, double>((const T*)c->up[0], (const T*)c->up[1], (const T*)c->up[2], (double*)c->rhs, c->g, cf,
                         1, (T)c->P.dt, 1, c->spart, c->s, fuse_wsum ? c->wpart : nullptr, wmask);
   c->rhs_wsum = fuse_wsum ? 1 : 0;
-  launch_finalize_stats(c->spart, z_blocks(c->g), c->g, c->diag->divp, c->s);
+  launch_finalize_stats(c->spart, div_blocks<T>(c->g), c->g, c->diag->divp, c->s);
   c->launches += 2;
   CKL();
   return O3D_OK;
@@ -306,7 +306,7 @@ int correct_t(o3d_ctx* c) {
   // min x3, max x3, |max| x3, nan flag
   unsigned long long ops = 0;
   for (int q = 0; q < 10; ++q) ops |= (unsigned long long)(q < 3 ? RED_MIN : RED_MAX) << (2 * q);
-  launch_finalize(c->part, z_blocks(c->g), 10, ops, c->diag->sums, c->s);
+  launch_finalize(c->part, corr_blocks<T>(c->g), 10, ops, c->diag->sums, c->s);
   c->launches += 2;
   CKL();
   return O3D_OK;
@@ -317,7 +317,7 @@ int divu_diag_t(o3d_ctx* c) {
   Coef3<T> cf = cast_coef<T>(c->cf);
   launch_div<T, T>((const T*)c->u[0], (const T*)c->u[1], (const T*)c->u[2], (T*)nullptr, c->g, cf, 1,
                    (T)c->P.dt, 0, c->spart, c->s);
-  launch_finalize_stats(c->spart, z_blocks(c->g), c->g, c->diag->divu, c->s);
+  launch_finalize_stats(c->spart, div_blocks<T>(c->g), c->g, c->diag->divu, c->s);
   c->launches += 2;
   CKL();
   return O3D_OK;
@@ -639,7 +639,7 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
     // residual kernel subtracts it as it reads the rhs
     // (from the divergence kernel's sums once per rhs: a later solve of the
     // same, possibly shifted, rhs sums it again)
-    if (c->rhs_wsum) launch_rhs_wmean_final(c->wpart, z_blocks(c->g), c->gp, c->ctrl, c->s, &c->launches);
+    if (c->rhs_wsum) launch_rhs_wmean_final(c->wpart, div_blocks<float>(c->g), c->gp, c->ctrl, c->s, &c->launches);
     else launch_rhs_wmean<double>((const double*)c->rhs, c->gp, c->part, c->ctrl, c->s, &c->launches);
     c->rhs_wsum = 0;
     if (!(c->mixed && use_mg)) {
@@ -868,7 +868,8 @@ int o3d_create(const o3d_params* p, o3d_ctx** out) {
   const long long nb = pt_blocks(c->g) + 1;
   st = st ? st : dalloc(c->s, (void**)&c->part, (size_t)nb * 16 * sizeof(double));
   st = st ? st : dalloc(c->s, (void**)&c->spart, (size_t)nb * sizeof(StatPart));
-  st = st ? st : dalloc(c->s, (void**)&c->wpart, (size_t)z_blocks(c->g) * sizeof(double));
+  st = st ? st : dalloc(c->s, (void**)&c->wpart,
+                        (size_t)std::max(z_blocks(c->g), div_blocks<float>(c->g)) * sizeof(double));
   st = st ? st : dalloc(c->s, (void**)&c->diag, sizeof(DevDiag));
   st = st ? st : dalloc(c->s, (void**)&c->ctrl, sizeof(SolveCtrl));
   if (!st && cudaMallocHost((void**)&c->diag_h, sizeof(DevDiag)) != cudaSuccess) st = O3D_ERR_NOMEM;

@@ -86,6 +86,18 @@ __device__ __forceinline__ int ghost(int m, int n, int bc, bool* flip) {
 template <class T>
 __device__ __forceinline__ T ld(const T* __restrict__ p, long long i) { return __ldg(p + i); }
 
+// plane k, ghost-mapped along z: element offset of the plane and its flip
+struct ZPlane {
+  long long off;
+  bool fz;
+};
+__device__ __forceinline__ ZPlane z_plane(const Grid& g, int k) {
+  ZPlane z;
+  const int kk = ghost(k, g.nz, g.bc[2] == AX_ZERO ? AX_PERIODIC : g.bc[2], &z.fz);
+  z.off = g.sz() * kk;
+  return z;
+}
+
 // block-wide max of nonnegative floats, result valid in thread 0
 __device__ __forceinline__ float block_max_f(float v) {
   __shared__ float sh[32];

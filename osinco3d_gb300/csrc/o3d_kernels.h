@@ -60,6 +60,13 @@ void set_error(const char* fmt, ...);
 long long pt_blocks(const Grid& g);
 // blocks of the z-marching (2.5D) kernels: divergence and correction
 long long z_blocks(const Grid& g);
+// blocks (statistics and weighted-sum records) of the divergence kernel that
+// launch_div runs for field type T, and of the correction kernel of
+// launch_correct
+template <class T>
+long long div_blocks(const Grid& g);
+template <class T>
+long long corr_blocks(const Grid& g);
 
 template <class T>
 void launch_der(const T* f, T* df, const Grid& g, const AxisCoef<T>& c, int axis, int order,
@@ -70,6 +77,18 @@ void launch_out_snapshot(const T* const u[3], double* const out[5], const Grid& 
                          cudaStream_t s);
 template <class T>
 void launch_predict(const PredArgs<T>& a, cudaStream_t s);
+// the FP32 2.5D kernels with two x-adjacent points per thread
+// (k_stencil25v.cu), for grids with nx a multiple of 4
+bool stencil_v_ok(const Grid& g);
+void launch_predict_v(const PredArgs<float>& a, cudaStream_t s);
+template <class O>
+void launch_div_v(const float* fx, const float* fy, const float* fz, O* out, const Grid& g, const Coef3<float>& cf,
+                  int odd, float dt, int divide, StatPart* part, cudaStream_t s, double* wpart, int wmask);
+void launch_correct_v(const CorrArgs<float, double>& a, cudaStream_t s);
+long long div_v_blocks(const Grid& g);
+long long corr_v_blocks(const Grid& g);
+// planes per block of the two-point kernels for `per_sm` resident blocks
+int v_chunk(const Grid& g, int per_sm);
 template <class T>
 void launch_nu_t(const T* ux, const T* uy, const T* uz, T* nu, const Grid& g, const Coef3<T>& cf,
                  T csd2, cudaStream_t s);
