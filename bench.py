@@ -43,7 +43,7 @@ PRED_BYTES_PER_PT = 15 * 4   # read u,v,w + 6 history, write 3 u* + 3 fluxes
 TRAFFIC_PER_LAUNCH: dict = {
     "mg_down": (73.19936 + 32.406016) * 1e6,      # k_mg_down_tgv256.md
     "mg_up": (288.510464 + 152.460032) * 1e6,     # k_mg_up_tgv256.md
-    "predict": (623.436032 + 365.83552) * 1e6,    # k_predict25_tgv256.md
+    "predict": (424.591104 + 348.993024) * 1e6,   # k_predict25v_tgv256.md
     "rhs": (202.962432 + 3.673088) * 1e6,         # k_div25_tgv256.md (statistics pass, no rhs write)
     "correct": (339.60832 + 169.290496) * 1e6,    # k_correct25_tgv256.md
     "resid64": (270.596864 + 53.38368) * 1e6,     # k_resid25_tgv256.md
@@ -272,11 +272,12 @@ KERNEL_BYTES = {
     "mg_down": (4 + 4 + 0.5, "k_mg_down<2,zero> (pre-smoothing + residual + restriction, finest level)"),
     # read e, r, p and the coarse correction (1/8), write e and p
     "mg_up": (4 + 4 + 8 + 0.5 + 4 + 8, "k_mg_up<2,update> (prolongation + post-smoothing + p += e, finest)"),
-    # read u* (3 x FP32), write the FP64 rhs (its trapezoid-weighted sums ride along)
-    "rhs": (4 * 3 + 8, "k_div25v<double> (Poisson rhs with its weighted sums)"),
+    # read u* (3 x FP32), write the FP32 rhs (its trapezoid-weighted sums ride along)
+    "rhs": (4 * 3 + 4, "k_div25v<float> (Poisson rhs, FP32, with its weighted sums)"),
     # read u* (3 x FP32) and the FP64 pressure, write u (3 x FP32)
     "correct": (4 * 6 + 8, "k_correct25v (FP64 pressure, FP32 velocity)"),
-    "resid64": (8 + 8 + 4, "k_resid25<float,double> (double-float residual, finest level)"),  # read p, rhs; write r
+    # read p (FP64) and the FP32 rhs, write r (FP32)
+    "resid64": (8 + 4 + 4, "k_resid25<float,float> (double-float residual, finest level)"),
 }
 # the kernel the roofline entry describes: the finest level's fused
 # post-smoothing kernel, the largest single share of the step

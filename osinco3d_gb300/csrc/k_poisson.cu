@@ -1367,11 +1367,16 @@ template void launch_level_kernel<float, double>(int, double*, const double*, co
                                                  cudaStream_t);
 template void launch_level_kernel<double, double>(int, double*, const double*, const MGLevel&, SolveCtrl*,
                                                   cudaStream_t);
+template void launch_level_kernel<float, float>(int, double*, const float*, const MGLevel&, SolveCtrl*,
+                                                cudaStream_t);
 
 template void launch_mg_outer<double, double>(double*, const double*, MGLevel*, int, int, int, int,
                                               double, int, SolveCtrl*, cudaStream_t, long long*);
 template void launch_mg_outer<float, double>(double*, const double*, MGLevel*, int, int, int, int,
                                              float, int, SolveCtrl*, cudaStream_t, long long*);
+template void launch_mg_outer<float, float>(double*, const float*, MGLevel*, int, int, int, int,
+                                            float, int, SolveCtrl*, cudaStream_t, long long*);
+template void launch_mg_resid<float, float>(double*, const float*, MGLevel*, SolveCtrl*, cudaStream_t, long long*);
 template void launch_rhs_wmean<double>(const double*, const Grid&, double*, SolveCtrl*, cudaStream_t, long long*);
 template void launch_rhs_wmean<float>(const float*, const Grid&, double*, SolveCtrl*, cudaStream_t, long long*);
 template void launch_residual_inf<double>(const double*, const double*, const Grid&, const PoiCoef<double>&,

@@ -87,6 +87,8 @@ struct o3d_ctx {
   void* src;
   void* fphi[3];
   void* rhs;
+  float* rhs32;      // the mixed multigrid step's rhs, FP32 (its values are FP32 numbers)
+  int rhs_f32;       // the current rhs is rhs32, not rhs
   double* pp;
   double* pp_prev;   // previous step's pressure (extrapolated and learned guesses, lazy)
   int pp_prev_valid;
@@ -121,6 +123,10 @@ struct o3d_ctx {
   int mg_batch;
   long long mg_nodes;
   cudaGraphExec_t learn_exec;  // first outer iteration with the learned guess (multigrid)
+  cudaGraphExec_t mg_exec32;    // the same two graphs for the FP32 rhs
+  long long mg_nodes32;
+  cudaGraphExec_t learn_exec32;
+  long long learn_nodes32;
   long long learn_nodes;
 
   cudaEvent_t ev[4];
@@ -281,8 +287,17 @@ int rhs_t(o3d_ctx* c) {
   int wmask = 0;
   for (int a = 0; a < 3; ++a)
     if (c->gp.bc[a] == AX_MIRROR) wmask |= 1 << a;
-  launch_div<T, double>((const T*)c->up[0], (const T*)c->up[1], (const T*)c->up[2], (double*)c->rhs, c->g, cf,
-                        1, (T)c->P.dt, 1, c->spart, c->s, fuse_wsum ? c->wpart : nullptr, wmask);
+  // the mixed multigrid solve reads the rhs as it is computed, in FP32: its
+  // residual kernel takes the value exactly (no FP64 load, no split) and
+  // subtracts the mean in double-float arithmetic
+  const bool f32 = sizeof(T) == 4 && c->P.solver == O3D_SOLVER_MG;
+  if (f32)
+    launch_div<T, T>((const T*)c->up[0], (const T*)c->up[1], (const T*)c->up[2], (T*)c->rhs32, c->g, cf, 1,
+                     (T)c->P.dt, 1, c->spart, c->s, c->wpart, wmask);
+  else
+    launch_div<T, double>((const T*)c->up[0], (const T*)c->up[1], (const T*)c->up[2], (double*)c->rhs, c->g, cf,
+                          1, (T)c->P.dt, 1, c->spart, c->s, fuse_wsum ? c->wpart : nullptr, wmask);
+  c->rhs_f32 = f32 ? 1 : 0;
   c->rhs_wsum = fuse_wsum ? 1 : 0;
   launch_finalize_stats(c->spart, div_blocks<T>(c->g), c->g, c->diag->divp, c->s);
   c->launches += 2;
@@ -486,7 +501,9 @@ double mg_omega_of(const o3d_ctx* c) {
 }
 
 int capture_mg(o3d_ctx* c) {
-  if (c->mg_exec) return O3D_OK;
+  const bool f32 = c->rhs_f32;
+  cudaGraphExec_t* exec = f32 ? &c->mg_exec32 : &c->mg_exec;
+  if (*exec) return O3D_OK;
   if (!c->mg_ok) {
     int st = build_mg(c);
     if (st) return st;
@@ -501,7 +518,10 @@ int capture_mg(o3d_ctx* c) {
   for (int q = 0; q < c->mg_batch; ++q) {
     const int cyc = mg_cycles_of(c);
     const double om = mg_omega_of(c);
-    if (c->mixed)
+    if (c->mixed && f32)
+      launch_mg_outer<float, float>(c->pp, c->rhs32, c->mg.data(), (int)c->mg.size(), pre, post, coarse_sweeps,
+                                    (float)om, cyc, c->ctrl, c->s, &nl);
+    else if (c->mixed)
       launch_mg_outer<float, double>(c->pp, (const double*)c->rhs, c->mg.data(), (int)c->mg.size(), pre,
                                     post, coarse_sweeps, (float)om, cyc, c->ctrl, c->s, &nl);
     else
@@ -509,9 +529,9 @@ int capture_mg(o3d_ctx* c) {
                                       pre, post, coarse_sweeps, om, cyc, c->ctrl, c->s, &nl);
   }
   CK(cudaStreamEndCapture(c->s, &graph));
-  CK(cudaGraphInstantiate(&c->mg_exec, graph, 0));
+  CK(cudaGraphInstantiate(exec, graph, 0));
   CK(cudaGraphDestroy(graph));
-  c->mg_nodes = nl;
+  (f32 ? c->mg_nodes32 : c->mg_nodes) = nl;
   return O3D_OK;
 }
 
@@ -560,7 +580,8 @@ int enqueue_learned_first(o3d_ctx* c, bool learned, bool sampling, bool use_mg, 
   if (c->mixed) launch_learn_extrapolate<float>(c->pp, c->pp_prev, lv, c->s, nl);
   else launch_learn_extrapolate<double>(c->pp, c->pp_prev, lv, c->s, nl);
   if (use_mg) {
-    if (c->mixed) launch_mg_resid<float, double>(c->pp, (const double*)c->rhs, lv, c->ctrl, c->s, nl);
+    if (c->mixed && c->rhs_f32) launch_mg_resid<float, float>(c->pp, c->rhs32, lv, c->ctrl, c->s, nl);
+    else if (c->mixed) launch_mg_resid<float, double>(c->pp, (const double*)c->rhs, lv, c->ctrl, c->s, nl);
     else launch_mg_resid<double, double>(c->pp, (const double*)c->rhs, lv, c->ctrl, c->s, nl);
   } else {
     if (c->mixed) launch_level_kernel<float, double>(1, c->pp, (const double*)c->rhs, lv[0], c->ctrl, c->s);
@@ -640,6 +661,7 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
     // (from the divergence kernel's sums once per rhs: a later solve of the
     // same, possibly shifted, rhs sums it again)
     if (c->rhs_wsum) launch_rhs_wmean_final(c->wpart, div_blocks<float>(c->g), c->gp, c->ctrl, c->s, &c->launches);
+    else if (c->rhs_f32) launch_rhs_wmean<float>(c->rhs32, c->gp, c->part, c->ctrl, c->s, &c->launches);
     else launch_rhs_wmean<double>((const double*)c->rhs, c->gp, c->part, c->ctrl, c->s, &c->launches);
     c->rhs_wsum = 0;
     if (!(c->mixed && use_mg)) {
@@ -660,7 +682,9 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
     if (c->pp_prev_valid && (learned || sampling)) {
       if (learned && use_mg && !sampling) {
         // replayed from a graph captured on first use
-        if (!c->learn_exec) {
+        cudaGraphExec_t& lexec = c->rhs_f32 ? c->learn_exec32 : c->learn_exec;
+        long long& lnodes = c->rhs_f32 ? c->learn_nodes32 : c->learn_nodes;
+        if (!lexec) {
           long long nl = 0;
           cudaGraph_t graph;
           CK(cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal));
@@ -671,13 +695,13 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
             return st1;
           }
           CK(e1);
-          const cudaError_t e2 = cudaGraphInstantiate(&c->learn_exec, graph, 0);
+          const cudaError_t e2 = cudaGraphInstantiate(&lexec, graph, 0);
           cudaGraphDestroy(graph);
           CK(e2);
-          c->learn_nodes = nl;
+          lnodes = nl;
         }
-        CK(cudaGraphLaunch(c->learn_exec, c->s));
-        c->launches += c->learn_nodes;
+        CK(cudaGraphLaunch(lexec, c->s));
+        c->launches += lnodes;
       } else {
         if ((st = enqueue_learned_first(c, learned, sampling, use_mg, pre, post, &c->launches))) return st;
       }
@@ -693,8 +717,8 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
   }
   for (;;) {
     if (use_mg) {
-      CK(cudaGraphLaunch(c->mg_exec, c->s));
-      c->launches += c->mg_nodes;
+      CK(cudaGraphLaunch(c->rhs_f32 ? c->mg_exec32 : c->mg_exec, c->s));
+      c->launches += c->rhs_f32 ? c->mg_nodes32 : c->mg_nodes;
     } else {
       CK(cudaGraphLaunch(c->sor_exec, c->s));
       c->launches += c->sor_nodes;
@@ -720,7 +744,8 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
   if (!use_mg || c->P.diagnostics >= 2) {
     PoiCoef<double> pc = make_poi<double>(c->dx, c->dy, c->dz);
     CK(cudaMemsetAsync(&c->ctrl->res_key, 0, sizeof(unsigned long long), c->s));
-    launch_residual_inf<double>(c->pp, (const double*)c->rhs, c->gp, pc, c->ctrl, c->mixed && use_mg, c->s);
+    if (c->rhs_f32) launch_residual_inf<float>(c->pp, c->rhs32, c->gp, pc, c->ctrl, c->mixed && use_mg, c->s);
+    else launch_residual_inf<double>(c->pp, (const double*)c->rhs, c->gp, pc, c->ctrl, c->mixed && use_mg, c->s);
     c->launches++;
     CKL();
   }
@@ -858,6 +883,8 @@ int o3d_create(const o3d_params* p, o3d_ctx** out) {
   }
   st = st ? st : dalloc(c->s, &c->nu_t, fb);
   st = st ? st : dalloc(c->s, &c->rhs, (size_t)c->g.n * 8);
+  if (p->precision == O3D_PREC_MIXED && p->solver == O3D_SOLVER_MG)
+    st = st ? st : dalloc(c->s, (void**)&c->rhs32, (size_t)c->g.n * 4);
   st = st ? st : dalloc(c->s, (void**)&c->pp, (size_t)c->g.n * 8);
   if (!st && p->nscr) {
     st = st ? st : dalloc(c->s, &c->phi, fb);
@@ -893,7 +920,7 @@ int o3d_destroy(o3d_ctx* c) {
     for (int h = 0; h < 3; ++h) cudaFree(c->fu[q][h]);
     cudaFree(c->fphi[q]);
   }
-  cudaFree(c->nu_t); cudaFree(c->rhs); cudaFree(c->pp); cudaFree(c->pp_prev);
+  cudaFree(c->nu_t); cudaFree(c->rhs); cudaFree(c->rhs32); cudaFree(c->pp); cudaFree(c->pp_prev);
   cudaFree(c->feat); cudaFree(c->ynet);
   cudaFree(c->phi); cudaFree(c->phi2); cudaFree(c->src);
   for (int q = 0; q < 4; ++q) cudaFree(c->stage[q]);
@@ -907,6 +934,8 @@ int o3d_destroy(o3d_ctx* c) {
   if (c->sor_exec) cudaGraphExecDestroy(c->sor_exec);
   if (c->mg_exec) cudaGraphExecDestroy(c->mg_exec);
   if (c->learn_exec) cudaGraphExecDestroy(c->learn_exec);
+  if (c->mg_exec32) cudaGraphExecDestroy(c->mg_exec32);
+  if (c->learn_exec32) cudaGraphExecDestroy(c->learn_exec32);
   for (int q = 0; q < 4; ++q) if (c->ev[q]) cudaEventDestroy(c->ev[q]);
   for (int q = 0; q < 8; ++q) if (c->xev[q]) cudaEventDestroy(c->xev[q]);
   if (c->xs) cudaStreamDestroy(c->xs);
@@ -923,7 +952,10 @@ int o3d_upload(o3d_ctx* c, int field, const double* host) {
   bool is_pp;
   void* d = field_ptr(c, field, &is_pp);
   if (!d) { errf("field %d not allocated or unknown", field); return O3D_ERR_BADARG; }
-  if (field == O3D_FIELD_RHS) c->rhs_wsum = 0;
+  if (field == O3D_FIELD_RHS) {
+    c->rhs_wsum = 0;
+    c->rhs_f32 = 0;
+  }
   if (is_pp) {
     CK(cudaMemcpyAsync(d, host, (size_t)c->g.n * 8, cudaMemcpyHostToDevice, c->s));
   } else {
@@ -939,7 +971,10 @@ int o3d_download(o3d_ctx* c, int field, double* host) {
   bool is_pp;
   void* d = field_ptr(c, field, &is_pp);
   if (!d) { errf("field %d not allocated or unknown", field); return O3D_ERR_BADARG; }
-  if (is_pp) {
+  if (field == O3D_FIELD_RHS && c->rhs_f32) {  // the step's FP32 rhs, widened exactly
+    int st = get_field(c, c->rhs32, host);
+    if (st) return st;
+  } else if (is_pp) {
     CK(cudaMemcpyAsync(host, d, (size_t)c->g.n * 8, cudaMemcpyDeviceToHost, c->s));
   } else {
     int st = get_field(c, d, host);
@@ -1046,6 +1081,7 @@ int o3d_poisson_solve(o3d_ctx* c, double* pp, const double* rhs, double* omega, 
   CK(cudaMemcpyAsync(c->pp, pp, (size_t)c->g.n * 8, cudaMemcpyHostToDevice, c->s));
   CK(cudaMemcpyAsync(c->rhs, rhs, (size_t)c->g.n * 8, cudaMemcpyHostToDevice, c->s));
   c->rhs_wsum = 0;  // a caller's rhs: its mean takes the separate pass
+  c->rhs_f32 = 0;
   int st = O3D_OK;
   o3d_step_info info;
   memset(&info, 0, sizeof info);
@@ -1342,10 +1378,12 @@ int o3d_rbsor_sweeps_dev(o3d_ctx* c, double* d_pp, const double* d_rhs, double o
 
 int o3d_attach_unet(o3d_ctx* c, o3d_unet* net) {
   if (!c) return O3D_ERR_BADARG;
-  if (c->learn_exec) {
+  if (c->learn_exec || c->learn_exec32) {
     CK(cudaStreamSynchronize(c->s));
-    cudaGraphExecDestroy(c->learn_exec);
+    if (c->learn_exec) cudaGraphExecDestroy(c->learn_exec);
+    if (c->learn_exec32) cudaGraphExecDestroy(c->learn_exec32);
     c->learn_exec = nullptr;
+    c->learn_exec32 = nullptr;
   }
   c->unet = net;
   if (!net) return O3D_OK;
@@ -1443,7 +1481,9 @@ int o3d_time_kernel(o3d_ctx* c, int kernel, int reps, double* ms_per_launch) {
         return O3D_OK;
       }
       default:
-        if (c->mixed)
+        if (c->mixed && c->rhs_f32)
+          launch_level_kernel<float, float>(kernel - 3, c->pp, c->rhs32, c->mg[0], c->ctrl, c->s);
+        else if (c->mixed)
           launch_level_kernel<float, double>(kernel - 3, c->pp, (const double*)c->rhs, c->mg[0], c->ctrl, c->s);
         else
           launch_level_kernel<double, double>(kernel - 3, c->pp, (const double*)c->rhs, c->mg[0], c->ctrl, c->s);
