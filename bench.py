@@ -44,9 +44,9 @@ TRAFFIC_PER_LAUNCH: dict = {
     "mg_down": (73.19936 + 32.406016) * 1e6,      # k_mg_down_tgv256.md
     "mg_up": (288.510464 + 152.460032) * 1e6,     # k_mg_up_tgv256.md
     "predict": (424.591104 + 348.993024) * 1e6,   # k_predict25v_tgv256.md
-    "rhs": (202.962432 + 3.673088) * 1e6,         # k_div25_tgv256.md (statistics pass, no rhs write)
-    "correct": (339.60832 + 169.290496) * 1e6,    # k_correct25_tgv256.md
-    "resid64": (270.596864 + 53.38368) * 1e6,     # k_resid25_tgv256.md
+    "rhs": (208.823552 + 43.305472) * 1e6,        # k_div25v_tgv256.md (the rhs-writing launch)
+    "correct": (352.484864 + 149.464832) * 1e6,   # k_correct25v_tgv256.md
+    "resid64": (204.008448 + 48.967936) * 1e6,    # k_resid25_tgv256.md
 }
 
 
@@ -262,7 +262,31 @@ def _measure_e2e(o3d, steps: int, warmup: int, world: int, weights=None, **kw) -
     nbytes = 4 * (N ** 3) * 8
     return {"value": world * (N ** 3) * steps / wall / 1e6, "unit": "Mpt-steps/s",
             "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
-            "ms_per_step": 1e3 * wall / steps}
+            "ms_per_step": 1e3 * wall / steps, "link": link_rates(bufs[0])}
+
+
+def link_rates(host) -> dict:
+    """Plain copies of one pinned FP64 field (the e2e run's own host buffer)
+    to and from the device, timed with CUDA events: the host link's rate on
+    this box, against which the e2e copies are judged."""
+    import torch
+
+    h = torch.from_numpy(host.reshape(-1, order="F"))  # a view: the page-locked memory itself
+    d = torch.empty(h.numel(), dtype=torch.float64, device="cuda")
+    nb = h.numel() * 8
+    out = {}
+    for name, fn in (("h2d_gbs", lambda: d.copy_(h, non_blocking=True)),
+                     ("d2h_gbs", lambda: h.copy_(d, non_blocking=True))):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(5):
+            fn()
+        e1.record()
+        e1.synchronize()
+        out[name] = 5 * nb / (e0.elapsed_time(e1) * 1e-3) / 1e9
+    return out
 
 
 # algorithmic bytes per grid point of the hot kernels (float32 storage)
@@ -384,7 +408,7 @@ def cpu_full_steps(nsteps: int, omp: bool) -> dict:
     return {"workload": WORKLOAD, "omp_cores": (os.cpu_count() or 1) if omp else 1, "steps": out}
 
 
-GUESS_DESC = {"mixed_mg_learned": "learned (U-Net correction of the previous pressure)",
+GUESS_DESC = {"mixed_mg_learned": "learned (U-Net correction of the linearly extrapolated pressure)",
               "mixed_mg": "previous pressure"}
 
 
@@ -429,9 +453,11 @@ def gpu_arm(args, rank, world, local):
                          # FP64 with the mixed method's smoother settings and extrapolated guess
                          ("fp64_mg_v11_om1.25_extrapolated",
                           dict(fp64, mg_pre=1, mg_post=1, mg_omega=1.25, guess=o3d.GUESS_EXTRAPOLATED)),
-                         # the fastest configuration found: extrapolated guess, V(2,1), omega 1.3
+                         # linear extrapolation with its best cycle: V(2,1), omega 1.3
                          ("mixed_mg_extrapolated_v21_om1.3",
-                          dict(mixed, mg_pre=2, mg_post=1, mg_omega=1.3, guess=o3d.GUESS_EXTRAPOLATED))):
+                          dict(mixed, mg_pre=2, mg_post=1, mg_omega=1.3, guess=o3d.GUESS_EXTRAPOLATED)),
+                         # quadratic extrapolation in time with the default V(1,1)
+                         ("mixed_mg_extrapolated2", dict(mixed, guess=o3d.GUESS_EXTRAPOLATED2))):
             if name in variants:
                 continue
             v, cx, _ = run_variant(o3d, name, args.steps, args.warmup, world, **kw)

@@ -66,7 +66,9 @@ enum {
   O3D_GUESS_PREVIOUS = 0, /* previous step's pressure (the reference: pp persists) */
   O3D_GUESS_ZERO = 1,
   O3D_GUESS_LEARNED = 2,  /* extrapolated pressure plus a 3D U-Net correction (below) */
-  O3D_GUESS_EXTRAPOLATED = 3 /* 2 p(n) - p(n-1): linear extrapolation in time */
+  O3D_GUESS_EXTRAPOLATED = 3, /* 2 p(n) - p(n-1): linear extrapolation in time */
+  O3D_GUESS_EXTRAPOLATED2 = 4 /* 3 p(n) - 3 p(n-1) + p(n-2): quadratic extrapolation in time
+                                 (the first solves take the previous, then the linear guess) */
 };
 
 /* field identifiers for o3d_upload / o3d_download */

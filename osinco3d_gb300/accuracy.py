@@ -70,6 +70,8 @@ def main():
     ap.add_argument("--nz", type=int, default=256)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--eps", type=float, default=1e-8)
+    ap.add_argument("--mixed-only", action="store_true",
+                    help="run the mixed method alone (for a launch list of its step) and print its timing")
     args = ap.parse_args()
     mg = dict(solver=o3d.SOLVER_MG, eps=args.eps, kmax=200)
     if args.case == "mixing":
@@ -92,6 +94,10 @@ def main():
         fields = o3d.tgv_fields(p64)
         names = ("ux", "uy", "uz", "pp")
         workload = f"Taylor-Green vortex {args.n}^3, Re 1600, AB3, CFL 0.2"
+    if args.mixed_only:
+        _, ms, cyc = _run(pmx, fields, args.steps, names)
+        print(json.dumps({"workload": workload, "mixed": {"ms_per_step": ms, "vcycles_per_step": cyc}}))
+        return
     res = compare(p64, pmx, fields, names, args.steps)
     res["workload"] = workload
     res["poisson_eps"] = args.eps

@@ -1121,6 +1121,22 @@ void launch_extrapolate(double* p, double* pprev, long long n, cudaStream_t s) {
   launch_pdl(k_extrapolate, (unsigned)((n + 255) / 256), 256, 0, s, p, pprev, n);
 }
 
+// p <- 3 p - 3 p_prev + p_prev2 (quadratic extrapolation in time), and the
+// current pressure into pprev2's buffer, which the caller then swaps with
+// pprev: the history shifts by one step without a copy
+__global__ void k_extrapolate2(double* __restrict__ p, const double* __restrict__ pprev,
+                               double* __restrict__ pprev2, long long n) {
+  pdl_enter();
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const double pc = p[q];
+  p[q] = 3.0 * (pc - pprev[q]) + pprev2[q];
+  pprev2[q] = pc;
+}
+void launch_extrapolate2(double* p, const double* pprev, double* pprev2, long long n, cudaStream_t s) {
+  launch_pdl(k_extrapolate2, (unsigned)((n + 255) / 256), 256, 0, s, p, pprev, pprev2, n);
+}
+
 // the same extrapolation, also writing the last increment d = p - p_prev in T
 template <class T>
 __global__ void k_extrapolate_d(double* __restrict__ p, double* __restrict__ pprev, T* __restrict__ d, long long n) {

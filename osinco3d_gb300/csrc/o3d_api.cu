@@ -7,6 +7,7 @@
 // loop).  The Adams-Bashforth flux history is a ring of three buffers per
 // component, so the history shift of src/integration.f90:176-188 costs no
 // copy.
+#include <utility>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -92,6 +93,8 @@ struct o3d_ctx {
   double* pp;
   double* pp_prev;   // previous step's pressure (extrapolated and learned guesses, lazy)
   int pp_prev_valid;
+  double* pp_prev2;  // the one before (quadratic extrapolation, lazy)
+  int pp_prev2_valid;
   o3d_unet* unet;    // network of the learned guess (not owned)
   float* feat;       // its input on the network grid (2 channels)
   float* ynet;       // its output
@@ -629,13 +632,18 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
   const int guess = c->P.guess;
   const bool learned = guess == O3D_GUESS_LEARNED;
   const bool sampling = c->sample_feat != nullptr;
-  const bool need_hist = guess == O3D_GUESS_EXTRAPOLATED || learned || sampling;
+  const bool quad = guess == O3D_GUESS_EXTRAPOLATED2;
+  const bool need_hist = guess == O3D_GUESS_EXTRAPOLATED || quad || learned || sampling;
   if (learned && !c->unet) {
     errf("the learned initial guess needs a network (o3d_attach_unet)");
     return O3D_ERR_NOT_BUILT;
   }
   if (need_hist && !c->pp_prev) {
     int st0 = dalloc(c->s, (void**)&c->pp_prev, (size_t)c->g.n * 8);
+    if (st0) return st0;
+  }
+  if (quad && !c->pp_prev2) {
+    int st0 = dalloc(c->s, (void**)&c->pp_prev2, (size_t)c->g.n * 8);
     if (st0) return st0;
   }
   if (sampling && (c->P.solver != O3D_SOLVER_MG || (guess != O3D_GUESS_EXTRAPOLATED && !learned))) {
@@ -705,7 +713,18 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
       } else {
         if ((st = enqueue_learned_first(c, learned, sampling, use_mg, pre, post, &c->launches))) return st;
       }
-    } else if (c->pp_prev_valid && guess == O3D_GUESS_EXTRAPOLATED) {
+    } else if (quad && c->pp_prev_valid && c->pp_prev2_valid) {
+      // 3 p(n) - 3 p(n-1) + p(n-2); p(n) lands in pp_prev2's buffer, which
+      // becomes pp_prev (the history shifts by a pointer swap, no copy)
+      launch_extrapolate2(c->pp, c->pp_prev, c->pp_prev2, c->g.n, c->s);
+      std::swap(c->pp_prev, c->pp_prev2);
+      c->launches++;
+      CKL();
+    } else if (c->pp_prev_valid && (guess == O3D_GUESS_EXTRAPOLATED || quad)) {
+      if (quad) {  // second solve: keep p(n-1) for the quadratic guess of the next one
+        CK(cudaMemcpyAsync(c->pp_prev2, c->pp_prev, (size_t)c->g.n * 8, cudaMemcpyDeviceToDevice, c->s));
+        c->pp_prev2_valid = 1;
+      }
       launch_extrapolate(c->pp, c->pp_prev, c->g.n, c->s);
       c->launches++;
       CKL();
@@ -921,6 +940,7 @@ int o3d_destroy(o3d_ctx* c) {
     cudaFree(c->fphi[q]);
   }
   cudaFree(c->nu_t); cudaFree(c->rhs); cudaFree(c->rhs32); cudaFree(c->pp); cudaFree(c->pp_prev);
+  cudaFree(c->pp_prev2);
   cudaFree(c->feat); cudaFree(c->ynet);
   cudaFree(c->phi); cudaFree(c->phi2); cudaFree(c->src);
   for (int q = 0; q < 4; ++q) cudaFree(c->stage[q]);
@@ -1249,29 +1269,34 @@ int ctx_geometry(o3d_ctx* c, o3d_params* p, int* nx, int* ny, int* nz, double* d
   return O3D_OK;
 }
 
-int ctx_history_state(o3d_ctx* c, double* omega, int* has_prev, double* prev_host) {
+int ctx_history_state(o3d_ctx* c, double* omega, int* nprev, double* prev_host, int which) {
   if (omega) *omega = c->omega;
-  if (has_prev) *has_prev = c->pp_prev && c->pp_prev_valid ? 1 : 0;
-  if (prev_host && c->pp_prev && c->pp_prev_valid) {
-    CK(cudaMemcpyAsync(prev_host, c->pp_prev, (size_t)c->g.n * 8, cudaMemcpyDeviceToHost, c->s));
+  const int n = !(c->pp_prev && c->pp_prev_valid) ? 0 : (c->pp_prev2 && c->pp_prev2_valid ? 2 : 1);
+  if (nprev) *nprev = n;
+  if (prev_host && which >= 1 && which <= n) {
+    CK(cudaMemcpyAsync(prev_host, which == 1 ? c->pp_prev : c->pp_prev2, (size_t)c->g.n * 8, cudaMemcpyDeviceToHost,
+                       c->s));
     CK(cudaStreamSynchronize(c->s));
   }
   return O3D_OK;
 }
 
-int ctx_restore_history(o3d_ctx* c, double omega, int has_prev, const double* prev_host) {
+int ctx_restore_history(o3d_ctx* c, double omega, int nprev, const double* prev1, const double* prev2) {
   c->omega = omega;
-  if (!has_prev) {
-    c->pp_prev_valid = 0;
-    return O3D_OK;
+  c->pp_prev_valid = 0;
+  c->pp_prev2_valid = 0;
+  const double* host[2] = {prev1, prev2};
+  double** dev[2] = {&c->pp_prev, &c->pp_prev2};
+  for (int q = 0; q < nprev && q < 2; ++q) {
+    if (!*dev[q]) {
+      int st = dalloc(c->s, (void**)dev[q], (size_t)c->g.n * 8);
+      if (st) return st;
+    }
+    CK(cudaMemcpyAsync(*dev[q], host[q], (size_t)c->g.n * 8, cudaMemcpyHostToDevice, c->s));
   }
-  if (!c->pp_prev) {
-    int st = dalloc(c->s, (void**)&c->pp_prev, (size_t)c->g.n * 8);
-    if (st) return st;
-  }
-  CK(cudaMemcpyAsync(c->pp_prev, prev_host, (size_t)c->g.n * 8, cudaMemcpyHostToDevice, c->s));
   CK(cudaStreamSynchronize(c->s));
-  c->pp_prev_valid = 1;
+  c->pp_prev_valid = nprev >= 1;
+  c->pp_prev2_valid = nprev >= 2;
   return O3D_OK;
 }
 }  // namespace o3d

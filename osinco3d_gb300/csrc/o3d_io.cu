@@ -15,9 +15,11 @@
 
 namespace {
 
-// the history file: magic, then int32 nx, ny, nz, nscr, has_prev,
-// then double omega, then the FP64 arrays (u, v, w fluxes newest then older,
-// the scalar fluxes when nscr = 1, the previous pressure when has_prev = 1)
+// the history file: magic, then int32 nx, ny, nz, nscr, nprev, then double
+// omega, then the FP64 arrays (u, v, w fluxes newest then older, the scalar
+// fluxes when nscr = 1, then the nprev previous pressures, newest first: one
+// for the linear extrapolation and the learned guess, two for the quadratic
+// extrapolation)
 const char HIST_MAGIC[8] = {'O', '3', 'D', 'H', 'I', 'S', 'T', '1'};
 
 struct File {
@@ -129,7 +131,7 @@ int o3d_save_history(o3d_ctx* c, const char* path) {
   std::vector<double> buf(n);
   double omega = 0.0;
   int has_prev = 0;
-  if ((st = o3d::ctx_history_state(c, &omega, &has_prev, nullptr))) return st;
+  if ((st = o3d::ctx_history_state(c, &omega, &has_prev, nullptr, 0))) return st;
   File F;
   F.f = fopen(path, "wb");
   if (!F.f) {
@@ -147,8 +149,8 @@ int o3d_save_history(o3d_ctx* c, const char* path) {
     if ((st = o3d_download(c, id, buf.data()))) return st;
     ok = put(F.f, buf.data(), n * 8);
   }
-  if (ok && has_prev) {
-    if ((st = o3d::ctx_history_state(c, nullptr, nullptr, buf.data()))) return st;
+  for (int q = 1; ok && q <= has_prev; ++q) {
+    if ((st = o3d::ctx_history_state(c, nullptr, nullptr, buf.data(), q))) return st;
     ok = put(F.f, buf.data(), n * 8);
   }
   if (!ok) {
@@ -195,15 +197,18 @@ int o3d_load_history(o3d_ctx* c, const char* path) {
     }
     if ((st = o3d_upload(c, id, buf.data()))) return st;
   }
-  const double* prev = nullptr;
-  if (hdr[4]) {
-    if (!get(F.f, buf.data(), n * 8)) {
+  if (hdr[4] < 0 || hdr[4] > 2) {
+    o3d::set_error("%s: %d previous pressures (at most 2)", path, hdr[4]);
+    return O3D_ERR_BADARG;
+  }
+  std::vector<double> prev((size_t)hdr[4] * n);
+  for (int q = 0; q < hdr[4]; ++q)
+    if (!get(F.f, prev.data() + (size_t)q * n, n * 8)) {
       o3d::set_error("%s: truncated", path);
       return O3D_ERR_BADARG;
     }
-    prev = buf.data();
-  }
-  return o3d::ctx_restore_history(c, omega, hdr[4], prev);
+  return o3d::ctx_restore_history(c, omega, hdr[4], hdr[4] >= 1 ? prev.data() : nullptr,
+                                  hdr[4] >= 2 ? prev.data() + n : nullptr);
 }
 
 }  // extern "C"

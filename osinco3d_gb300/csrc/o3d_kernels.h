@@ -155,8 +155,11 @@ void launch_mg_up(const MGLevel& L, const MGLevel& C, float om, int post, double
 int ctx_geometry(o3d_ctx* c, o3d_params* p, int* nx, int* ny, int* nz, double* dx, double* dy, double* dz);
 // omega and whether a previous pressure exists; prev_host (may be null)
 // receives the previous pressure
-int ctx_history_state(o3d_ctx* c, double* omega, int* has_prev, double* prev_host);
-int ctx_restore_history(o3d_ctx* c, double omega, int has_prev, const double* prev_host);
+// the SOR omega and the previous pressures kept for the extrapolated and
+// learned guesses: *nprev of them (0..2); prev_host receives number `which`
+// (1 = the newest)
+int ctx_history_state(o3d_ctx* c, double* omega, int* nprev, double* prev_host, int which);
+int ctx_restore_history(o3d_ctx* c, double omega, int nprev, const double* prev1, const double* prev2);
 
 // output-cadence diagnostics (k_diag.cu)
 template <class T>
@@ -189,6 +192,7 @@ template <class T>
 void launch_mg_cycles(double* p, MGLevel* lv, int nlev, int pre, int post, int coarse_sweeps, T smooth_omega,
                       int cycles, bool from_e, SolveCtrl* ctrl, cudaStream_t s, long long* nl);
 void launch_extrapolate(double* p, double* pprev, long long n, cudaStream_t s);
+void launch_extrapolate2(double* p, const double* pprev, double* pprev2, long long n, cudaStream_t s);
 
 // learned warm start: the network works on multigrid level ll
 template <class T>

@@ -32,7 +32,7 @@ ERR_NOT_BUILT = -5
 
 PREC_FP64, PREC_MIXED = 0, 1
 SOLVER_SOR, SOLVER_MG = 0, 1
-GUESS_PREVIOUS, GUESS_ZERO, GUESS_LEARNED, GUESS_EXTRAPOLATED = 0, 1, 2, 3
+GUESS_PREVIOUS, GUESS_ZERO, GUESS_LEARNED, GUESS_EXTRAPOLATED, GUESS_EXTRAPOLATED2 = 0, 1, 2, 3, 4
 
 FIELD = {"ux": 0, "uy": 1, "uz": 2, "pp": 3, "ux_pred": 4, "uy_pred": 5, "uz_pred": 6,
          "phi": 7, "src": 8, "nu_t": 9, "rhs": 10}

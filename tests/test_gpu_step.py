@@ -146,11 +146,11 @@ def test_mixing_layer_odd_periodic_steps(oracle, o3d, solver):
     ctx.close()
 
 
-@pytest.mark.parametrize("guess,cycles", [(0, 1), (0, 2), (3, 1), (1, 1)])
+@pytest.mark.parametrize("guess,cycles", [(0, 1), (0, 2), (3, 1), (4, 1), (1, 1)])
 def test_multigrid_step_matches(oracle, o3d, guess, cycles):
     """The multigrid solver inside the step gives the same velocity, whatever
-    the initial guess (previous, extrapolated, zero) and the number of
-    V-cycles per FP64 residual."""
+    the initial guess (previous, linear or quadratic extrapolation in time,
+    zero) and the number of V-cycles per FP64 residual."""
     c = periodic_case(oracle, 32, omega=1.6, eps=EPS, kmax=100000)
     s, ctx, infos = _run_both(oracle, o3d, c, 4, solver=o3d.SOLVER_MG, kmax=200, guess=guess,
                               mg_cycles=cycles)
