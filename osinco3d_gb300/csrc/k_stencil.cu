@@ -112,62 +112,105 @@ __global__ void __launch_bounds__(256) k_stats(const T* __restrict__ ux, const T
 // ---------------------------------------------------------------------------
 // transeq (src/integration.f90:405-447): scalar flux, AB update and the
 // first clipping pass; partial sums of phi before clipping, after clipping
-// and of the weights min(phi, 1-phi).
+// and of the weights min(phi, 1-phi).  A thread marches a column of TQ_KZ
+// planes: the z-line of phi is a register queue (one new load per plane),
+// the x- and y-lines come through the L1 cache, and the three sums are
+// accumulated per thread -- in TwoSum-compensated FP32 pairs for the mixed
+// method (exact to about 2^-48 over the column), FP64 otherwise -- and
+// widened once per thread for the block reduction.
 // ---------------------------------------------------------------------------
+constexpr int TQ_KZ = 16;
+static dim3 tq_grid(const Grid& g) {
+  return dim3((g.nx + 31) / 32, (g.ny + 7) / 8, (g.nz + TQ_KZ - 1) / TQ_KZ);
+}
+static long long tq_blocks(const Grid& g) {
+  const dim3 b = tq_grid(g);
+  return (long long)b.x * b.y * b.z;
+}
+
 template <class T>
 __global__ void __launch_bounds__(256) k_transeq(ScalArgs<T> A) {
   pdl_enter();
   const Grid& g = A.g;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
+  const int k0 = blockIdx.z * TQ_KZ, k1 = min(k0 + TQ_KZ, g.nz);
+  constexpr bool F32 = sizeof(T) == 4;
+  float s_hi[3] = {0.f, 0.f, 0.f}, s_lo[3] = {0.f, 0.f, 0.f};
   double r[3] = {0.0, 0.0, 0.0};
   const int ops[3] = {RED_SUM, RED_SUM, RED_SUM};
   if (i < g.nx && j < g.ny) {
-    const long long q = (long long)i + g.sy() * j + g.sz() * k;
-    T s1[3], s2[3], pc = (T)0;
+    const int cls = xclass(g, i);
+    const bool zon = g.bc[2] != AX_ZERO;
+    const long long xy = (long long)i + g.sy() * j;
+    T zq[7];
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      if (g.bc[a] == AX_ZERO) { s1[a] = (T)0; s2[a] = (T)0; continue; }
-      T v[7];
-      load_line<3>(A.phi, g, a, i, j, k, false, v);
-      const int cls = a == 0 ? xclass(g, i) : 0;
-      s1[a] = d1c(v, A.cf.ax[a], cls);
-      s2[a] = d2c(v, A.cf.ax[a], cls);
-      if (a == 0) pc = v[3];
+    for (int m = 0; m < 7; ++m) zq[m] = (T)0;
+    if (zon) load_line<3>(A.phi, g, 2, i, j, k0, false, zq);  // planes k0 - 3 .. k0 + 3
+    for (int k = k0; k < k1; ++k) {
+      if (zon && k > k0) {  // the scalar is even: the z ghost planes need no sign
+#pragma unroll
+        for (int m = 0; m < 6; ++m) zq[m] = zq[m + 1];
+        zq[6] = __ldg(A.phi + z_plane(g, k + 3).off + xy);
+      }
+      const long long q = xy + g.sz() * k;
+      T vx[7], vy[7];
+      load_line<3>(A.phi, g, 0, i, j, k, false, vx);
+      load_line<3>(A.phi, g, 1, i, j, k, false, vy);
+      const T pc = vx[3];
+      const T s1x = d1c(vx, A.cf.ax[0], cls), s2x = d2c(vx, A.cf.ax[0], cls);
+      const T s1y = d1(vy, A.cf.ax[1]), s2y = d2(vy, A.cf.ax[1]);
+      const T s1z = zon ? d1(zq, A.cf.ax[2]) : (T)0, s2z = zon ? d2(zq, A.cf.ax[2]) : (T)0;
+      T alpha = A.alpha0;
+      if (A.les) alpha = alpha + A.nu_t[q] / A.sc;
+      const T F = alpha * (s2x + s2y + s2z) - (A.u[0][q] * s1x + A.u[1][q] * s1y + A.u[2][q] * s1z) + A.src[q];
+      T ph = pc + A.adu * F;
+      if (A.f2) ph = ph + A.bdu * A.f2[q];
+      if (A.f3) ph = ph + A.cdu * A.f3[q];
+      if (cls == 1) ph = pc;  // open x axis: the inflow value is held
+      A.fnew[q] = F;
+      const T cl = fmax((T)0, fmin((T)1, ph));
+      const T w = cls == 1 ? (T)0 : fmin(cl, (T)1 - cl);  // held inflow nodes take no excess
+      A.phi_out[q] = cl;
+      if constexpr (F32) {
+        two_sum_acc(s_hi[0], s_lo[0], ph);
+        two_sum_acc(s_hi[1], s_lo[1], cl);
+        two_sum_acc(s_hi[2], s_lo[2], w);
+      } else {
+        r[0] += (double)ph;
+        r[1] += (double)cl;
+        r[2] += (double)w;
+      }
     }
-    T alpha = A.alpha0;
-    if (A.les) alpha = alpha + A.nu_t[q] / A.sc;
-    const T F = alpha * (s2[0] + s2[1] + s2[2]) -
-                (A.u[0][q] * s1[0] + A.u[1][q] * s1[1] + A.u[2][q] * s1[2]) + A.src[q];
-    T ph = pc + A.adu * F;
-    if (A.f2) ph = ph + A.bdu * A.f2[q];
-    if (A.f3) ph = ph + A.cdu * A.f3[q];
-    if (xclass(g, i) == 1) ph = pc;  // open x axis: the inflow value is held
-    A.fnew[q] = F;
-    r[0] = (double)ph;
-    const T cl = fmax((T)0, fmin((T)1, ph));
-    r[1] = (double)cl;
-    r[2] = xclass(g, i) == 1 ? 0.0 : (double)fmin(cl, (T)1 - cl);  // held inflow nodes take no excess
-    A.phi_out[q] = cl;
+    if constexpr (F32) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) r[c] = to_t<double>(s_hi[c]) + to_t<double>(s_lo[c]);
+    }
   }
   block_reduce_store<3>(r, ops, A.part, block_linear_id());
 }
 
 // second clipping pass (src/integration.f90:443-450); sums[0..2] are the
-// finalized totals of k_transeq.
+// finalized totals of k_transeq.  The FP64 coefficient excess / sum(weight)
+// is formed once per block, so no thread divides in FP64; then
+// phi <- clip(phi + min(phi, 1 - phi) * coefficient).
 template <class T>
-__global__ void k_scalar_redistribute(T* __restrict__ phi, long long n, const double* sums, int nx_inflow) {
+__global__ void __launch_bounds__(256) k_scalar_redistribute(T* __restrict__ phi, long long n, const double* sums,
+                                                             int nx_inflow) {
   pdl_enter();
-  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= n) return;
-  if (nx_inflow > 0 && q % nx_inflow == 0) return;  // open x axis: inflow nodes are held
-  const double wsum = sums[2];
-  if (wsum == 0.0) return;  // nothing to spread the excess over
-  const double excess = sums[0] / (double)n - sums[1] / (double)n;
-  const T p = phi[q];
-  const T w = (T)((double)fmin(p, (T)1 - p) / wsum);
-  phi[q] = fmax((T)0, fmin((T)1, p + (T)excess * w));
+  __shared__ double coef;
+  if (threadIdx.x == 0) {
+    const double wsum = sums[2];
+    coef = wsum == 0.0 ? 0.0 : (sums[0] / (double)n - sums[1] / (double)n) / wsum;
+  }
+  __syncthreads();
+  if (sums[2] == 0.0) return;  // nothing to spread the excess over
+  const T c = (T)coef;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+    if (nx_inflow > 0 && q % nx_inflow == 0) continue;  // open x axis: inflow nodes are held
+    const T p = phi[q];
+    phi[q] = fmax((T)0, fmin((T)1, p + fmin(p, (T)1 - p) * c));
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -261,10 +304,12 @@ void launch_stats(const T* ux, const T* uy, const T* uz, const Grid& g, const Co
 }
 template <class T>
 void launch_transeq(const ScalArgs<T>& a, const double* sums, cudaStream_t s, long long* nl) {
-  launch_pdl(k_transeq<T>, pt_grid(a.g), pt_block(), 0, s, a);
-  launch_finalize(a.part, pt_blocks(a.g), 3, 0ull, (double*)sums, s);
-  launch_pdl(k_scalar_redistribute<T>, (unsigned)((a.g.n + 255) / 256), 256, 0, s, a.phi_out, a.g.n, sums,
-             a.g.bc[0] == AX_OPEN ? a.g.nx : 0);
+  launch_pdl(k_transeq<T>, tq_grid(a.g), dim3(32, 8), 0, s, a);
+  launch_finalize(a.part, tq_blocks(a.g), 3, 0ull, (double*)sums, s);
+  // a grid-stride loop over at most 8 blocks of 256 threads per SM
+  const long long want = (a.g.n + 255) / 256;
+  launch_pdl(k_scalar_redistribute<T>, (unsigned)(want < 152 * 8 ? want : 152 * 8), 256, 0, s, a.phi_out, a.g.n,
+             sums, a.g.bc[0] == AX_OPEN ? a.g.nx : 0);
   *nl += 3;
 }
 void launch_finalize(const double* part, long long nblk, int M, unsigned long long opmask,
