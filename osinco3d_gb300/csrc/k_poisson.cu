@@ -743,6 +743,48 @@ __global__ void __launch_bounds__(256) k_restrict_nn(const T* __restrict__ tf, T
   rc[idx3(gc, I, J, K)] = acc;
 }
 
+// The same restriction for a level whose z axis is halved (taps 2K - 1, 2K,
+// 2K + 1): a thread marches its (I, J) column over NNZ_KC coarse planes and
+// forms the x-y sum of each fine plane once, so that coarse planes K and
+// K + 1 share the sum of fine plane 2K + 1.  Each coarse value is the same
+// expression in the same order as k_restrict_nn's: the results are identical.
+constexpr int NNZ_KC = 8;
+template <class T>
+__global__ void __launch_bounds__(256) k_restrict_nnz(const T* __restrict__ tf, T* __restrict__ rc, Grid gf,
+                                                      Grid gc, NNXfer<T> nn, const SolveCtrl* ctrl) {
+  pdl_enter();
+  if (ctrl->done) return;
+  const int I = blockIdx.x * blockDim.x + threadIdx.x;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y;
+  const int K0 = blockIdx.z * NNZ_KC, K1 = min(K0 + NNZ_KC, gc.nz);
+  if (I >= gc.nx || J >= gc.ny) return;
+  int xi[NN_MAXT], yi[NN_MAXT];
+  T xw[NN_MAXT], yw[NN_MAXT];
+  const int nxt = restrict_taps<T>(I, gf.nx, gc.nx, gf.bc[0], nn.c[0], nn.wsc[0], xi, xw);
+  const int nyt = restrict_taps<T>(J, gf.ny, gc.ny, gf.bc[1], nn.c[1], nn.wsc[1], yi, yw);
+  auto plane = [&](int k) {
+    T accy = (T)0;
+    for (int b = 0; b < nyt; ++b) {
+      const T* row = tf + gf.sz() * k + gf.sy() * yi[b];
+      T accx = (T)0;
+      for (int q = 0; q < nxt; ++q) accx += xw[q] * __ldg(row + xi[q]);
+      accy += yw[b] * accx;
+    }
+    return accy;
+  };
+  T s0 = plane(fine_of(K0, -1, gf.nz, gf.bc[2], 1));
+  for (int K = K0; K < K1; ++K) {
+    const T s1 = plane(fine_of(K, 0, gf.nz, gf.bc[2], 1));
+    const T s2 = plane(fine_of(K, 1, gf.nz, gf.bc[2], 1));
+    T acc = (T)0;
+    acc += (T)0.25 * s0;
+    acc += (T)0.5 * s1;
+    acc += (T)0.25 * s2;
+    rc[idx3(gc, I, J, K)] = acc;
+    s0 = s2;  // fine plane 2K + 1 is the first tap of coarse plane K + 1
+  }
+}
+
 // Prolongation unit of one axis: a coarse cell (fine 2u and 2u + 1) on a
 // halved axis, one fine point otherwise; its two coarse corners and, per
 // fine point, the weight of the second corner.
@@ -992,7 +1034,10 @@ static void launch_restrict(const MGLevel& L, const MGLevel& C, const T* tf, T* 
   Coarsen cz;
   for (int a = 0; a < 3; ++a) cz.c[a] = L.coarsen[a];
   const dim3 b(32, 8);
-  if (cz.c[0] == 2 || cz.c[1] == 2 || cz.c[2] == 2)
+  if ((cz.c[0] == 2 || cz.c[1] == 2) && cz.c[2] == 1)
+    launch_pdl(k_restrict_nnz<T>, dim3((C.g.nx + 31) / 32, (C.g.ny + 7) / 8, (C.g.nz + NNZ_KC - 1) / NNZ_KC), b, 0,
+               s, tf, rc, L.g, C.g, nn_xfer<T>(L, C), ctrl);
+  else if (cz.c[0] == 2 || cz.c[1] == 2 || cz.c[2] == 2)
     launch_pdl(k_restrict_nn<T>, g3(C.g), b, 0, s, tf, rc, L.g, C.g, nn_xfer<T>(L, C), ctrl);
   else if (cz.c[0] && cz.c[1] && cz.c[2])
     launch_pdl(k_restrict_full<T>, g3(C.g), b, 0, s, tf, rc, L.g, C.g, ctrl);
