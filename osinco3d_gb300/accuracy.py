@@ -70,10 +70,18 @@ def main():
     ap.add_argument("--nz", type=int, default=256)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--eps", type=float, default=1e-8)
+    ap.add_argument("--guess", choices=["previous", "extrapolated", "extrapolated2"], default="previous",
+                    help="initial guess of every pressure solve (both runs)")
+    ap.add_argument("--pre", type=int, default=0, help="multigrid pre-smoothing sweeps (0: the default)")
+    ap.add_argument("--post", type=int, default=0, help="multigrid post-smoothing sweeps (0: the default)")
+    ap.add_argument("--mg-omega", type=float, default=0.0, help="smoother relaxation (0: the default)")
     ap.add_argument("--mixed-only", action="store_true",
                     help="run the mixed method alone (for a launch list of its step) and print its timing")
     args = ap.parse_args()
-    mg = dict(solver=o3d.SOLVER_MG, eps=args.eps, kmax=200)
+    guess = {"previous": o3d.GUESS_PREVIOUS, "extrapolated": o3d.GUESS_EXTRAPOLATED,
+             "extrapolated2": o3d.GUESS_EXTRAPOLATED2}[args.guess]
+    mg = dict(solver=o3d.SOLVER_MG, eps=args.eps, kmax=200, guess=guess, mg_pre=args.pre, mg_post=args.post,
+              mg_omega=args.mg_omega)
     if args.case == "mixing":
         p64 = o3d.mixing_layer_params(args.nx, args.ny, args.nz, precision=o3d.PREC_FP64, **mg)
         pmx = o3d.mixing_layer_params(args.nx, args.ny, args.nz, precision=o3d.PREC_MIXED, **mg)
