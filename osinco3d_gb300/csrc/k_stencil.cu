@@ -304,8 +304,17 @@ void launch_stats(const T* ux, const T* uy, const T* uz, const Grid& g, const Co
 }
 template <class T>
 void launch_transeq(const ScalArgs<T>& a, const double* sums, cudaStream_t s, long long* nl) {
-  launch_pdl(k_transeq<T>, tq_grid(a.g), dim3(32, 8), 0, s, a);
-  launch_finalize(a.part, tq_blocks(a.g), 3, 0ull, (double*)sums, s);
+  long long nblk = tq_blocks(a.g);
+  bool two_point = false;
+  if constexpr (sizeof(T) == 4) {
+    if (stencil_v_ok(a.g)) {
+      launch_transeq_v(a, s);
+      nblk = transeq_v_blocks(a.g);
+      two_point = true;
+    }
+  }
+  if (!two_point) launch_pdl(k_transeq<T>, tq_grid(a.g), dim3(32, 8), 0, s, a);
+  launch_finalize(a.part, nblk, 3, 0ull, (double*)sums, s);
   // a grid-stride loop over at most 8 blocks of 256 threads per SM
   const long long want = (a.g.n + 255) / 256;
   launch_pdl(k_scalar_redistribute<T>, (unsigned)(want < 152 * 8 ? want : 152 * 8), 256, 0, s, a.phi_out, a.g.n,

@@ -9,7 +9,9 @@
 //                  function_stats (src/functions.f90:27-63), optionally the
 //                  Poisson rhs and its trapezoid-weighted sums;
 //   k_correct25v   correct_velocity (src/integration.f90:297-325) with the
-//                  extrema of the corrected velocity.
+//                  extrema of the corrected velocity;
+//   k_transeq25v   transeq (src/integration.f90:405-447): the scalar's flux,
+//                  AB update, first clipping pass and clipping sums.
 //
 // A block of 32 x 8 threads owns a 64 x 8 tile of (x, y) points and marches
 // along z over a chunk of planes; thread (tx, ty) computes points
@@ -794,6 +796,175 @@ __global__ void __launch_bounds__(NT, 3) k_correct25v(CorrArgs<float, double> A,
   block_reduce_store_t<float, 10>(r, ops, A.part, block_linear_id());
 }
 
+// ---------------------------------------------------------------------------
+// transeq for the mixed method (src/integration.f90:405-447): the scalar flux,
+// its AB update and the first clipping pass, with the three clipping sums of
+// the reference (phi before clipping, after clipping, and the weights
+// min(phi, 1 - phi)) accumulated per thread in TwoSum-compensated FP32 pairs
+// and widened once for the block reduction.  The scalar's plane lands in a
+// ring stage of 14 rows x 72 columns (it is even in every axis: no sign
+// fixes); u, v, w, nu_t, the source and the flux history come through
+// registers, one plane ahead.
+// ---------------------------------------------------------------------------
+constexpr int TS = VR * VW;        // floats per stage
+constexpr int TUNIT = VR * NCH;    // 224 chunk units
+struct TRing {
+  float s[ZQ][TS];
+};
+
+template <bool LES, bool ZON, bool XO>
+__global__ void __launch_bounds__(NT, 3) k_transeq25v(ScalArgs<float> A, int kc) {
+  pdl_enter();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  TRing& sm = *reinterpret_cast<TRing*>(smem_raw);
+  const Grid& g = A.g;
+  const int tx = threadIdx.x, ty = threadIdx.y, t = ty * VTX + tx;
+  const int i0 = blockIdx.x * VX, j0 = blockIdx.y * VY;
+  const int ia = i0 + 2 * tx, j = j0 + ty;
+  const bool valid = ia < g.nx && j < g.ny;
+  const int k0 = blockIdx.z * kc;
+  const int np = min(kc, g.nz - k0);
+  constexpr bool zon = ZON;
+  const int pca = XO ? xclass(g, ia) : 0, pcb = XO ? xclass(g, ia + 1) : 0;
+  const long long sz = g.sz();
+  const long long out0 = valid ? (long long)ia + (long long)g.nx * j : 0;
+  const int last_centre = zon ? np + 2 : np - 1;
+  const unsigned ring0 = smem_u32(&sm.s[0][0]);
+
+  const Unit un = t < TUNIT ? unit_of(g, i0, j0, t / NCH, t % NCH, (t / NCH) * VW + 4 + 4 * (t % NCH), 0, false,
+                                      t / NCH >= 3 && t / NCH < 3 + VY)
+                            : unit_none();
+  const bool has_x = t < VY * 6;
+  const XCell xc = xcell_of(g, i0, j0, has_x ? t / 6 : 0, t % 6, (3 + (has_x ? t / 6 : 0)) * VW);
+
+  auto issue = [&](int lp, int st) {
+    if (lp <= last_centre) {
+      const ZPlane z = z_plane(g, k0 + lp);
+      const unsigned sbase = ring0 + (unsigned)(st * TS) * 4u;
+      const bool full = lp < np;
+      if ((un.flags & 1) && (full || (un.flags & 4))) issue_unit(un, A.phi, z, g, sbase);
+      if (full && has_x) cp4(sbase + (unsigned)xc.dst * 4u, A.phi + z.off + xc.xy);
+    }
+    cp_async_commit();
+  };
+
+  const int own = (ty + 3) * VW + 4 + 2 * tx;
+  float2 q[ZQ];
+#pragma unroll
+  for (int m = 0; m < ZQ; ++m) q[m] = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int lp = 0; lp < PD + 3; ++lp) issue(lp, lp);
+  if constexpr (zon) {
+    bool fxa, fxb, fyy;
+    const int iia = ghost(ia, g.nx, g.bc[0], &fxa), iib = ghost(ia + 1, g.nx, g.bc[0], &fxb);
+    const int jj = ghost(j, g.ny, g.bc[1], &fyy);
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      const float* f = A.phi + z_plane(g, k0 - 3 + m).off + (long long)g.nx * jj;
+      q[m] = make_float2(__ldg(f + iia), __ldg(f + iib));
+    }
+  }
+  // the per-point inputs of a plane: u, v, w, then nu_t, src, f2, f3
+  float2 in[7];
+  auto load_in = [&](long long p) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) in[a] = ld_stream2(A.u[a] + p);
+    in[3] = LES ? ld_stream2(A.nu_t + p) : make_float2(0.f, 0.f);
+    in[4] = ld_stream2(A.src + p);
+    in[5] = A.f2 ? ld_stream2(A.f2 + p) : make_float2(0.f, 0.f);
+    in[6] = A.f3 ? ld_stream2(A.f3 + p) : make_float2(0.f, 0.f);
+  };
+  if (valid && np > 0) load_in(out0 + sz * k0);
+  cp_async_wait<PD>();
+  __syncthreads();
+  if constexpr (zon) {
+#pragma unroll
+    for (int m = 0; m < 3; ++m) q[3 + m] = lds2(&sm.s[m][own]);
+  }
+  float s_hi[3] = {0.f, 0.f, 0.f}, s_lo[3] = {0.f, 0.f, 0.f};
+#pragma unroll 1
+  for (int lp = 0; lp < np; ++lp) {
+    cp_async_wait<PD - 1>();
+    __syncthreads();
+    issue(lp + 3 + PD, (lp + 3 + PD) % ZQ);
+    const float* s = sm.s[lp % ZQ];
+    if constexpr (zon) q[6] = lds2(&sm.s[(lp + 3) % ZQ][own]);
+    float w[10];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      const float2 p2 = lds2(&s[own - 4 + 2 * m]);
+      w[2 * m] = p2.x;
+      w[2 * m + 1] = p2.y;
+    }
+    float d1a[3], d1b[3], d2a[3], d2b[3];
+    d1a[0] = d1x<XO>(w + 1, A.cf.ax[0], pca);
+    d2a[0] = d2x<XO>(w + 1, A.cf.ax[0], pca);
+    d1b[0] = d1x<XO>(w + 2, A.cf.ax[0], pcb);
+    d2b[0] = d2x<XO>(w + 2, A.cf.ax[0], pcb);
+    float va[7], vb[7];
+#pragma unroll
+    for (int m = 0; m < 7; ++m) {
+      const float2 p2 = lds2(&s[own + (m - 3) * VW]);
+      va[m] = p2.x;
+      vb[m] = p2.y;
+    }
+    d1a[1] = d1(va, A.cf.ax[1]);
+    d2a[1] = d2(va, A.cf.ax[1]);
+    d1b[1] = d1(vb, A.cf.ax[1]);
+    d2b[1] = d2(vb, A.cf.ax[1]);
+    d1a[2] = d2a[2] = d1b[2] = d2b[2] = 0.f;
+    if constexpr (zon) {
+#pragma unroll
+      for (int m = 0; m < 7; ++m) {
+        va[m] = q[m].x;
+        vb[m] = q[m].y;
+      }
+      d1a[2] = d1(va, A.cf.ax[2]);
+      d2a[2] = d2(va, A.cf.ax[2]);
+      d1b[2] = d1(vb, A.cf.ax[2]);
+      d2b[2] = d2(vb, A.cf.ax[2]);
+#pragma unroll
+      for (int m = 0; m < ZQ - 1; ++m) q[m] = q[m + 1];
+    }
+    if (valid) {
+      const long long p = out0 + sz * (k0 + lp);
+      const float pc[2] = {w[4], w[5]};
+      const int cls[2] = {pca, pcb};
+      float Fo[2], co[2];
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const float* d1v = e ? d1b : d1a;
+        const float* d2v = e ? d2b : d2a;
+        const float uu = e ? in[0].y : in[0].x, vv = e ? in[1].y : in[1].x, ww = e ? in[2].y : in[2].x;
+        float alpha = A.alpha0;
+        if (LES) alpha = alpha + (e ? in[3].y : in[3].x) / A.sc;
+        const float F = alpha * (d2v[0] + d2v[1] + d2v[2]) - (uu * d1v[0] + vv * d1v[1] + ww * d1v[2]) +
+                        (e ? in[4].y : in[4].x);
+        float ph = pc[e] + A.adu * F;
+        if (A.f2) ph = ph + A.bdu * (e ? in[5].y : in[5].x);
+        if (A.f3) ph = ph + A.cdu * (e ? in[6].y : in[6].x);
+        if (XO && cls[e] == 1) ph = pc[e];  // open x axis: the inflow value is held
+        const float cl = fmaxf(0.f, fminf(1.f, ph));
+        const float wt = (XO && cls[e] == 1) ? 0.f : fminf(cl, 1.f - cl);  // held inflow nodes take no excess
+        two_sum_acc(s_hi[0], s_lo[0], ph);
+        two_sum_acc(s_hi[1], s_lo[1], cl);
+        two_sum_acc(s_hi[2], s_lo[2], wt);
+        Fo[e] = F;
+        co[e] = cl;
+      }
+      __stcs(reinterpret_cast<float2*>(A.fnew + p), make_float2(Fo[0], Fo[1]));
+      __stcs(reinterpret_cast<float2*>(A.phi_out + p), make_float2(co[0], co[1]));
+      if (lp + 1 < np) load_in(p + sz);
+    }
+  }
+  cp_async_wait<0>();
+  double r[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) r[c] = to_t<double>(s_hi[c]) + to_t<double>(s_lo[c]);
+  const int ops[3] = {RED_SUM, RED_SUM, RED_SUM};
+  block_reduce_store<3>(r, ops, A.part, block_linear_id());
+}
+
 dim3 v_grid(const Grid& g, int kc) {
   return dim3((g.nx + VX - 1) / VX, (g.ny + VY - 1) / VY, (g.nz + kc - 1) / kc);
 }
@@ -825,6 +996,15 @@ void correct_v_launch(const CorrArgs<float, double>& a, cudaStream_t s) {
   allow_smem_v(k_correct25v<ZON, XO>, bytes, attr);
   const int kc = v_chunk(a.g, 3);
   launch_pdl(k_correct25v<ZON, XO>, v_grid(a.g, kc), dim3(VTX, VTY), bytes, s, a, kc);
+}
+
+template <bool LES, bool ZON, bool XO>
+void transeq_v_launch(const ScalArgs<float>& a, cudaStream_t s) {
+  constexpr size_t bytes = sizeof(TRing);
+  static std::atomic<bool> attr[64];
+  allow_smem_v(k_transeq25v<LES, ZON, XO>, bytes, attr);
+  const int kc = v_chunk(a.g, 3);
+  launch_pdl(k_transeq25v<LES, ZON, XO>, v_grid(a.g, kc), dim3(VTX, VTY), bytes, s, a, kc);
 }
 
 }  // namespace
@@ -893,5 +1073,20 @@ long long div_v_blocks(const Grid& g) {
   return (long long)((g.nx + VX - 1) / VX) * ((g.ny + VY - 1) / VY) * ((g.nz + kc - 1) / kc);
 }
 long long corr_v_blocks(const Grid& g) { return div_v_blocks(g); }
+
+void launch_transeq_v(const ScalArgs<float>& a, cudaStream_t s) {
+  const bool zon = a.g.bc[2] != AX_ZERO, xo = a.g.bc[0] == AX_OPEN;
+#define TV(L, Z, X) transeq_v_launch<L, Z, X>(a, s)
+  if (a.les) {
+    if (zon) { if (xo) TV(true, true, true); else TV(true, true, false); }
+    else { if (xo) TV(true, false, true); else TV(true, false, false); }
+  } else {
+    if (zon) { if (xo) TV(false, true, true); else TV(false, true, false); }
+    else { if (xo) TV(false, false, true); else TV(false, false, false); }
+  }
+#undef TV
+}
+// the transport kernel runs with the divergence's tiling
+long long transeq_v_blocks(const Grid& g) { return div_v_blocks(g); }
 
 }  // namespace o3d

@@ -87,6 +87,8 @@ void launch_div_v(const float* fx, const float* fy, const float* fz, O* out, con
 void launch_correct_v(const CorrArgs<float, double>& a, cudaStream_t s);
 long long div_v_blocks(const Grid& g);
 long long corr_v_blocks(const Grid& g);
+void launch_transeq_v(const ScalArgs<float>& a, cudaStream_t s);
+long long transeq_v_blocks(const Grid& g);
 // planes per block of the two-point kernels for `per_sm` resident blocks
 int v_chunk(const Grid& g, int per_sm);
 template <class T>
