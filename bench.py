@@ -298,10 +298,10 @@ KERNEL_BYTES = {
     "mg_up": (4 + 4 + 8 + 0.5 + 4 + 8, "k_mg_up<2,update> (prolongation + post-smoothing + p += e, finest)"),
     # read u* (3 x FP32), write the FP32 rhs (its trapezoid-weighted sums ride along)
     "rhs": (4 * 3 + 4, "k_div25v<float> (Poisson rhs, FP32, with its weighted sums)"),
-    # read u* (3 x FP32) and the FP64 pressure, write u (3 x FP32)
-    "correct": (4 * 6 + 8, "k_correct25v (FP64 pressure, FP32 velocity)"),
-    # read p (FP64) and the FP32 rhs, write r (FP32)
-    "resid64": (8 + 4 + 4, "k_resid25<float,float> (double-float residual, finest level)"),
+    # read u* (3 x FP32) and the pressure's FP32 high plane, write u (3 x FP32)
+    "correct": (4 * 6 + 4, "k_correct25vf (FP32 high plane of the pressure pair, FP32 velocity)"),
+    # read the pressure pair (2 x FP32) and the FP32 rhs, write r (FP32)
+    "resid64": (8 + 4 + 4, "k_resid25<float,float,pair> (double-float residual, finest level)"),
 }
 # the kernel the roofline entry describes: the finest level's fused
 # post-smoothing kernel, the largest single share of the step

@@ -253,8 +253,11 @@ O3D_API int o3d_save_fields(o3d_ctx *ctx, const char *path, double time);
 O3D_API int o3d_load_fields(o3d_ctx *ctx, const char *path, double *time);
 /* What the flow-state file lacks for an exact restart: the Adams-Bashforth
  * flux history of the velocity and the scalar, the previous pressure of the
- * extrapolated and learned guesses and the dynamic SOR omega.  With both
- * files, a restarted run continues bit for bit.  No counterpart in the
+ * extrapolated and learned guesses and the dynamic SOR omega; in the mixed
+ * multigrid method, which holds its pressures as double-float pairs of FP32
+ * values, also the current pressure as that pair (the FP64 value in the
+ * flow-state file may round it).  Load the history after the fields: with
+ * both files a restarted run continues bit for bit.  No counterpart in the
  * reference (its restart resets the history). */
 O3D_API int o3d_save_history(o3d_ctx *ctx, const char *path);
 O3D_API int o3d_load_history(o3d_ctx *ctx, const char *path);

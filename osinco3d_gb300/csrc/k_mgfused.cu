@@ -364,7 +364,7 @@ struct UpGeom {
 template <int S2, bool UPD>
 __global__ void __launch_bounds__(MF_NT, S2 == 2 ? 4 : 3)
     k_mg_up(const float* __restrict__ epre, const float* __restrict__ ecrs, const float* __restrict__ r,
-            float* __restrict__ eout, double* __restrict__ p, Grid gf, Grid gc, PoiCoef<float> c, float om, int kc,
+            float* __restrict__ eout, PPair p, Grid gf, Grid gc, PoiCoef<float> c, float om, int kc,
             SolveCtrl* ctrl) {
   pdl_enter();
   if (ctrl->done) return;
@@ -376,7 +376,8 @@ __global__ void __launch_bounds__(MF_NT, S2 == 2 ? 4 : 3)
   float* const E = (float*)mf_smem;
   float* const R = E + NE * PL;
   float* const CR = R + NR * PL;
-  double* const PR = (double*)((char*)mf_smem + ((G::floats * 4 + 15) / 16) * 16);
+  // the pressure ring: NP planes of the owned cells' high parts, then NP of their low parts
+  float* const PR = (float*)((char*)mf_smem + ((G::floats * 4 + 15) / 16) * 16);
   const int t = threadIdx.x;
   const int x0 = blockIdx.x * MF_FX, y0 = blockIdx.y * MF_FY;
   const int k0 = blockIdx.z * kc, k1 = min(k0 + kc, gf.nz);
@@ -429,7 +430,11 @@ __global__ void __launch_bounds__(MF_NT, S2 == 2 ? 4 : 3)
     if (UPD && P >= k0 && P < k1) {
 #pragma unroll
       for (int u = 0; u < NOWN; ++u)
-        if (own[u]) cp_async<8>(PR + ((P - k0 + 8) % NP) * MF_OWN + t + u * MF_NT, p + oq[u] + gf.sz() * P);
+        if (own[u]) {
+          const int slot = ((P - k0 + 8) % NP) * MF_OWN + t + u * MF_NT;
+          cp_async<4>(PR + slot, p.hi + oq[u] + gf.sz() * P);
+          cp_async<4>(PR + NP * MF_OWN + slot, p.lo + oq[u] + gf.sz() * P);
+        }
     }
   };
   const int tau0 = k0 - S2, tau1 = k1 - 1 + S2;
@@ -500,7 +505,7 @@ __global__ void __launch_bounds__(MF_NT, S2 == 2 ? 4 : 3)
     const int Po = tau - S2;
     if (Po >= k0) {
       const float* Ef = E + rsub<NE>(sE, S2) * PL;
-      const double* Pf = PR + ((Po - k0 + 8) % NP) * MF_OWN;
+      const float* Pf = PR + ((Po - k0 + 8) % NP) * MF_OWN;
 #pragma unroll
       for (int u = 0; u < NOWN; ++u) {
         const int o = t + u * MF_NT;
@@ -508,8 +513,11 @@ __global__ void __launch_bounds__(MF_NT, S2 == 2 ? 4 : 3)
         const float ev = Ef[X::at(S2 + o % MF_FX, S2 + o / MF_FX)];
         const long long q = oq[u] + gf.sz() * Po;
         eout[q] = ev;
-        if (UPD) {
-          p[q] = Pf[o] + f32_to_f64(ev);
+        if (UPD) {  // p += e on the double-float pair, in the order of k_update
+          float ph = Pf[o], pl = Pf[NP * MF_OWN + o];
+          df_add_f(ph, pl, ev);
+          p.hi[q] = ph;
+          p.lo[q] = pl;
           emax = fmaxf(emax, fabsf(ev));
         }
       }
@@ -618,8 +626,9 @@ void launch_mg_up(const MGLevel& L, const MGLevel& C, float om, int post, double
   const float* ec = (const float*)C.e;
   const float* r = (const float*)L.r;
   float* eout = (float*)L.e;
+  const PPair pp = p ? ppair(p, L.g.n) : PPair{nullptr, nullptr};
 #define MF_UP(S2, U) \
-  launch_pdl(k_mg_up<S2, U>, grid, MF_NT, up_smem<S2>(), s, epre, ec, r, eout, p, L.g, C.g, c, om, kc, ctrl)
+  launch_pdl(k_mg_up<S2, U>, grid, MF_NT, up_smem<S2>(), s, epre, ec, r, eout, pp, L.g, C.g, c, om, kc, ctrl)
   if (post == 1) {
     if (p) MF_UP(2, true);
     else MF_UP(2, false);

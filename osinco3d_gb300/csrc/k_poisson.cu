@@ -315,15 +315,37 @@ struct RzVal<true> {
   static __device__ __forceinline__ DF of(float x) { return DF{x, 0.f}; }
 };
 
-template <class T, class R, bool MAX>
-__global__ void __launch_bounds__(RZ_TX * RZ_TY) k_resid25(const double* __restrict__ p, const R* __restrict__ rhs,
-                                                           T* __restrict__ r0, Grid g, PoiCoef<double> c,
-                                                           PoiDF cdf, SolveCtrl* ctrl, int shift) {
+// PP: the pressure is the double-float pair pp (the mixed multigrid method's
+// layout): its values are loaded as (hi, lo) and need no split.
+template <bool PP>
+struct RzRaw {
+  using type = double;
+};
+template <>
+struct RzRaw<true> {
+  using type = float2;
+};
+
+template <class T, class R, bool MAX, bool PP>
+__global__ void __launch_bounds__(RZ_TX * RZ_TY) k_resid25(const double* __restrict__ p, PPair pp,
+                                                           const R* __restrict__ rhs, T* __restrict__ r0, Grid g,
+                                                           PoiCoef<double> c, PoiDF cdf, SolveCtrl* ctrl,
+                                                           int shift) {
   pdl_enter();
   if (ctrl->done) return;
   constexpr bool DFP = sizeof(T) == 4;
+  static_assert(DFP || !PP, "the double-float pressure pair is the mixed method's");
   using Cv = RzVal<DFP>;
   using V = typename Cv::V;
+  using Raw = typename RzRaw<PP>::type;
+  auto ldr = [&](long long q) -> Raw {
+    if constexpr (PP) return make_float2(__ldg(pp.hi + q), __ldg(pp.lo + q));
+    else return __ldg(p + q);
+  };
+  auto cvt = [&](Raw x) -> V {
+    if constexpr (PP) return DF{x.x, x.y};
+    else return Cv::of(x);
+  };
   constexpr int TX = RZ_TX, TY = RZ_TY, SW = TX + 2;
   __shared__ V tile[2][(TY + 2) * SW];
   const int tx = threadIdx.x, ty = threadIdx.y, t = ty * TX + tx;
@@ -353,20 +375,20 @@ __global__ void __launch_bounds__(RZ_TX * RZ_TY) k_resid25(const double* __restr
 
   // loads run one plane ahead and stay raw until they are used, so that the
   // split of a value never waits on a load issued in the same plane step
-  V pb = Cv::of(__ldg(p + zoff(k0 - 1) + cxy)), pc = Cv::of(__ldg(p + zoff(k0) + cxy));
-  double ptraw = __ldg(p + zoff(k0 + 1) + cxy);
-  double hv = hon ? __ldg(p + zoff(k0) + hxy) : 0.0;
+  V pb = cvt(ldr(zoff(k0 - 1) + cxy)), pc = cvt(ldr(zoff(k0) + cxy));
+  Raw ptraw = ldr(zoff(k0 + 1) + cxy);
+  Raw hv = hon ? ldr(zoff(k0) + hxy) : Raw{};
   R rr = valid ? __ldg(rhs + out0 + sz * k0) : (R)0;
   float m = 0.f;
   int buf = 0;
   for (int k = k0; k < k1; ++k) {
-    const V pt = Cv::of(ptraw);
+    const V pt = cvt(ptraw);
     tile[buf][sc] = pc;
-    if (hon) tile[buf][hidx] = Cv::of(hv);
+    if (hon) tile[buf][hidx] = cvt(hv);
     const R rcur = rr;
     if (k + 1 < k1) {
-      ptraw = __ldg(p + zoff(k + 2) + cxy);
-      if (hon) hv = __ldg(p + zoff(k + 1) + hxy);
+      ptraw = ldr(zoff(k + 2) + cxy);
+      if (hon) hv = ldr(zoff(k + 1) + hxy);
       if (valid) rr = __ldg(rhs + out0 + sz * (k + 1));
     }
     __syncthreads();
@@ -404,8 +426,8 @@ __global__ void __launch_bounds__(RZ_TX * RZ_TY) k_resid25(const double* __restr
 
 // max |rhs - A p| after a solve (less the rhs mean when shift: the mixed
 // multigrid solve leaves the rhs unshifted)
-template <class R>
-__global__ void __launch_bounds__(256) k_resid_inf(const double* __restrict__ p, const R* __restrict__ rhs,
+template <class R, bool PP>
+__global__ void __launch_bounds__(256) k_resid_inf(const double* __restrict__ p, PPair pp, const R* __restrict__ rhs,
                                                    Grid g, PoiCoef<double> c, SolveCtrl* ctrl, int shift) {
   pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -414,7 +436,15 @@ __global__ void __launch_bounds__(256) k_resid_inf(const double* __restrict__ p,
   double d = 0.0;
   if (i < g.nx && j < g.ny) {
     const long long q = (long long)i + g.sy() * j + g.sz() * k;
-    const double ap = lap_nb<double>(p, g, i, j, k, c) + c.A * p[q];
+    double ap;
+    if constexpr (PP) {  // the pair's value hi + lo, exact in FP64
+      auto v = [&](long long o) { return f32_to_f64(pp.hi[o]) + f32_to_f64(pp.lo[o]); };
+      const Nb6 o = nb6(g, i, j, k);
+      ap = c.ox * (v(q + o.xm) + v(q + o.xp)) + c.oy * (v(q + o.ym) + v(q + o.yp)) +
+           c.oz * (v(q + o.zm) + v(q + o.zp)) + c.A * v(q);
+    } else {
+      ap = lap_nb<double>(p, g, i, j, k, c) + c.A * p[q];
+    }
     d = fabs((to_t<double>(rhs[q]) - (shift ? ctrl->rhs_mean : 0.0)) - ap);
   }
   const double bm = block_max(d);
@@ -968,9 +998,10 @@ static inline int coarse_threads(const Grid& g) {
 // the only FP64 work is the addition itself.
 constexpr int UPD_PER = 8;
 
-template <class T>
-__global__ void __launch_bounds__(256) k_update(double* __restrict__ p, const T* __restrict__ e, long long n,
-                                                SolveCtrl* ctrl) {
+// PP: p is the double-float pair pp, updated by df_add_f (no FP64 operation)
+template <class T, bool PP>
+__global__ void __launch_bounds__(256) k_update(double* __restrict__ p, PPair pp, const T* __restrict__ e,
+                                                long long n, SolveCtrl* ctrl) {
   pdl_enter();
   if (ctrl->done) return;
   const long long base = (long long)blockIdx.x * blockDim.x * UPD_PER + threadIdx.x;
@@ -980,7 +1011,14 @@ __global__ void __launch_bounds__(256) k_update(double* __restrict__ p, const T*
     const long long q = base + (long long)u * blockDim.x;
     if (q < n) {
       const T ev = e[q];
-      p[q] += to_t<double>(ev);
+      if constexpr (PP) {
+        float h = pp.hi[q], l = pp.lo[q];
+        df_add_f(h, l, (float)ev);
+        pp.hi[q] = h;
+        pp.lo[q] = l;
+      } else {
+        p[q] += to_t<double>(ev);
+      }
       m = fmax(m, fabs(ev));
     }
   }
@@ -1115,13 +1153,15 @@ static bool vcycle(MGLevel* lv, int l, int nlev, int pre, int post, int coarse_s
 
 // One outer iteration of the defect-correction loop, in two parts.
 // launch_mg_resid: r0 = rhs - mean - A p in FP64 (stored in T) with max |r0|.
+// In the mixed method (T = float) p is the double-float pair buffer.
 template <class T, class R>
 void launch_mg_resid(double* p, const R* rhs, MGLevel* lv, SolveCtrl* ctrl, cudaStream_t s, long long* nl) {
   const MGLevel& L0 = lv[0];
   PoiCoef<double> c64 = make_poi<double>(L0.h[0], L0.h[1], L0.h[2]);
   // the mixed method subtracts the rhs mean here; the FP64 method's rhs was shifted in place
-  launch_pdl(k_resid25<T, R, true>, rz_grid(L0.g), dim3(RZ_TX, RZ_TY), 0, s, p, rhs, (T*)L0.r, L0.g, c64,
-             poi_df(c64), ctrl, (int)(sizeof(T) == 4));
+  constexpr bool PP = sizeof(T) == 4;
+  launch_pdl(k_resid25<T, R, true, PP>, rz_grid(L0.g), dim3(RZ_TX, RZ_TY), 0, s, p, ppair(p, L0.g.n), rhs,
+             (T*)L0.r, L0.g, c64, poi_df(c64), ctrl, (int)(sizeof(T) == 4));
   *nl += 1;
 }
 
@@ -1136,9 +1176,9 @@ void launch_mg_cycles(double* p, MGLevel* lv, int nlev, int pre, int post, int c
   for (int q = 0; q < cycles; ++q)
     updated = vcycle<T>(lv, 0, nlev, pre, post, coarse_sweeps, smooth_omega, ctrl, s, nl, q == 0 && !from_e,
                         q == cycles - 1 ? p : nullptr);
-  if (!updated) {
-    launch_pdl(k_update<T>, (unsigned)((L0.g.n + 256LL * UPD_PER - 1) / (256LL * UPD_PER)), 256, 0, s, p,
-               (const T*)L0.e, L0.g.n, ctrl);
+  if (!updated) {  // the mixed method's p is the double-float pair
+    launch_pdl(k_update<T, sizeof(T) == 4>, (unsigned)((L0.g.n + 256LL * UPD_PER - 1) / (256LL * UPD_PER)), 256, 0,
+               s, p, ppair(p, L0.g.n), (const T*)L0.e, L0.g.n, ctrl);
     *nl += 1;
   }
   launch_pdl(k_mg_control, 1, 1, 0, s, ctrl);
@@ -1162,8 +1202,18 @@ __global__ void k_extrapolate(double* __restrict__ p, double* __restrict__ pprev
   p[q] = 2.0 * pc - pprev[q];
   pprev[q] = pc;
 }
-void launch_extrapolate(double* p, double* pprev, long long n, cudaStream_t s) {
-  launch_pdl(k_extrapolate, (unsigned)((n + 255) / 256), 256, 0, s, p, pprev, n);
+// the same on double-float pairs
+__global__ void k_extrapolate_pp(PPair p, PPair pprev, long long n) {
+  pdl_enter();
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const DF pc = pp_load(p, q);
+  pp_store(p, q, df_add(df_scale(pc, 2.f), df_neg(pp_load(pprev, q))));
+  pp_store(pprev, q, pc);
+}
+void launch_extrapolate(double* p, double* pprev, long long n, cudaStream_t s, bool pair) {
+  if (pair) launch_pdl(k_extrapolate_pp, (unsigned)((n + 255) / 256), 256, 0, s, ppair(p, n), ppair(pprev, n), n);
+  else launch_pdl(k_extrapolate, (unsigned)((n + 255) / 256), 256, 0, s, p, pprev, n);
 }
 
 // p <- 3 p - 3 p_prev + p_prev2 (quadratic extrapolation in time), and the
@@ -1178,8 +1228,20 @@ __global__ void k_extrapolate2(double* __restrict__ p, const double* __restrict_
   p[q] = 3.0 * (pc - pprev[q]) + pprev2[q];
   pprev2[q] = pc;
 }
-void launch_extrapolate2(double* p, const double* pprev, double* pprev2, long long n, cudaStream_t s) {
-  launch_pdl(k_extrapolate2, (unsigned)((n + 255) / 256), 256, 0, s, p, pprev, pprev2, n);
+__global__ void k_extrapolate2_pp(PPair p, PPair pprev, PPair pprev2, long long n) {
+  pdl_enter();
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const DF pc = pp_load(p, q);
+  pp_store(p, q, df_add(df_scale(df_add(pc, df_neg(pp_load(pprev, q))), 3.f), pp_load(pprev2, q)));
+  pp_store(pprev2, q, pc);
+}
+void launch_extrapolate2(double* p, const double* pprev, double* pprev2, long long n, cudaStream_t s, bool pair) {
+  if (pair)
+    launch_pdl(k_extrapolate2_pp, (unsigned)((n + 255) / 256), 256, 0, s, ppair(p, n), ppair((void*)pprev, n),
+               ppair(pprev2, n), n);
+  else
+    launch_pdl(k_extrapolate2, (unsigned)((n + 255) / 256), 256, 0, s, p, pprev, pprev2, n);
 }
 
 // the same extrapolation, also writing the last increment d = p - p_prev in T
@@ -1192,6 +1254,16 @@ __global__ void k_extrapolate_d(double* __restrict__ p, double* __restrict__ ppr
   p[q] = 2.0 * pc - pv;
   pprev[q] = pc;
   d[q] = to_t<T>(pc - pv);
+}
+__global__ void k_extrapolate_d_pp(PPair p, PPair pprev, float* __restrict__ d, long long n) {
+  pdl_enter();
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const DF pc = pp_load(p, q), pv = pp_load(pprev, q);
+  const DF inc = df_add(pc, df_neg(pv));
+  pp_store(p, q, df_add(pc, inc));
+  pp_store(pprev, q, pc);
+  d[q] = inc.h + inc.l;
 }
 
 // ---------------------------------------------------------------------------
@@ -1288,6 +1360,13 @@ __global__ void k_pdiff(const double* __restrict__ p, const double* __restrict__
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q < n) d[q] = to_t<T>(p[q] - pprev[q]);
 }
+__global__ void k_pdiff_pp(PPair p, PPair pprev, float* __restrict__ d, long long n) {
+  pdl_enter();
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const DF v = df_add(pp_load(p, q), df_neg(pp_load(pprev, q)));
+  d[q] = v.h + v.l;
+}
 
 // p += e
 template <class T>
@@ -1316,8 +1395,16 @@ static T* restrict_to(MGLevel* lv, int ll, const T* f0, int which, SolveCtrl* ct
 
 // p <- p_ex, p_prev <- p, and the increment into the finest level's t
 template <class T>
-void launch_learn_extrapolate(double* p, double* pprev, MGLevel* lv, cudaStream_t s, long long* nl) {
-  launch_pdl(k_extrapolate_d<T>, b256(lv[0].g.n), 256, 0, s, p, pprev, (T*)lv[0].t, lv[0].g.n);
+void launch_learn_extrapolate(double* p, double* pprev, MGLevel* lv, cudaStream_t s, long long* nl, bool pair) {
+  const long long n = lv[0].g.n;
+  if constexpr (sizeof(T) == 4) {
+    if (pair) {
+      launch_pdl(k_extrapolate_d_pp, b256(n), 256, 0, s, ppair(p, n), ppair(pprev, n), (float*)lv[0].t, n);
+      *nl += 1;
+      return;
+    }
+  }
+  launch_pdl(k_extrapolate_d<T>, b256(n), 256, 0, s, p, pprev, (T*)lv[0].t, n);
   *nl += 1;
 }
 
@@ -1360,14 +1447,18 @@ template <class T>
 void launch_learn_target(const double* p, const double* pprev, MGLevel* lv, int ll, SolveCtrl* ctrl,
                          const float* ch1, float* tgt, cudaStream_t s, long long* nl) {
   const MGLevel& L0 = lv[0];
-  launch_pdl(k_pdiff<T>, b256(L0.g.n), 256, 0, s, p, pprev, (T*)L0.t, L0.g.n);
+  if constexpr (sizeof(T) == 4)  // training samples come from multigrid solves: the pair layout
+    launch_pdl(k_pdiff_pp, b256(L0.g.n), 256, 0, s, ppair((void*)p, L0.g.n), ppair((void*)pprev, L0.g.n),
+               (float*)L0.t, L0.g.n);
+  else
+    launch_pdl(k_pdiff<T>, b256(L0.g.n), 256, 0, s, p, pprev, (T*)L0.t, L0.g.n);
   const T* dc = restrict_to<T>(lv, ll, (const T*)L0.t, 1, ctrl, s, nl);
   launch_pdl(k_target<T>, 1, 1024, 0, s, dc, lv[ll].g.n, ctrl, ch1, tgt);
   *nl += 2;
 }
 
 #define O3D_LEARN_INST(T)                                                                                      \
-  template void launch_learn_extrapolate<T>(double*, double*, MGLevel*, cudaStream_t, long long*);             \
+  template void launch_learn_extrapolate<T>(double*, double*, MGLevel*, cudaStream_t, long long*, bool);       \
   template void launch_learn_features<T>(MGLevel*, int, SolveCtrl*, float*, cudaStream_t, long long*);         \
   template void launch_learn_apply<T>(double*, const float*, MGLevel*, int, bool, SolveCtrl*, cudaStream_t,    \
                                       long long*);                                                             \
@@ -1402,8 +1493,10 @@ void launch_rhs_wmean_final(const double* part, long long nblk, const Grid& g, S
 
 template <class R>
 void launch_residual_inf(const double* p, const R* rhs, const Grid& g, const PoiCoef<double>& c, SolveCtrl* ctrl,
-                         bool shift, cudaStream_t s) {
-  launch_pdl(k_resid_inf<R>, g3(g), dim3(32, 8), 0, s, p, rhs, g, c, ctrl, shift);
+                         bool shift, cudaStream_t s, bool pair) {
+  const PPair pp = ppair((void*)p, g.n);
+  if (pair) launch_pdl(k_resid_inf<R, true>, g3(g), dim3(32, 8), 0, s, p, pp, rhs, g, c, ctrl, (int)shift);
+  else launch_pdl(k_resid_inf<R, false>, g3(g), dim3(32, 8), 0, s, p, pp, rhs, g, c, ctrl, (int)shift);
 }
 template <class R>
 void launch_rhs_shift(R* rhs, long long n, SolveCtrl* ctrl, cudaStream_t s) {
@@ -1414,22 +1507,30 @@ template void launch_rhs_shift<double>(double*, long long, SolveCtrl*, cudaStrea
 
 template <class T, class R>
 void launch_level_kernel(int which, double* p, const R* rhs, const MGLevel& L, SolveCtrl* ctrl,
-                         cudaStream_t s) {
+                         cudaStream_t s, bool pair) {
   PoiCoef<T> c = make_poi<T>(L.h[0], L.h[1], L.h[2]);
   if (which == 0) {
     launch_pdl(k_smooth<T>, g3rb(L.g), dim3(32, 8), 0, s, (T*)L.e, (const T*)L.r, L.g, c, 0, (T)1, ctrl);
   } else {
     PoiCoef<double> c64 = make_poi<double>(L.h[0], L.h[1], L.h[2]);
-    launch_pdl(k_resid25<T, R, false>, rz_grid(L.g), dim3(RZ_TX, RZ_TY), 0, s, p, rhs, (T*)L.r, L.g, c64, poi_df(c64),
-                                                                       ctrl, 0);
+    const PPair pp = ppair(p, L.g.n);
+    if constexpr (sizeof(T) == 4) {
+      if (pair) {
+        launch_pdl(k_resid25<T, R, false, true>, rz_grid(L.g), dim3(RZ_TX, RZ_TY), 0, s, p, pp, rhs, (T*)L.r, L.g,
+                   c64, poi_df(c64), ctrl, 0);
+        return;
+      }
+    }
+    launch_pdl(k_resid25<T, R, false, false>, rz_grid(L.g), dim3(RZ_TX, RZ_TY), 0, s, p, pp, rhs, (T*)L.r, L.g, c64,
+               poi_df(c64), ctrl, 0);
   }
 }
 template void launch_level_kernel<float, double>(int, double*, const double*, const MGLevel&, SolveCtrl*,
-                                                 cudaStream_t);
+                                                 cudaStream_t, bool);
 template void launch_level_kernel<double, double>(int, double*, const double*, const MGLevel&, SolveCtrl*,
-                                                  cudaStream_t);
+                                                  cudaStream_t, bool);
 template void launch_level_kernel<float, float>(int, double*, const float*, const MGLevel&, SolveCtrl*,
-                                                cudaStream_t);
+                                                cudaStream_t, bool);
 
 template void launch_mg_outer<double, double>(double*, const double*, MGLevel*, int, int, int, int,
                                               double, int, SolveCtrl*, cudaStream_t, long long*);
@@ -1441,8 +1542,8 @@ template void launch_mg_resid<float, float>(double*, const float*, MGLevel*, Sol
 template void launch_rhs_wmean<double>(const double*, const Grid&, double*, SolveCtrl*, cudaStream_t, long long*);
 template void launch_rhs_wmean<float>(const float*, const Grid&, double*, SolveCtrl*, cudaStream_t, long long*);
 template void launch_residual_inf<double>(const double*, const double*, const Grid&, const PoiCoef<double>&,
-                                          SolveCtrl*, bool, cudaStream_t);
+                                          SolveCtrl*, bool, cudaStream_t, bool);
 template void launch_residual_inf<float>(const double*, const float*, const Grid&, const PoiCoef<double>&,
-                                         SolveCtrl*, bool, cudaStream_t);
+                                         SolveCtrl*, bool, cudaStream_t, bool);
 
 }  // namespace o3d

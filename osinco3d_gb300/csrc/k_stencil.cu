@@ -334,6 +334,38 @@ void launch_convert(const S* s_, D* d, long long n, cudaStream_t s) {
   launch_pdl(k_convert<S, D>, (unsigned)((n + 255) / 256), 256, 0, s, s_, d, n);
 }
 
+// FP64 field <-> double-float pair of FP32 planes: hi = RN32(x), lo =
+// RN32(x - hi), and back x = hi + lo (exact in FP64).  The conversions are
+// the hardware's, subnormals included, so that split(join(pair)) returns
+// every normalised pair (a pair hi = RN32(hi + lo)) unchanged at any
+// magnitude: a saved and reloaded pressure continues bit for bit.  (These
+// run at the API boundary only; the solver's kernels never split.)
+__global__ void k_split_pair(const double* __restrict__ x, float* __restrict__ hi, float* __restrict__ lo,
+                             long long n) {
+  pdl_enter();
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const double v = x[q];
+  const float h = (float)v;
+  hi[q] = h;
+  lo[q] = (float)(v - (double)h);
+}
+__global__ void k_join_pair(const float* __restrict__ hi, const float* __restrict__ lo, double* __restrict__ x,
+                            long long n) {
+  pdl_enter();
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  x[q] = (double)hi[q] + (double)lo[q];
+}
+void launch_split_pair(const double* x, void* pair, long long n, cudaStream_t s) {
+  const PPair p = ppair(pair, n);
+  launch_pdl(k_split_pair, (unsigned)((n + 255) / 256), 256, 0, s, x, p.hi, p.lo, n);
+}
+void launch_join_pair(const void* pair, double* x, long long n, cudaStream_t s) {
+  const PPair p = ppair((void*)pair, n);
+  launch_pdl(k_join_pair, (unsigned)((n + 255) / 256), 256, 0, s, (const float*)p.hi, (const float*)p.lo, x, n);
+}
+
 #define O3D_INST(T)                                                                            \
   template void launch_der<T>(const T*, T*, const Grid&, const AxisCoef<T>&, int, int, int,     \
                               cudaStream_t);                                                   \

@@ -688,7 +688,7 @@ static void correct_launch(const CorrArgs<T, S>& a, cudaStream_t s) {
 }
 template <class T, class S>
 void launch_correct(const CorrArgs<T, S>& a, cudaStream_t s) {
-  if constexpr (sizeof(T) == 4 && sizeof(S) == 8) {
+  if constexpr (sizeof(T) == 4) {
     if (stencil_v_ok(a.g)) {
       launch_correct_v(a, s);
       return;
@@ -715,5 +715,6 @@ template void launch_div<float, double>(const float*, const float*, const float*
                                         const Coef3<float>&, int, float, int, StatPart*, cudaStream_t, double*, int);
 template void launch_correct<double, double>(const CorrArgs<double, double>&, cudaStream_t);
 template void launch_correct<float, double>(const CorrArgs<float, double>&, cudaStream_t);
+template void launch_correct<float, float>(const CorrArgs<float, float>&, cudaStream_t);
 
 }  // namespace o3d

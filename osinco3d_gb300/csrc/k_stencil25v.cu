@@ -965,6 +965,150 @@ __global__ void __launch_bounds__(NT, 3) k_transeq25v(ScalArgs<float> A, int kc)
   block_reduce_store<3>(r, ops, A.part, block_linear_id());
 }
 
+// ---------------------------------------------------------------------------
+// correction with an FP32 pressure: the high plane of the mixed multigrid
+// method's double-float pair (the FP32 rounding of the FP64 pressure, the
+// value the FP64-pressure kernel above converts to).  Its planes land in a
+// ring of 7 single-field stages of 14 rows x 72 columns, as the scalar's in
+// k_transeq25v, with no conversion pass.
+// ---------------------------------------------------------------------------
+template <bool ZON, bool XO>
+__global__ void __launch_bounds__(NT, 3) k_correct25vf(CorrArgs<float, float> A, int kc) {
+  pdl_enter();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  TRing& sm = *reinterpret_cast<TRing*>(smem_raw);
+  const Grid& g = A.g;
+  const int tx = threadIdx.x, ty = threadIdx.y, t = ty * VTX + tx;
+  const int i0 = blockIdx.x * VX, j0 = blockIdx.y * VY;
+  const int ia = i0 + 2 * tx, j = j0 + ty;
+  const bool valid = ia < g.nx && j < g.ny;
+  const int k0 = blockIdx.z * kc;
+  const int np = min(kc, g.nz - k0);
+  constexpr bool zon = ZON;
+  const int pca = XO ? xclass(g, ia) : 0, pcb = XO ? xclass(g, ia + 1) : 0;
+  const long long sz = g.sz();
+  const long long out0 = valid ? (long long)ia + (long long)g.nx * j : 0;
+  const int last_centre = zon ? np + 2 : np - 1;
+  const unsigned ring0 = smem_u32(&sm.s[0][0]);
+
+  const Unit un = t < TUNIT ? unit_of(g, i0, j0, t / NCH, t % NCH, (t / NCH) * VW + 4 + 4 * (t % NCH), 0, false,
+                                      t / NCH >= 3 && t / NCH < 3 + VY)
+                            : unit_none();
+  const bool has_x = t < VY * 6;
+  const XCell xc = xcell_of(g, i0, j0, has_x ? t / 6 : 0, t % 6, (3 + (has_x ? t / 6 : 0)) * VW);
+
+  auto issue = [&](int lp, int st) {
+    if (lp <= last_centre) {
+      const ZPlane z = z_plane(g, k0 + lp);
+      const unsigned sbase = ring0 + (unsigned)(st * TS) * 4u;
+      const bool full = lp < np;
+      if ((un.flags & 1) && (full || (un.flags & 4))) issue_unit(un, A.p, z, g, sbase);
+      if (full && has_x) cp4(sbase + (unsigned)xc.dst * 4u, A.p + z.off + xc.xy);
+    }
+    cp_async_commit();
+  };
+
+  const int own = (ty + 3) * VW + 4 + 2 * tx;
+  float2 q[ZQ];
+#pragma unroll
+  for (int m = 0; m < ZQ; ++m) q[m] = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int lp = 0; lp < PD + 3; ++lp) issue(lp, lp);
+  if constexpr (zon) {
+    bool fxa, fxb, fyy;
+    const int iia = ghost(ia, g.nx, g.bc[0], &fxa), iib = ghost(ia + 1, g.nx, g.bc[0], &fxb);
+    const int jj = ghost(j, g.ny, g.bc[1], &fyy);
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      const float* f = A.p + z_plane(g, k0 - 3 + m).off + (long long)g.nx * jj;
+      q[m] = make_float2(__ldg(f + iia), __ldg(f + iib));
+    }
+  }
+  float2 us[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) us[a] = (valid && np > 0) ? ld_stream2(A.up[a] + out0 + sz * k0) : make_float2(0.f, 0.f);
+  cp_async_wait<PD>();
+  __syncthreads();
+  if constexpr (zon) {
+#pragma unroll
+    for (int m = 0; m < 3; ++m) q[3 + m] = lds2(&sm.s[m][own]);
+  }
+  float mn[3], mx[3], am[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) { mn[a] = INFINITY; mx[a] = -INFINITY; am[a] = 0.f; }
+  bool nan = false;
+#pragma unroll 1
+  for (int lp = 0; lp < np; ++lp) {
+    cp_async_wait<PD - 1>();
+    __syncthreads();
+    issue(lp + 3 + PD, (lp + 3 + PD) % ZQ);
+    const float* s = sm.s[lp % ZQ];
+    if constexpr (zon) q[6] = lds2(&sm.s[(lp + 3) % ZQ][own]);
+    float w[10];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      const float2 p2 = lds2(&s[own - 4 + 2 * m]);
+      w[2 * m] = p2.x;
+      w[2 * m + 1] = p2.y;
+    }
+    float ga[3], gb[3];
+    ga[0] = d1x<XO>(w + 1, A.cf.ax[0], pca);
+    gb[0] = d1x<XO>(w + 2, A.cf.ax[0], pcb);
+    float va[7], vb[7];
+#pragma unroll
+    for (int m = 0; m < 7; ++m) {
+      const float2 p2 = lds2(&s[own + (m - 3) * VW]);
+      va[m] = p2.x;
+      vb[m] = p2.y;
+    }
+    ga[1] = d1(va, A.cf.ax[1]);
+    gb[1] = d1(vb, A.cf.ax[1]);
+    ga[2] = gb[2] = 0.f;
+    if constexpr (zon) {
+#pragma unroll
+      for (int m = 0; m < 7; ++m) {
+        va[m] = q[m].x;
+        vb[m] = q[m].y;
+      }
+      ga[2] = d1(va, A.cf.ax[2]);
+      gb[2] = d1(vb, A.cf.ax[2]);
+#pragma unroll
+      for (int m = 0; m < ZQ - 1; ++m) q[m] = q[m + 1];
+    }
+    if (valid) {
+      const long long p = out0 + sz * (k0 + lp);
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        float na = us[a].x - A.dt * ga[a], nb = us[a].y - A.dt * gb[a];
+        if (XO) {  // inflow nodes keep their value
+          if (pca == 1) na = us[a].x;
+          if (pcb == 1) nb = us[a].y;
+        }
+        __stcs(reinterpret_cast<float2*>(A.u[a] + p), make_float2(na, nb));
+        if (na != na || nb != nb) nan = true;
+        mn[a] = fminf(mn[a], fminf(na, nb));
+        mx[a] = fmaxf(mx[a], fmaxf(na, nb));
+        am[a] = fmaxf(am[a], fmaxf(fabsf(na), fabsf(nb)));
+      }
+      if (lp + 1 < np) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) us[a] = ld_stream2(A.up[a] + p + sz);
+      }
+    }
+  }
+  cp_async_wait<0>();
+  float r[10];
+  const int ops[10] = {RED_MIN, RED_MIN, RED_MIN, RED_MAX, RED_MAX, RED_MAX, RED_MAX, RED_MAX, RED_MAX, RED_MAX};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    r[a] = mn[a];
+    r[3 + a] = mx[a];
+    r[6 + a] = am[a];
+  }
+  r[9] = nan ? 1.f : 0.f;
+  block_reduce_store_t<float, 10>(r, ops, A.part, block_linear_id());
+}
+
 dim3 v_grid(const Grid& g, int kc) {
   return dim3((g.nx + VX - 1) / VX, (g.ny + VY - 1) / VY, (g.nz + kc - 1) / kc);
 }
@@ -996,6 +1140,15 @@ void correct_v_launch(const CorrArgs<float, double>& a, cudaStream_t s) {
   allow_smem_v(k_correct25v<ZON, XO>, bytes, attr);
   const int kc = v_chunk(a.g, 3);
   launch_pdl(k_correct25v<ZON, XO>, v_grid(a.g, kc), dim3(VTX, VTY), bytes, s, a, kc);
+}
+
+template <bool ZON, bool XO>
+void correct_vf_launch(const CorrArgs<float, float>& a, cudaStream_t s) {
+  constexpr size_t bytes = sizeof(TRing);
+  static std::atomic<bool> attr[64];
+  allow_smem_v(k_correct25vf<ZON, XO>, bytes, attr);
+  const int kc = v_chunk(a.g, 3);  // the tiling of the FP64-pressure kernel (one record table)
+  launch_pdl(k_correct25vf<ZON, XO>, v_grid(a.g, kc), dim3(VTX, VTY), bytes, s, a, kc);
 }
 
 template <bool LES, bool ZON, bool XO>
@@ -1065,6 +1218,12 @@ void launch_correct_v(const CorrArgs<float, double>& a, cudaStream_t s) {
   const bool zon = a.g.bc[2] != AX_ZERO, xo = a.g.bc[0] == AX_OPEN;
   if (zon) { if (xo) correct_v_launch<true, true>(a, s); else correct_v_launch<true, false>(a, s); }
   else { if (xo) correct_v_launch<false, true>(a, s); else correct_v_launch<false, false>(a, s); }
+}
+
+void launch_correct_v(const CorrArgs<float, float>& a, cudaStream_t s) {
+  const bool zon = a.g.bc[2] != AX_ZERO, xo = a.g.bc[0] == AX_OPEN;
+  if (zon) { if (xo) correct_vf_launch<true, true>(a, s); else correct_vf_launch<true, false>(a, s); }
+  else { if (xo) correct_vf_launch<false, true>(a, s); else correct_vf_launch<false, false>(a, s); }
 }
 
 // the divergence and the correction run with the same tiling (3 blocks/SM)

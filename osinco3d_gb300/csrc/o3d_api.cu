@@ -90,7 +90,11 @@ struct o3d_ctx {
   void* rhs;
   float* rhs32;      // the mixed multigrid step's rhs, FP32 (its values are FP32 numbers)
   int rhs_f32;       // the current rhs is rhs32, not rhs
+  // the pressure and its history; with pdf (the mixed multigrid method) each
+  // of these buffers holds a double-float pair of FP32 planes (PPair: hi =
+  // RN32(p), then lo = RN32(p - hi)), converted to FP64 at the API
   double* pp;
+  int pdf;
   double* pp_prev;   // previous step's pressure (extrapolated and learned guesses, lazy)
   int pp_prev_valid;
   double* pp_prev2;  // the one before (quadratic extrapolation, lazy)
@@ -195,6 +199,38 @@ int get_field(o3d_ctx* c, const void* src, double* host) {
   c->launches++;
   CKL();
   CK(cudaMemcpyAsync(host, c->stage[0], (size_t)c->g.n * 8, cudaMemcpyDeviceToHost, c->s));
+  return O3D_OK;
+}
+
+// host FP64 pressure <-> a pressure buffer of the context (pp or its
+// history): a plain copy, or through stage[0] and the pair split / join
+// when the context holds its pressure as double-float pairs
+int put_pressure(o3d_ctx* c, double* dev, const double* host) {
+  const size_t bytes = (size_t)c->g.n * 8;
+  if (!c->pdf) {
+    CK(cudaMemcpyAsync(dev, host, bytes, cudaMemcpyHostToDevice, c->s));
+    return O3D_OK;
+  }
+  int st = stage_ready(c, 0);
+  if (st) return st;
+  CK(cudaMemcpyAsync(c->stage[0], host, bytes, cudaMemcpyHostToDevice, c->s));
+  launch_split_pair(c->stage[0], dev, c->g.n, c->s);
+  c->launches++;
+  CKL();
+  return O3D_OK;
+}
+int get_pressure(o3d_ctx* c, const double* dev, double* host) {
+  const size_t bytes = (size_t)c->g.n * 8;
+  if (!c->pdf) {
+    CK(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, c->s));
+    return O3D_OK;
+  }
+  int st = stage_ready(c, 0);
+  if (st) return st;
+  launch_join_pair(dev, c->stage[0], c->g.n, c->s);
+  c->launches++;
+  CKL();
+  CK(cudaMemcpyAsync(host, c->stage[0], bytes, cudaMemcpyDeviceToHost, c->s));
   return O3D_OK;
 }
 
@@ -308,10 +344,9 @@ int rhs_t(o3d_ctx* c) {
   return O3D_OK;
 }
 
-template <class T>
-int correct_t(o3d_ctx* c) {
-  CorrArgs<T, double> A;
-  A.p = c->pp;
+template <class T, class P>
+void correct_args(o3d_ctx* c, const P* p, CorrArgs<T, P>& A) {
+  A.p = p;
   for (int q = 0; q < 3; ++q) {
     A.up[q] = (const T*)c->up[q];
     A.u[q] = (T*)c->u[q];
@@ -320,7 +355,21 @@ int correct_t(o3d_ctx* c) {
   A.cf = cast_coef<T>(c->cf);
   A.dt = (T)c->P.dt;
   A.part = c->part;
-  launch_correct<T, double>(A, c->s);
+}
+
+template <class T>
+int correct_t(o3d_ctx* c) {
+  if (sizeof(T) == 4 && c->pdf) {
+    // the gradient of the FP32 pressure: the high plane of the pair (the
+    // FP32 rounding of the FP64 value, as the FP64-pressure kernels convert)
+    CorrArgs<float, float> A;
+    correct_args<float, float>(c, (const float*)c->pp, A);
+    launch_correct<float, float>(A, c->s);
+  } else {
+    CorrArgs<T, double> A;
+    correct_args<T, double>(c, c->pp, A);
+    launch_correct<T, double>(A, c->s);
+  }
   // min x3, max x3, |max| x3, nan flag
   unsigned long long ops = 0;
   for (int q = 0; q < 10; ++q) ops |= (unsigned long long)(q < 3 ? RED_MIN : RED_MAX) << (2 * q);
@@ -580,15 +629,15 @@ int enqueue_learned_first(o3d_ctx* c, bool learned, bool sampling, bool use_mg, 
                           long long* nl) {
   const int ll = c->learn_level;
   MGLevel* lv = c->mg.data();
-  if (c->mixed) launch_learn_extrapolate<float>(c->pp, c->pp_prev, lv, c->s, nl);
-  else launch_learn_extrapolate<double>(c->pp, c->pp_prev, lv, c->s, nl);
+  if (c->mixed) launch_learn_extrapolate<float>(c->pp, c->pp_prev, lv, c->s, nl, c->pdf);
+  else launch_learn_extrapolate<double>(c->pp, c->pp_prev, lv, c->s, nl, false);
   if (use_mg) {
     if (c->mixed && c->rhs_f32) launch_mg_resid<float, float>(c->pp, c->rhs32, lv, c->ctrl, c->s, nl);
     else if (c->mixed) launch_mg_resid<float, double>(c->pp, (const double*)c->rhs, lv, c->ctrl, c->s, nl);
     else launch_mg_resid<double, double>(c->pp, (const double*)c->rhs, lv, c->ctrl, c->s, nl);
   } else {
-    if (c->mixed) launch_level_kernel<float, double>(1, c->pp, (const double*)c->rhs, lv[0], c->ctrl, c->s);
-    else launch_level_kernel<double, double>(1, c->pp, (const double*)c->rhs, lv[0], c->ctrl, c->s);
+    if (c->mixed) launch_level_kernel<float, double>(1, c->pp, (const double*)c->rhs, lv[0], c->ctrl, c->s, false);
+    else launch_level_kernel<double, double>(1, c->pp, (const double*)c->rhs, lv[0], c->ctrl, c->s, false);
     *nl += 1;
   }
   if (c->mixed) launch_learn_features<float>(lv, ll, c->ctrl, c->feat, c->s, nl);
@@ -628,6 +677,11 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
   if (c->p_in_wait) {  // o3d_step_host: the pressure upload overlapped the predictor and the rhs
     CK(cudaStreamWaitEvent(c->s, c->p_in_wait, 0));
     c->p_in_wait = nullptr;
+    if (c->pdf) {
+      launch_split_pair(c->stage[3], c->pp, c->g.n, c->s);
+      c->launches++;
+      CKL();
+    }
   }
   const int guess = c->P.guess;
   const bool learned = guess == O3D_GUESS_LEARNED;
@@ -716,7 +770,7 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
     } else if (quad && c->pp_prev_valid && c->pp_prev2_valid) {
       // 3 p(n) - 3 p(n-1) + p(n-2); p(n) lands in pp_prev2's buffer, which
       // becomes pp_prev (the history shifts by a pointer swap, no copy)
-      launch_extrapolate2(c->pp, c->pp_prev, c->pp_prev2, c->g.n, c->s);
+      launch_extrapolate2(c->pp, c->pp_prev, c->pp_prev2, c->g.n, c->s, c->pdf);
       std::swap(c->pp_prev, c->pp_prev2);
       c->launches++;
       CKL();
@@ -725,7 +779,7 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
         CK(cudaMemcpyAsync(c->pp_prev2, c->pp_prev, (size_t)c->g.n * 8, cudaMemcpyDeviceToDevice, c->s));
         c->pp_prev2_valid = 1;
       }
-      launch_extrapolate(c->pp, c->pp_prev, c->g.n, c->s);
+      launch_extrapolate(c->pp, c->pp_prev, c->g.n, c->s, c->pdf);
       c->launches++;
       CKL();
     } else {
@@ -763,8 +817,11 @@ int solve(o3d_ctx* c, double* omega_io, double eps, int kmax, int idyn, o3d_step
   if (!use_mg || c->P.diagnostics >= 2) {
     PoiCoef<double> pc = make_poi<double>(c->dx, c->dy, c->dz);
     CK(cudaMemsetAsync(&c->ctrl->res_key, 0, sizeof(unsigned long long), c->s));
-    if (c->rhs_f32) launch_residual_inf<float>(c->pp, c->rhs32, c->gp, pc, c->ctrl, c->mixed && use_mg, c->s);
-    else launch_residual_inf<double>(c->pp, (const double*)c->rhs, c->gp, pc, c->ctrl, c->mixed && use_mg, c->s);
+    if (c->rhs_f32)
+      launch_residual_inf<float>(c->pp, c->rhs32, c->gp, pc, c->ctrl, c->mixed && use_mg, c->s, c->pdf);
+    else
+      launch_residual_inf<double>(c->pp, (const double*)c->rhs, c->gp, pc, c->ctrl, c->mixed && use_mg, c->s,
+                                  c->pdf);
     c->launches++;
     CKL();
   }
@@ -860,6 +917,7 @@ int o3d_create(const o3d_params* p, o3d_ctx** out) {
   if (!c) return O3D_ERR_NOMEM;
   c->P = *p;
   c->mixed = p->precision == O3D_PREC_MIXED;
+  c->pdf = c->mixed && p->solver == O3D_SOLVER_MG;
   c->esz = c->mixed ? 4 : 8;
   c->g.nx = p->nx; c->g.ny = p->ny; c->g.nz = p->nz;
   c->g.n = (long long)p->nx * p->ny * p->nz;
@@ -976,7 +1034,10 @@ int o3d_upload(o3d_ctx* c, int field, const double* host) {
     c->rhs_wsum = 0;
     c->rhs_f32 = 0;
   }
-  if (is_pp) {
+  if (field == O3D_FIELD_PP) {
+    int st = put_pressure(c, c->pp, host);
+    if (st) return st;
+  } else if (is_pp) {
     CK(cudaMemcpyAsync(d, host, (size_t)c->g.n * 8, cudaMemcpyHostToDevice, c->s));
   } else {
     int st = put_field(c, d, host);
@@ -993,6 +1054,9 @@ int o3d_download(o3d_ctx* c, int field, double* host) {
   if (!d) { errf("field %d not allocated or unknown", field); return O3D_ERR_BADARG; }
   if (field == O3D_FIELD_RHS && c->rhs_f32) {  // the step's FP32 rhs, widened exactly
     int st = get_field(c, c->rhs32, host);
+    if (st) return st;
+  } else if (field == O3D_FIELD_PP) {
+    int st = get_pressure(c, c->pp, host);
     if (st) return st;
   } else if (is_pp) {
     CK(cudaMemcpyAsync(host, d, (size_t)c->g.n * 8, cudaMemcpyDeviceToHost, c->s));
@@ -1098,7 +1162,8 @@ int o3d_transeq(o3d_ctx* c, int itime) {
 int o3d_poisson_solve(o3d_ctx* c, double* pp, const double* rhs, double* omega, double eps, int kmax,
                       int idyn, int* iters, double* dmax) {
   if (!c || !pp || !rhs || !omega) return O3D_ERR_BADARG;
-  CK(cudaMemcpyAsync(c->pp, pp, (size_t)c->g.n * 8, cudaMemcpyHostToDevice, c->s));
+  int pst = put_pressure(c, c->pp, pp);
+  if (pst) return pst;
   CK(cudaMemcpyAsync(c->rhs, rhs, (size_t)c->g.n * 8, cudaMemcpyHostToDevice, c->s));
   c->rhs_wsum = 0;  // a caller's rhs: its mean takes the separate pass
   c->rhs_f32 = 0;
@@ -1110,7 +1175,7 @@ int o3d_poisson_solve(o3d_ctx* c, double* pp, const double* rhs, double* omega, 
   int rs = solve(c, omega, eps, kmax, idyn, &info);
   c->P.guess = guess;
   if (rs < 0) return rs;
-  CK(cudaMemcpyAsync(pp, c->pp, (size_t)c->g.n * 8, cudaMemcpyDeviceToHost, c->s));
+  if ((pst = get_pressure(c, c->pp, pp))) return pst;
   CK(cudaStreamSynchronize(c->s));
   if (iters) *iters = info.poisson_iters;
   if (dmax) *dmax = info.poisson_dmax;
@@ -1130,9 +1195,16 @@ int o3d_step(o3d_ctx* c, int itime, o3d_step_info* info) {
   const int ps = solve(c, &c->omega, c->P.eps, c->P.kmax, c->P.idyn, info);
   if (ps < 0) return ps;
   if (c->p_out_host) {  // o3d_step_host: the final pressure goes out while the step finishes
+    const double* src = c->pp;
+    if (c->pdf) {  // joined to FP64 in stage 3 first
+      launch_join_pair(c->pp, c->stage[3], c->g.n, c->s);
+      c->launches++;
+      CKL();
+      src = c->stage[3];
+    }
     CK(cudaEventRecord(c->xev[5], c->s));
     CK(cudaStreamWaitEvent(c->xs, c->xev[5], 0));
-    CK(cudaMemcpyAsync(c->p_out_host, c->pp, (size_t)c->g.n * 8, cudaMemcpyDeviceToHost, c->xs));
+    CK(cudaMemcpyAsync(c->p_out_host, src, (size_t)c->g.n * 8, cudaMemcpyDeviceToHost, c->xs));
     c->p_out_host = nullptr;
   }
   st = c->mixed ? correct_t<float>(c) : correct_t<double>(c);
@@ -1178,7 +1250,7 @@ int o3d_step_host(o3d_ctx* c, int itime, double* ux, double* uy, double* uz, dou
     CK(cudaStreamCreateWithFlags(&c->xs, cudaStreamNonBlocking));
     for (int q = 0; q < 8; ++q) CK(cudaEventCreateWithFlags(&c->xev[q], cudaEventDisableTiming));
   }
-  if (c->mixed && (st = stage_ready(c, 2))) return st;
+  if (c->mixed && (st = stage_ready(c, c->pdf ? 3 : 2))) return st;
   double* const hu[3] = {ux, uy, uz};
   const size_t bytes = (size_t)c->g.n * 8;
   // inputs: copied on the copy stream (after earlier work of the context
@@ -1202,7 +1274,8 @@ int o3d_step_host(o3d_ctx* c, int itime, double* ux, double* uy, double* uz, dou
   }
   // the pressure lands while the predictor and the rhs run (the solve waits
   // for it) and leaves as soon as the solve ends (o3d_step issues the copy)
-  CK(cudaMemcpyAsync(c->pp, pp, bytes, cudaMemcpyHostToDevice, c->xs));
+  // (with pdf into stage 3, split into the pair by solve() once it landed)
+  CK(cudaMemcpyAsync(c->pdf ? (void*)c->stage[3] : (void*)c->pp, pp, bytes, cudaMemcpyHostToDevice, c->xs));
   CK(cudaEventRecord(c->xev[3], c->xs));
   c->p_in_wait = c->xev[3];
   c->p_out_host = pp;
@@ -1274,10 +1347,34 @@ int ctx_history_state(o3d_ctx* c, double* omega, int* nprev, double* prev_host, 
   const int n = !(c->pp_prev && c->pp_prev_valid) ? 0 : (c->pp_prev2 && c->pp_prev2_valid ? 2 : 1);
   if (nprev) *nprev = n;
   if (prev_host && which >= 1 && which <= n) {
-    CK(cudaMemcpyAsync(prev_host, which == 1 ? c->pp_prev : c->pp_prev2, (size_t)c->g.n * 8, cudaMemcpyDeviceToHost,
-                       c->s));
+    int st = get_pressure(c, which == 1 ? c->pp_prev : c->pp_prev2, prev_host);
+    if (st) return st;
     CK(cudaStreamSynchronize(c->s));
   }
+  return O3D_OK;
+}
+
+int ctx_pressure_pairs(const o3d_ctx* c) { return c->pdf; }
+
+int ctx_pressure_raw(o3d_ctx* c, int which, void* host, int to_device) {
+  double** buf = which == 0 ? &c->pp : which == 1 ? &c->pp_prev : &c->pp_prev2;
+  const size_t bytes = (size_t)c->g.n * 8;
+  if (to_device) {
+    if (!*buf) {
+      int st = dalloc(c->s, (void**)buf, bytes);
+      if (st) return st;
+    }
+    CK(cudaMemcpyAsync(*buf, host, bytes, cudaMemcpyHostToDevice, c->s));
+    if (which == 1) c->pp_prev_valid = 1;
+    if (which == 2) c->pp_prev2_valid = 1;
+  } else {
+    if (!*buf) {
+      errf("no pressure buffer %d to read", which);
+      return O3D_ERR_BADARG;
+    }
+    CK(cudaMemcpyAsync(host, *buf, bytes, cudaMemcpyDeviceToHost, c->s));
+  }
+  CK(cudaStreamSynchronize(c->s));
   return O3D_OK;
 }
 
@@ -1292,7 +1389,8 @@ int ctx_restore_history(o3d_ctx* c, double omega, int nprev, const double* prev1
       int st = dalloc(c->s, (void**)dev[q], (size_t)c->g.n * 8);
       if (st) return st;
     }
-    CK(cudaMemcpyAsync(*dev[q], host[q], (size_t)c->g.n * 8, cudaMemcpyHostToDevice, c->s));
+    int st = put_pressure(c, *dev[q], host[q]);
+    if (st) return st;
   }
   CK(cudaStreamSynchronize(c->s));
   c->pp_prev_valid = nprev >= 1;
@@ -1507,11 +1605,13 @@ int o3d_time_kernel(o3d_ctx* c, int kernel, int reps, double* ms_per_launch) {
       }
       default:
         if (c->mixed && c->rhs_f32)
-          launch_level_kernel<float, float>(kernel - 3, c->pp, c->rhs32, c->mg[0], c->ctrl, c->s);
+          launch_level_kernel<float, float>(kernel - 3, c->pp, c->rhs32, c->mg[0], c->ctrl, c->s, c->pdf);
         else if (c->mixed)
-          launch_level_kernel<float, double>(kernel - 3, c->pp, (const double*)c->rhs, c->mg[0], c->ctrl, c->s);
+          launch_level_kernel<float, double>(kernel - 3, c->pp, (const double*)c->rhs, c->mg[0], c->ctrl, c->s,
+                                             c->pdf);
         else
-          launch_level_kernel<double, double>(kernel - 3, c->pp, (const double*)c->rhs, c->mg[0], c->ctrl, c->s);
+          launch_level_kernel<double, double>(kernel - 3, c->pp, (const double*)c->rhs, c->mg[0], c->ctrl, c->s,
+                                              false);
         c->launches++;
         CKL();
         return O3D_OK;
@@ -1555,7 +1655,8 @@ int o3d_write_output(o3d_ctx* c, const char* dir, int num, double time) {
   }
   c->launches++;
   CKL();
-  CK(cudaMemcpyAsync(snap + 3 * n, c->pp, (size_t)n * 8, cudaMemcpyDeviceToDevice, c->s));
+  if (c->pdf) launch_join_pair(c->pp, snap + 3 * n, n, c->s);
+  else CK(cudaMemcpyAsync(snap + 3 * n, c->pp, (size_t)n * 8, cudaMemcpyDeviceToDevice, c->s));
   int q = 6;
   for (void* f : {c->P.nscr == 1 ? c->phi : nullptr, c->P.iles == 1 ? c->nu_t : nullptr}) {
     if (!f) continue;

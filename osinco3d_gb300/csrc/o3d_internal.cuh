@@ -295,6 +295,49 @@ __device__ __forceinline__ float df_resid7(const DF& rh, const DF& pc, const DF&
   return s + l;
 }
 
+// ---- the pressure of the mixed multigrid method: a double-float pair of
+// FP32 planes in one buffer the size of n doubles, hi = RN32(p) at [0, n)
+// and lo = RN32(p - hi) at [n, 2n) (floats) ----
+struct PPair {
+  float* hi;
+  float* lo;
+};
+inline PPair ppair(void* buf, long long n) { return PPair{(float*)buf, (float*)buf + n}; }
+
+// (h, l) <- (h, l) + d for a double-float value and an FP32 increment: the
+// exact sum of h and d by TwoSum, the low parts added, and the pair
+// renormalised by a second TwoSum (h stays the FP32 rounding of the value)
+__device__ __forceinline__ void df_add_f(float& h, float& l, float d) {
+  float s, e;
+  two_sum(h, d, s, e);
+  e += l;
+  two_sum(s, e, h, l);
+}
+// a + b, renormalised
+__device__ __forceinline__ DF df_add(const DF& a, const DF& b) {
+  float s, e;
+  two_sum(a.h, b.h, s, e);
+  e += a.l + b.l;
+  DF r;
+  two_sum(s, e, r.h, r.l);
+  return r;
+}
+// k a for a small integer k (the high product's error recovered by FMA)
+__device__ __forceinline__ DF df_scale(const DF& a, float k) {
+  const float p = k * a.h;
+  float e = fmaf(k, a.h, -p);
+  e = fmaf(k, a.l, e);
+  DF r;
+  two_sum(p, e, r.h, r.l);
+  return r;
+}
+__device__ __forceinline__ DF df_neg(const DF& a) { return DF{-a.h, -a.l}; }
+__device__ __forceinline__ DF pp_load(const PPair& p, long long q) { return DF{p.hi[q], p.lo[q]}; }
+__device__ __forceinline__ void pp_store(const PPair& p, long long q, const DF& v) {
+  p.hi[q] = v.h;
+  p.lo[q] = v.l;
+}
+
 // conversion of a loaded value to the compute type
 template <class T, class S>
 __device__ __forceinline__ T to_t(S v) { return (T)v; }

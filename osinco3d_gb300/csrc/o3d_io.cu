@@ -15,12 +15,20 @@
 
 namespace {
 
-// the history file: magic, then int32 nx, ny, nz, nscr, nprev, then double
-// omega, then the FP64 arrays (u, v, w fluxes newest then older, the scalar
-// fluxes when nscr = 1, then the nprev previous pressures, newest first: one
-// for the linear extrapolation and the learned guess, two for the quadratic
-// extrapolation)
-const char HIST_MAGIC[8] = {'O', '3', 'D', 'H', 'I', 'S', 'T', '1'};
+// the history file: magic, then int32 nx, ny, nz, nscr, nprev, pairs, then
+// double omega, then the FP64 arrays (u, v, w fluxes newest then older, the
+// scalar fluxes when nscr = 1), then the pressures: with pairs = 0 the nprev
+// previous pressures as FP64 arrays, newest first (one for the linear
+// extrapolation and the learned guess, two for the quadratic extrapolation);
+// with pairs = 1 (a context that holds its pressures as double-float pairs)
+// the current pressure and the nprev previous ones as raw pairs (n FP32 high
+// parts, then n low parts each).  A pair need not be representable in FP64
+// (its low part may reach more than 29 bits below the high part's last
+// bit), so the FP64 pressure of the fields file restores it only to FP64
+// precision; loading the history after the fields restores it exactly.
+// Files of the first version (magic ...1, no pairs field) load as pairs = 0.
+const char HIST_MAGIC[8] = {'O', '3', 'D', 'H', 'I', 'S', 'T', '2'};
+const char HIST_MAGIC1[8] = {'O', '3', 'D', 'H', 'I', 'S', 'T', '1'};
 
 struct File {
   FILE* f = nullptr;
@@ -138,8 +146,9 @@ int o3d_save_history(o3d_ctx* c, const char* path) {
     o3d::set_error("cannot open %s for writing", path);
     return O3D_ERR_BADARG;
   }
-  const int hdr[5] = {nx, ny, nz, P.nscr, has_prev};
-  bool ok = put(F.f, HIST_MAGIC, 8) && put(F.f, hdr, 20) && put(F.f, &omega, 8);
+  const int pairs = o3d::ctx_pressure_pairs(c);
+  const int hdr[6] = {nx, ny, nz, P.nscr, has_prev, pairs};
+  bool ok = put(F.f, HIST_MAGIC, 8) && put(F.f, hdr, 24) && put(F.f, &omega, 8);
   std::vector<int> ids;
   for (int q = 0; q < 6; ++q) ids.push_back(O3D_FIELD_FU0 + q);
   if (P.nscr)
@@ -149,8 +158,10 @@ int o3d_save_history(o3d_ctx* c, const char* path) {
     if ((st = o3d_download(c, id, buf.data()))) return st;
     ok = put(F.f, buf.data(), n * 8);
   }
-  for (int q = 1; ok && q <= has_prev; ++q) {
-    if ((st = o3d::ctx_history_state(c, nullptr, nullptr, buf.data(), q))) return st;
+  for (int q = pairs ? 0 : 1; ok && q <= has_prev; ++q) {
+    if (pairs) st = o3d::ctx_pressure_raw(c, q, buf.data(), 0);
+    else st = o3d::ctx_history_state(c, nullptr, nullptr, buf.data(), q);
+    if (st) return st;
     ok = put(F.f, buf.data(), n * 8);
   }
   if (!ok) {
@@ -174,9 +185,12 @@ int o3d_load_history(o3d_ctx* c, const char* path) {
     return O3D_ERR_BADARG;
   }
   char magic[8];
-  int hdr[5];
+  int hdr[6] = {0, 0, 0, 0, 0, 0};
   double omega;
-  if (!get(F.f, magic, 8) || memcmp(magic, HIST_MAGIC, 8) || !get(F.f, hdr, 20) || !get(F.f, &omega, 8)) {
+  bool ok = get(F.f, magic, 8);
+  const bool v2 = ok && !memcmp(magic, HIST_MAGIC, 8);
+  ok = ok && (v2 || !memcmp(magic, HIST_MAGIC1, 8)) && get(F.f, hdr, v2 ? 24 : 20) && get(F.f, &omega, 8);
+  if (!ok || hdr[5] < 0 || hdr[5] > 1) {
     o3d::set_error("%s is not a history file", path);
     return O3D_ERR_BADARG;
   }
@@ -201,14 +215,31 @@ int o3d_load_history(o3d_ctx* c, const char* path) {
     o3d::set_error("%s: %d previous pressures (at most 2)", path, hdr[4]);
     return O3D_ERR_BADARG;
   }
-  std::vector<double> prev((size_t)hdr[4] * n);
-  for (int q = 0; q < hdr[4]; ++q)
-    if (!get(F.f, prev.data() + (size_t)q * n, n * 8)) {
+  const int pairs = hdr[5], npres = hdr[4] + (pairs ? 1 : 0);
+  std::vector<double> pres((size_t)npres * n);
+  for (int q = 0; q < npres; ++q)
+    if (!get(F.f, pres.data() + (size_t)q * n, n * 8)) {
       o3d::set_error("%s: truncated", path);
       return O3D_ERR_BADARG;
     }
-  return o3d::ctx_restore_history(c, omega, hdr[4], hdr[4] >= 1 ? prev.data() : nullptr,
-                                  hdr[4] >= 2 ? prev.data() + n : nullptr);
+  if (pairs && o3d::ctx_pressure_pairs(c)) {  // exact: the raw pairs back into their buffers
+    if ((st = o3d::ctx_restore_history(c, omega, 0, nullptr, nullptr))) return st;
+    for (int q = 0; q < npres; ++q)
+      if ((st = o3d::ctx_pressure_raw(c, q, pres.data() + (size_t)q * n, 1))) return st;
+    return O3D_OK;
+  }
+  if (pairs) {  // pairs into a context with FP64 pressures: their values hi + lo, rounded to FP64
+    std::vector<double> v((size_t)npres * n);
+    for (int q = 0; q < npres; ++q) {
+      const float* h = reinterpret_cast<const float*>(pres.data() + (size_t)q * n);
+      for (size_t i = 0; i < n; ++i) v[(size_t)q * n + i] = (double)h[i] + (double)h[n + i];
+    }
+    if ((st = o3d_upload(c, O3D_FIELD_PP, v.data()))) return st;
+    return o3d::ctx_restore_history(c, omega, hdr[4], hdr[4] >= 1 ? v.data() + n : nullptr,
+                                    hdr[4] >= 2 ? v.data() + 2 * n : nullptr);
+  }
+  return o3d::ctx_restore_history(c, omega, hdr[4], hdr[4] >= 1 ? pres.data() : nullptr,
+                                  hdr[4] >= 2 ? pres.data() + n : nullptr);
 }
 
 }  // extern "C"

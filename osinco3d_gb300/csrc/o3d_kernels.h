@@ -85,6 +85,7 @@ template <class O>
 void launch_div_v(const float* fx, const float* fy, const float* fz, O* out, const Grid& g, const Coef3<float>& cf,
                   int odd, float dt, int divide, StatPart* part, cudaStream_t s, double* wpart, int wmask);
 void launch_correct_v(const CorrArgs<float, double>& a, cudaStream_t s);
+void launch_correct_v(const CorrArgs<float, float>& a, cudaStream_t s);
 long long div_v_blocks(const Grid& g);
 long long corr_v_blocks(const Grid& g);
 void launch_transeq_v(const ScalArgs<float>& a, cudaStream_t s);
@@ -111,6 +112,9 @@ void launch_finalize_stats(const StatPart* part, long long nblk, const Grid& g, 
                            cudaStream_t s);
 template <class S, class D>
 void launch_convert(const S* s_, D* d, long long n, cudaStream_t s);
+// FP64 field <-> double-float pair buffer (PPair layout: hi plane, lo plane)
+void launch_split_pair(const double* x, void* pair, long long n, cudaStream_t s);
+void launch_join_pair(const void* pair, double* x, long long n, cudaStream_t s);
 
 // ---- pressure solve (k_poisson.cu) ----------------------------------------
 
@@ -150,18 +154,23 @@ int mg_fused_setup();
 bool mg_fusable(const MGLevel& L, int pre, int post, bool any_size);
 void launch_mg_down(const MGLevel& L, const MGLevel& C, float om, int pre, bool zero, const SolveCtrl* ctrl,
                     cudaStream_t s);
+// p: the finest level's pressure as a double-float pair buffer (p += e), or nullptr
 void launch_mg_up(const MGLevel& L, const MGLevel& C, float om, int post, double* p, SolveCtrl* ctrl,
                   cudaStream_t s);
 
 // context state for checkpoint and restart (o3d_api.cu, used by o3d_io.cu)
 int ctx_geometry(o3d_ctx* c, o3d_params* p, int* nx, int* ny, int* nz, double* dx, double* dy, double* dz);
-// omega and whether a previous pressure exists; prev_host (may be null)
-// receives the previous pressure
 // the SOR omega and the previous pressures kept for the extrapolated and
 // learned guesses: *nprev of them (0..2); prev_host receives number `which`
 // (1 = the newest)
 int ctx_history_state(o3d_ctx* c, double* omega, int* nprev, double* prev_host, int which);
 int ctx_restore_history(o3d_ctx* c, double omega, int nprev, const double* prev1, const double* prev2);
+// whether the context holds its pressures as double-float pairs, and their
+// raw buffers (n doubles' size: hi plane, lo plane): `which` 0 = the
+// pressure, 1 and 2 = the previous ones; to_device copies host -> device
+// (allocating a missing history buffer and marking it valid)
+int ctx_pressure_pairs(const o3d_ctx* c);
+int ctx_pressure_raw(o3d_ctx* c, int which, void* host, int to_device);
 
 // output-cadence diagnostics (k_diag.cu)
 template <class T>
@@ -193,12 +202,13 @@ void launch_mg_resid(double* p, const R* rhs, MGLevel* lv, SolveCtrl* ctrl, cuda
 template <class T>
 void launch_mg_cycles(double* p, MGLevel* lv, int nlev, int pre, int post, int coarse_sweeps, T smooth_omega,
                       int cycles, bool from_e, SolveCtrl* ctrl, cudaStream_t s, long long* nl);
-void launch_extrapolate(double* p, double* pprev, long long n, cudaStream_t s);
-void launch_extrapolate2(double* p, const double* pprev, double* pprev2, long long n, cudaStream_t s);
+// pair: the buffers hold double-float pairs (the mixed multigrid method)
+void launch_extrapolate(double* p, double* pprev, long long n, cudaStream_t s, bool pair);
+void launch_extrapolate2(double* p, const double* pprev, double* pprev2, long long n, cudaStream_t s, bool pair);
 
 // learned warm start: the network works on multigrid level ll
 template <class T>
-void launch_learn_extrapolate(double* p, double* pprev, MGLevel* lv, cudaStream_t s, long long* nl);
+void launch_learn_extrapolate(double* p, double* pprev, MGLevel* lv, cudaStream_t s, long long* nl, bool pair);
 template <class T>
 void launch_learn_features(MGLevel* lv, int ll, SolveCtrl* ctrl, float* feat, cudaStream_t s, long long* nl);
 template <class T>
@@ -211,7 +221,7 @@ void launch_learn_target(const double* p, const double* pprev, MGLevel* lv, int 
 // one finest-level kernel for timing: 0 smoother (one sweep), 1 FP64 residual
 template <class T, class R>
 void launch_level_kernel(int which, double* p, const R* rhs, const MGLevel& L, SolveCtrl* ctrl,
-                         cudaStream_t s);
+                         cudaStream_t s, bool pair);
 template <class R>
 void launch_rhs_wmean(const R* rhs, const Grid& g, double* part, SolveCtrl* ctrl, cudaStream_t s,
                       long long* nl);
@@ -219,8 +229,7 @@ void launch_rhs_wmean_final(const double* part, long long nblk, const Grid& g, S
                             long long* nl);
 template <class R>
 void launch_residual_inf(const double* p, const R* rhs, const Grid& g, const PoiCoef<double>& c, SolveCtrl* ctrl,
-                         bool shift,
-                         cudaStream_t s);
+                         bool shift, cudaStream_t s, bool pair);
 template <class R>
 void launch_rhs_shift(R* rhs, long long n, SolveCtrl* ctrl, cudaStream_t s);
 
