@@ -13,6 +13,8 @@
 // the deep levels' small grids the reduction is split into slices over the
 // (tap, 16-channel step) sequence, each block writing FP32 partials that a
 // second kernel sums in slice order (deterministic) before the epilogue.
+#include <atomic>
+
 #include <cuda_bf16.h>
 
 #include "o3d_internal.cuh"
@@ -438,6 +440,205 @@ __global__ void k_pack_input(const float* __restrict__ in, int nch, long long nv
 }
 
 // ---------------------------------------------------------------------------
+// The same convolution on the fifth-generation tensor cores: one CTA of 4
+// warps computes 128 voxels x all N output channels as a chain of
+// tcgen05.mma (kind::f16, BF16 operands, M = 128, N, K = 16 per instruction)
+// accumulating in tensor memory (TMEM, 128 lanes x N FP32 columns).  Each
+// K-step is one (tap, 16-channel) pair: its A tile (the 128 voxels' shifted
+// input rows, zeros outside the volume) and B tile (W[tap][n][k0..k0+15])
+// are gathered by cp.async into one of TC_STAGES shared-memory stages in the
+// canonical K-major layout without swizzle (8-row x 16-byte core matrices,
+// the two K halves 128 B apart, row groups 256 B apart).  Thread 0 issues
+// the MMA of a stage once all threads' copies landed (cp.async.wait_group,
+// fence.proxy.async, barrier) and commits it to the stage's mbarrier; a
+// stage is refilled after that mbarrier fired.  The epilogue reads the
+// accumulator back with tcgen05.ld (warp w: lanes 32w .. 32w + 31, its
+// voxels) and applies conv_epilogue, or stores the FP32 partial of a split
+// slice as k_conv3 does.  Every mbarrier wait is bounded (about a second
+// of clock); a wait that runs out sets g_tc_timeout and the CTA finishes
+// without further waits.
+// ---------------------------------------------------------------------------
+constexpr int TC_M = 128, TC_THREADS = 128, TC_STAGES = 4;
+constexpr int TC_A_BYTES = TC_M * 32;  // 128 rows x 16 BF16
+
+__device__ int g_tc_timeout;
+
+__device__ __forceinline__ uint32_t tc_smem(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+// byte offset of row r, K half h (BF16 k 0..7 or 8..15) in a K-major tile
+__device__ __forceinline__ uint32_t tc_off(int r, int h) {
+  return (uint32_t)(((r >> 3) * 2 + h) * 128 + (r & 7) * 16);
+}
+// shared-memory matrix descriptor: start address, leading byte offset (K
+// direction) 128, stride byte offset (row groups) 256, descriptor version 1,
+// no swizzle
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr) {
+  return (uint64_t)((saddr >> 4) & 0x3fffu) | ((uint64_t)(128u >> 4) << 16) | ((uint64_t)(256u >> 4) << 32) |
+         ((uint64_t)1 << 46);
+}
+// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N >> 3 and M >> 4
+__device__ __forceinline__ uint32_t tc_idesc(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
+}
+__device__ __forceinline__ void tc_cp16(uint32_t dst, const void* src, bool ok) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(ok ? 16 : 0) : "memory");
+}
+__device__ __forceinline__ void tc_mbar_init(uint32_t a) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(a) : "memory");
+}
+// waits for the completion of the phase of parity `par`; false after about
+// 2^31 clocks without it
+__device__ __forceinline__ bool tc_mbar_wait(uint32_t a, uint32_t par) {
+  const long long t0 = clock64();
+  for (;;) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(par)
+        : "memory");
+    if (done) return true;
+    if (clock64() - t0 > (1LL << 31)) return false;
+  }
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t idesc, int accum) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          tmem),
+      "l"(ad), "l"(bd), "r"(idesc), "r"(accum)
+      : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar) : "memory");
+}
+// 16 consecutive FP32 columns of the warp's 32 TMEM lanes (one lane per thread)
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+               : "r"(taddr)
+               : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__global__ void __launch_bounds__(TC_THREADS) k_conv3_tc(ConvArgs A, int ncols) {
+  pdl_enter();
+  extern __shared__ __align__(128) unsigned char tc_sm[];
+  const int t = threadIdx.x, warp = t >> 5;
+  const int N = A.N;
+  const int stage_bytes = TC_A_BYTES + N * 32;
+  const uint32_t sbase = tc_smem(tc_sm);
+  const uint32_t mbar0 = sbase + TC_STAGES * stage_bytes;  // TC_STAGES mbarriers, 8 B each
+  volatile uint32_t* tslot = reinterpret_cast<volatile uint32_t*>(tc_sm + TC_STAGES * stage_bytes + 8 * TC_STAGES);
+  const long long nvox = (long long)A.v.nx * A.v.ny * A.v.nz;
+  const long long p = (long long)blockIdx.x * TC_M + t;  // this thread's voxel row
+  const bool live = p < nvox;
+  const long long pc = live ? p : 0;
+  const int ci = (int)(pc % A.v.nx), cj = (int)((pc / A.v.nx) % A.v.ny), ck = (int)(pc / ((long long)A.v.nx * A.v.ny));
+  const int kpt = A.K / 16, nq = 27 * kpt, S = gridDim.z;
+  const int q0 = (int)((long long)nq * blockIdx.z / S), q1 = (int)((long long)nq * (blockIdx.z + 1) / S);
+  const int nsteps = q1 - q0;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                     tc_smem((const void*)tslot)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  if (t == 0) {
+    for (int s = 0; s < TC_STAGES; ++s) tc_mbar_init(mbar0 + 8 * s);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+  const uint32_t idesc = tc_idesc(N);
+
+  auto load = [&](int q, int st) {
+    const int tap = q / kpt, k0 = (q - tap * kpt) * 16;
+    bool ox, oy, oz;
+    const int ii = wrapc(ci + tap % 3 - 1, A.v.nx, A.v.per[0], &ox);
+    const int jj = wrapc(cj + (tap / 3) % 3 - 1, A.v.ny, A.v.per[1], &oy);
+    const int kk = wrapc(ck + tap / 9 - 1, A.v.nz, A.v.per[2], &oz);
+    const bool ok = live && ox && oy && oz;
+    const __nv_bfloat16* row = A.x + (((long long)kk * A.v.ny + jj) * A.v.nx + ii) * A.xcs + A.xc0 + k0;
+    const uint32_t a = sbase + st * stage_bytes;
+    tc_cp16(a + tc_off(t, 0), ok ? (const void*)row : (const void*)A.x, ok);
+    tc_cp16(a + tc_off(t, 1), ok ? (const void*)(row + 8) : (const void*)A.x, ok);
+    const uint32_t b = a + TC_A_BYTES;
+    const __nv_bfloat16* wt = A.w + (long long)tap * N * A.K + k0;
+    for (int c = t; c < 2 * N; c += TC_THREADS) {
+      const int n = c >> 1, h = c & 1;
+      tc_cp16(b + tc_off(n, h), wt + (long long)n * A.K + 8 * h, true);
+    }
+  };
+
+  bool ok_all = true;
+#pragma unroll 1
+  for (int i = 0; i < TC_STAGES - 1; ++i) {
+    if (i < nsteps) load(q0 + i, i);
+    cp_async_commit();
+  }
+#pragma unroll 1
+  for (int i = 0; i < nsteps; ++i) {
+    const int st = i % TC_STAGES;
+    const int nx = i + TC_STAGES - 1;  // the step whose copies start now
+    if (nx < nsteps) {
+      const int sn = nx % TC_STAGES;
+      // its stage was last read by the MMA of step nx - TC_STAGES
+      if (nx >= TC_STAGES && ok_all) ok_all = tc_mbar_wait(mbar0 + 8 * sn, (uint32_t)((nx / TC_STAGES - 1) & 1));
+      load(q0 + nx, sn);
+    }
+    cp_async_commit();
+    cp_async_wait<TC_STAGES - 1>();  // step i's copies landed
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    ok_all = __syncthreads_and(ok_all) != 0;  // one verdict for the CTA: after a timeout nobody waits again
+    if (t == 0 && ok_all) {
+      tc_fence_after();
+      const uint32_t a = sbase + st * stage_bytes;
+      tc_mma(tmem, tc_desc(a), tc_desc(a + TC_A_BYTES), idesc, i > 0 ? 1 : 0);
+      tc_commit(mbar0 + 8 * st);
+    }
+  }
+  cp_async_wait<0>();
+  // every thread waits for the last MMA (its commit covers all earlier ones)
+  if (nsteps > 0 && ok_all) {
+    const int st = (nsteps - 1) % TC_STAGES;
+    ok_all = tc_mbar_wait(mbar0 + 8 * st, (uint32_t)(((nsteps - 1) / TC_STAGES) & 1));
+  }
+  ok_all = __syncthreads_and(ok_all) != 0;
+  tc_fence_after();
+  if (!ok_all) atomicExch(&g_tc_timeout, 1);
+  if (nsteps > 0 && ok_all) {
+    const uint32_t lane_base = tmem + ((uint32_t)(32 * warp) << 16);
+    for (int c0 = 0; c0 < N; c0 += 16) {
+      float v[16];
+      tc_ld16(lane_base + (uint32_t)c0, v);
+      if (live) {
+#pragma unroll
+        for (int j = 0; j < 16; j += 2) {
+          const int n = c0 + j;
+          if (S == 1) {
+            conv_epilogue(A, p, n, v[j], v[j + 1]);
+          } else {
+            *reinterpret_cast<float2*>(A.ws + ((long long)blockIdx.z * nvox + p) * N + n) = make_float2(v[j], v[j + 1]);
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(ncols) : "memory");
+}
+
+// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 // blocks of a convolution before splitting: 64 voxels x (16 or 32) channels
@@ -454,8 +655,56 @@ int conv_splits(long long nvox, int K, int N) {
   return S < 1 ? 1 : (int)S;
 }
 
+// the tensor-core kernel takes 16-byte aligned rows (channel stride and
+// offset multiples of 8) and N a multiple of 16 up to 256
+static bool conv_tc_ok(const ConvArgs& a) {
+  return a.xcs % 8 == 0 && a.xc0 % 8 == 0 && a.K % 16 == 0 && a.N % 16 == 0 && a.N >= 16 && a.N <= 256 &&
+         ((uintptr_t)a.x % 16) == 0 && ((uintptr_t)a.w % 16) == 0;
+}
+static int conv_tc_splits(long long nvox, int K) {
+  const long long tiles = (nvox + TC_M - 1) / TC_M;
+  const int nq = 27 * (K / 16);
+  const long long want = (2LL * 152 + tiles - 1) / tiles;  // two CTAs per SM
+  long long S = want < nq / 4 ? want : nq / 4;             // at least 4 K-steps per slice
+  if (S > 27) S = 27;
+  return S < 1 ? 1 : (int)S;
+}
+
+// whether a tensor-core convolution gave up on a wait since the last call
+// (the flag is cleared); call with no kernel of the network in flight
+int conv_tc_timed_out() {
+  int v = 0;
+  if (cudaMemcpyFromSymbol(&v, g_tc_timeout, sizeof v) != cudaSuccess) return -1;
+  if (v) {
+    const int z = 0;
+    cudaMemcpyToSymbol(g_tc_timeout, &z, sizeof z);
+  }
+  return v;
+}
+
 int launch_conv3(const ConvArgs& a, cudaStream_t s) {
   const long long nvox = (long long)a.v.nx * a.v.ny * a.v.nz;
+  if (conv_tc_ok(a)) {
+    int S = a.ws ? conv_tc_splits(nvox, a.K) : 1;
+    while (S > 1 && (long long)S * nvox * a.N > a.ws_cap) --S;
+    int ncols = 32;
+    while (ncols < a.N) ncols *= 2;
+    const size_t smem = (size_t)TC_STAGES * (TC_A_BYTES + a.N * 32) + 8 * TC_STAGES + 16;
+    // the shared-memory opt-in belongs to the current device: set it per device
+    static std::atomic<bool> attr_done[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) dev = -1;
+    if (!(dev >= 0 && dev < 64 && attr_done[dev].load())) {
+      if (cudaFuncSetAttribute(k_conv3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)((size_t)TC_STAGES * (TC_A_BYTES + 256 * 32) + 8 * TC_STAGES + 16)) ==
+              cudaSuccess &&
+          dev >= 0 && dev < 64)
+        attr_done[dev].store(true);
+    }
+    launch_pdl(k_conv3_tc, dim3((unsigned)((nvox + TC_M - 1) / TC_M), 1, S), TC_THREADS, smem, s, a, ncols);
+    if (S > 1) launch_pdl(k_conv3_reduce, (unsigned)((nvox * (a.N / 2) + 255) / 256), 256, 0, s, a, S);
+    return S > 1 ? 2 : 1;
+  }
   const unsigned gx = (unsigned)((nvox + 63) / 64);
   int S = a.ws ? conv_splits(nvox, a.K, a.N) : 1;
   while (S > 1 && (long long)S * nvox * a.N > a.ws_cap) --S;

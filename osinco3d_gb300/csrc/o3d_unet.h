@@ -45,6 +45,9 @@ struct WgradArgs {
 // GPU, up to 27 * K / 64 on the small grids of the deep levels.
 int conv_splits(long long nvox, int K, int N);
 int launch_conv3(const ConvArgs& a, cudaStream_t s);  // returns the kernels launched
+// 1 if a tensor-core convolution gave up on a bounded wait since the last
+// call (then its output is not valid), 0 if not, -1 if the flag is unreadable
+int conv_tc_timed_out();
 void launch_wgrad(const WgradArgs& a, cudaStream_t s);
 void launch_bias_grad(const __nv_bfloat16* dy, int dycs, int dyc0, long long nvox, int N, float* db, cudaStream_t s);
 void launch_pool(const __nv_bfloat16* x, int xcs, int xc0, const Vol& vf, __nv_bfloat16* y, int ycs, int yc0,

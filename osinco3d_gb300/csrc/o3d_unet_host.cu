@@ -512,7 +512,14 @@ int unet_enqueue_forward(o3d_unet* n, const float* d_in, float* d_out, cudaStrea
   return e == cudaSuccess ? O3D_OK : O3D_ERR_CUDA;
 }
 // waits for the network's own queued work (weight packing after training)
-int unet_sync(o3d_unet* n) { return cudaStreamSynchronize(n->u.s) == cudaSuccess ? O3D_OK : O3D_ERR_CUDA; }
+int unet_sync(o3d_unet* n) {
+  if (cudaStreamSynchronize(n->u.s) != cudaSuccess) return O3D_ERR_CUDA;
+  if (conv_tc_timed_out() != 0) {
+    set_error("a tensor-core convolution of the network timed out on a wait; its output is invalid");
+    return O3D_ERR_CUDA;
+  }
+  return O3D_OK;
+}
 int unet_grid(const o3d_unet* n, int* nx, int* ny, int* nz, int* in_ch) {
   *nx = n->u.vol[0].nx;
   *ny = n->u.vol[0].ny;
