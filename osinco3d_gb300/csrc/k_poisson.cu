@@ -513,15 +513,129 @@ int launch_sor_sweep_ctrl(double* p, const double* rhs, const Grid& g, const Poi
   return 2 + sor_seam_passes(p, rhs, g, c, ctrl, 0.0, 1, s);
 }
 
+// ---------------------------------------------------------------------------
+// The one-pass level kernels of a large level as 2.5D marches (FP32): a
+// block owns a 32 x 8 column and marches along z over LV_KC planes; the
+// stencil field's plane lands in a double-buffered shared tile with a
+// 1-cell halo (loaded one plane ahead, as in k_resid25), its z-neighbours
+// stay in registers.  OP 0: one colour of a relaxed Gauss-Seidel sweep, in
+// place (k_smooth); OP 1: the first sweep from e = 0 (k_smooth_first); OP 2:
+// the residual t = r - A e (k_resid).  Each value is the expression of the
+// one-pass kernel in the same order, so the results are bit-identical.  In
+// place (OP 0) a colour's update reads only the other colour's values and
+// its own, which no block writes in that pass.
+// ---------------------------------------------------------------------------
+constexpr int LV_TX = 32, LV_TY = 8, LV_KC = 16;
+static inline dim3 lv_grid(const Grid& g) {
+  return dim3((g.nx + LV_TX - 1) / LV_TX, (g.ny + LV_TY - 1) / LV_TY, (g.nz + LV_KC - 1) / LV_KC);
+}
+// the level kernels take the 2.5D form from this size on
+static inline bool lv_big(const Grid& g) { return g.n >= (1LL << 22) && g.nx >= 16 && g.ny >= 8 && g.nz >= 8; }
+
+template <int OP>
+__global__ void __launch_bounds__(LV_TX * LV_TY) k_lvl25(float* __restrict__ e, const float* __restrict__ r,
+                                                         float* __restrict__ t, Grid g, PoiCoef<float> c, float om,
+                                                         int color, const SolveCtrl* ctrl) {
+  pdl_enter();
+  if (ctrl->done) return;
+  constexpr int TX = LV_TX, TY = LV_TY, SW = TX + 2;
+  __shared__ float tile[2][(TY + 2) * SW];
+  const float* F = OP == 1 ? r : e;  // the field the operator acts on
+  const int tx = threadIdx.x, ty = threadIdx.y, th = ty * TX + tx;
+  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+  const int i = i0 + tx, j = j0 + ty;
+  const bool valid = i < g.nx && j < g.ny;
+  const int k0 = blockIdx.z * LV_KC, k1 = min(k0 + LV_KC, g.nz);
+  const long long sz = g.sz();
+  bool f;
+  const int cxy = ghost(i, g.nx, g.bc[0], &f) + g.nx * ghost(j, g.ny, g.bc[1], &f);
+  // halo cell of this thread (th < 2 (TX + TY)): left, right, below, above
+  const bool hon = th < 2 * (TX + TY);
+  int hi, hj, hidx;
+  if (th < TY) { hi = i0 - 1; hj = j0 + th; hidx = (th + 1) * SW; }
+  else if (th < 2 * TY) { hi = i0 + TX; hj = j0 + th - TY; hidx = (th - TY + 1) * SW + TX + 1; }
+  else if (th < 2 * TY + TX) { hi = i0 + th - 2 * TY; hj = j0 - 1; hidx = th - 2 * TY + 1; }
+  else { const int u = min(th - 2 * TY - TX, TX - 1); hi = i0 + u; hj = j0 + TY; hidx = (TY + 1) * SW + u + 1; }
+  const int hxy = ghost(hi, g.nx, g.bc[0], &f) + g.nx * ghost(hj, g.ny, g.bc[1], &f);
+  const int sc = (ty + 1) * SW + tx + 1;
+  auto zoff = [&](int k) { return sz * ghost(k, g.nz, g.bc[2], &f); };
+  const long long out0 = valid ? (long long)i + (long long)g.nx * j : 0;
+
+  float pb = __ldg(F + zoff(k0 - 1) + cxy), pc = __ldg(F + zoff(k0) + cxy);
+  float ptn = __ldg(F + zoff(k0 + 1) + cxy);
+  float hv = hon ? __ldg(F + zoff(k0) + hxy) : 0.f;
+  float rr = (OP != 1 && valid) ? __ldg(r + out0 + sz * k0) : 0.f;
+  int buf = 0;
+  for (int k = k0; k < k1; ++k) {
+    const float pt = ptn;
+    tile[buf][sc] = pc;
+    if (hon) tile[buf][hidx] = hv;
+    const float rcur = rr;
+    if (k + 1 < k1) {
+      ptn = __ldg(F + zoff(k + 2) + cxy);
+      if (hon) hv = __ldg(F + zoff(k + 1) + hxy);
+      if (OP != 1 && valid) rr = __ldg(r + out0 + sz * (k + 1));
+    }
+    __syncthreads();
+    if (valid) {
+      const float* T0 = tile[buf];
+      const long long q = out0 + sz * k;
+      const bool mine = ((i + j + k + color) & 1) == 0;
+      if (OP == 0) {
+        if (mine) {
+          const float s = c.ox * (T0[sc - 1] + T0[sc + 1]) + c.oy * (T0[sc - SW] + T0[sc + SW]) + c.oz * (pb + pt);
+          const float en = (rcur - s) * c.invA;
+          e[q] = pc + om * (en - pc);
+        }
+      } else if (OP == 1) {
+        if (((i + j + k) & 1) == 0) {
+          e[q] = om * (pc * c.invA);
+        } else {
+          const float s = c.ox * (T0[sc - 1] + T0[sc + 1]) + c.oy * (T0[sc - SW] + T0[sc + SW]) + c.oz * (pb + pt);
+          e[q] = om * ((pc - om * (s * c.invA)) * c.invA);
+        }
+      } else {
+        const float s = c.ox * (T0[sc - 1] + T0[sc + 1]) + c.oy * (T0[sc - SW] + T0[sc + SW]) + c.oz * (pb + pt);
+        t[q] = rcur - (s + c.A * pc);
+      }
+    }
+    pb = pc;
+    pc = pt;
+    buf ^= 1;
+  }
+}
+
 // `n` red-black sweeps of A e = r with relaxation om, in place on e
 template <class T>
 static void smooth_sweeps(const MGLevel& L, T* e, const T* r, const PoiCoef<T>& c, T om, int n,
                           const SolveCtrl* ctrl, cudaStream_t s, long long* nl) {
   for (int q = 0; q < n; ++q)
-    for (int color = 0; color < 2; ++color)
+    for (int color = 0; color < 2; ++color) {
+      if constexpr (sizeof(T) == 4) {
+        if (lv_big(L.g)) {
+          launch_pdl(k_lvl25<0>, lv_grid(L.g), dim3(LV_TX, LV_TY), 0, s, (float*)e, (const float*)r, (float*)nullptr,
+                     L.g, c, (float)om, color, ctrl);
+          continue;
+        }
+      }
       launch_pdl(k_smooth<T>, dim3((unsigned)(((L.g.nx + 1) / 2 + 31) / 32), (L.g.ny + 7) / 8, L.g.nz), dim3(32, 8),
                  0, s, e, r, L.g, c, color, om, ctrl);
+    }
   *nl += 2 * n;
+}
+// the first sweep from e = 0 and the residual t = r - A e of a level
+template <class T>
+static void smooth_first(const MGLevel& L, T* e, const T* r, const PoiCoef<T>& c, T om, const SolveCtrl* ctrl,
+                         cudaStream_t s) {
+  if constexpr (sizeof(T) == 4) {
+    if (lv_big(L.g)) {
+      launch_pdl(k_lvl25<1>, lv_grid(L.g), dim3(LV_TX, LV_TY), 0, s, (float*)e, (const float*)r, (float*)nullptr, L.g,
+                 c, (float)om, 0, ctrl);
+      return;
+    }
+  }
+  launch_pdl(k_smooth_first<T>, dim3((L.g.nx + 31) / 32, (L.g.ny + 7) / 8, L.g.nz), dim3(32, 8), 0, s, e, r, L.g, c,
+             om, ctrl);
 }
 
 template <class T>
@@ -536,6 +650,19 @@ __global__ void __launch_bounds__(256) k_resid(const T* __restrict__ e, const T*
   if (i >= g.nx || j >= g.ny) return;
   const int q = idx3(g, i, j, k);
   t[q] = r[q] - (lap6<T>(e, q, nb6(g, i, j, k), c) + c.A * e[q]);
+}
+
+template <class T>
+static void level_resid(const MGLevel& L, const T* e, const T* r, T* t, const PoiCoef<T>& c, const SolveCtrl* ctrl,
+                        cudaStream_t s) {
+  if constexpr (sizeof(T) == 4) {
+    if (lv_big(L.g)) {
+      launch_pdl(k_lvl25<2>, lv_grid(L.g), dim3(LV_TX, LV_TY), 0, s, (float*)e, (const float*)r, (float*)t, L.g, c,
+                 1.f, 0, ctrl);
+      return;
+    }
+  }
+  launch_pdl(k_resid<T>, dim3((L.g.nx + 31) / 32, (L.g.ny + 7) / 8, L.g.nz), dim3(32, 8), 0, s, e, r, t, L.g, c, ctrl);
 }
 
 struct Coarsen {
@@ -712,36 +839,48 @@ __host__ __device__ __forceinline__ void nn_ratio(int nf, int nc, int bc, int* n
 
 __device__ __forceinline__ int floor_div(int a, int b) { return a >= 0 ? a / b : -((-a + b - 1) / b); }
 
-// restriction taps of coarse index J along one axis: fine indices and weights
+// restriction taps of coarse index J along one axis: NN_MAXT slots of fine
+// indices and weights in increasing fine order, unused slots with weight 0
+// (and a valid index), so that the sums below run over a fixed, unrolled
+// count with the taps in registers: the zero terms add exact zeros
 template <class T>
-__device__ __forceinline__ int restrict_taps(int J, int nf, int nc, int bc, int mode, T wsc, int* idx, T* w) {
-  if (mode == 0) { idx[0] = J; w[0] = (T)1; return 1; }
+__device__ __forceinline__ void restrict_taps(int J, int nf, int nc, int bc, int mode, T wsc, int (&idx)[NN_MAXT],
+                                              T (&w)[NN_MAXT]) {
+#pragma unroll
+  for (int o = 0; o < NN_MAXT; ++o) {
+    idx[o] = 0;
+    w[o] = (T)0;
+  }
+  if (mode == 0) {
+    idx[0] = J;
+    w[0] = (T)1;
+    return;
+  }
   if (mode == 1) {
 #pragma unroll
     for (int o = 0; o < 3; ++o) {
       idx[o] = fine_of(J, o - 1, nf, bc, 1);
       w[o] = o == 1 ? (T)0.5 : (T)0.25;
     }
-    return 3;
+    return;
   }
   int num, den;
   nn_ratio(nf, nc, bc, &num, &den);
   // fine je with |je num - J den| < den, weight (den - d) num / den^2,
   // mapped back by the ghost rule
   const int lo = floor_div(J * den - den, num) + 1, hi = floor_div(J * den + den - 1, num);
-  int t = 0;
-  for (int je = lo; je <= hi && t < NN_MAXT; ++je) {
+#pragma unroll
+  for (int o = 0; o < NN_MAXT; ++o) {
+    const int je = lo + o;
     const int d = abs(je * num - J * den);
-    if (d >= den) continue;
+    if (je > hi || d >= den) continue;
     int j = je;
     if (bc == AX_PERIODIC) j = j < 0 ? j + nf : (j >= nf ? j - nf : j);
     else if (j < 0) j = -j;
     else if (j > nf - 1) j = 2 * (nf - 1) - j;
-    idx[t] = j;
-    w[t] = (T)(den - d) * wsc;
-    ++t;
+    idx[o] = j;
+    w[o] = (T)(den - d) * wsc;
   }
-  return t;
 }
 
 // One thread per coarse point; the taps are summed along x, then y, then z.
@@ -756,16 +895,22 @@ __global__ void __launch_bounds__(256) k_restrict_nn(const T* __restrict__ tf, T
   if (I >= gc.nx || J >= gc.ny) return;
   int xi[NN_MAXT], yi[NN_MAXT], zi[NN_MAXT];
   T xw[NN_MAXT], yw[NN_MAXT], zw[NN_MAXT];
-  const int nxt = restrict_taps<T>(I, gf.nx, gc.nx, gf.bc[0], nn.c[0], nn.wsc[0], xi, xw);
-  const int nyt = restrict_taps<T>(J, gf.ny, gc.ny, gf.bc[1], nn.c[1], nn.wsc[1], yi, yw);
-  const int nzt = restrict_taps<T>(K, gf.nz, gc.nz, gf.bc[2], nn.c[2], nn.wsc[2], zi, zw);
+  restrict_taps<T>(I, gf.nx, gc.nx, gf.bc[0], nn.c[0], nn.wsc[0], xi, xw);
+  restrict_taps<T>(J, gf.ny, gc.ny, gf.bc[1], nn.c[1], nn.wsc[1], yi, yw);
+  restrict_taps<T>(K, gf.nz, gc.nz, gf.bc[2], nn.c[2], nn.wsc[2], zi, zw);
   T acc = (T)0;
-  for (int a = 0; a < nzt; ++a) {
+#pragma unroll
+  for (int a = 0; a < NN_MAXT; ++a) {
+    if (zw[a] == (T)0) continue;
     T accy = (T)0;
-    for (int b = 0; b < nyt; ++b) {
+#pragma unroll
+    for (int b = 0; b < NN_MAXT; ++b) {
+      if (yw[b] == (T)0) continue;
       const T* row = tf + gf.sz() * zi[a] + gf.sy() * yi[b];
       T accx = (T)0;
-      for (int q = 0; q < nxt; ++q) accx += xw[q] * __ldg(row + xi[q]);
+#pragma unroll
+      for (int q = 0; q < NN_MAXT; ++q)
+        if (xw[q] != (T)0) accx += xw[q] * __ldg(row + xi[q]);
       accy += yw[b] * accx;
     }
     acc += zw[a] * accy;
@@ -790,14 +935,18 @@ __global__ void __launch_bounds__(256) k_restrict_nnz(const T* __restrict__ tf, 
   if (I >= gc.nx || J >= gc.ny) return;
   int xi[NN_MAXT], yi[NN_MAXT];
   T xw[NN_MAXT], yw[NN_MAXT];
-  const int nxt = restrict_taps<T>(I, gf.nx, gc.nx, gf.bc[0], nn.c[0], nn.wsc[0], xi, xw);
-  const int nyt = restrict_taps<T>(J, gf.ny, gc.ny, gf.bc[1], nn.c[1], nn.wsc[1], yi, yw);
+  restrict_taps<T>(I, gf.nx, gc.nx, gf.bc[0], nn.c[0], nn.wsc[0], xi, xw);
+  restrict_taps<T>(J, gf.ny, gc.ny, gf.bc[1], nn.c[1], nn.wsc[1], yi, yw);
   auto plane = [&](int k) {
     T accy = (T)0;
-    for (int b = 0; b < nyt; ++b) {
+#pragma unroll
+    for (int b = 0; b < NN_MAXT; ++b) {
+      if (yw[b] == (T)0) continue;
       const T* row = tf + gf.sz() * k + gf.sy() * yi[b];
       T accx = (T)0;
-      for (int q = 0; q < nxt; ++q) accx += xw[q] * __ldg(row + xi[q]);
+#pragma unroll
+      for (int q = 0; q < NN_MAXT; ++q)
+        if (xw[q] != (T)0) accx += xw[q] * __ldg(row + xi[q]);
       accy += yw[b] * accx;
     }
     return accy;
@@ -1127,7 +1276,7 @@ static bool vcycle(MGLevel* lv, int l, int nlev, int pre, int post, int coarse_s
       launch_pdl(k_coarse<T>, 1, coarse_threads(L.g), 0, s, e, r, L.g, c, coarse_sweeps, ctrl);
       *nl += 1;
     } else {
-      launch_pdl(k_smooth_first<T>, g3(L.g), b, 0, s, e, r, L.g, c, (T)1, ctrl);
+      smooth_first<T>(L, e, r, c, (T)1, ctrl, s);
       *nl += 1;
       smooth_sweeps<T>(L, e, r, c, (T)1, coarse_sweeps - 1, ctrl, s, nl);
     }
@@ -1135,12 +1284,12 @@ static bool vcycle(MGLevel* lv, int l, int nlev, int pre, int post, int coarse_s
   }
   int sweeps = pre;
   if (zero_init) {
-    launch_pdl(k_smooth_first<T>, g3(L.g), b, 0, s, e, r, L.g, c, om, ctrl);
+    smooth_first<T>(L, e, r, c, om, ctrl, s);
     *nl += 1;
     sweeps -= 1;
   }
   smooth_sweeps<T>(L, e, r, c, om, sweeps, ctrl, s, nl);
-  launch_pdl(k_resid<T>, g3(L.g), b, 0, s, e, r, (T*)L.t, L.g, c, ctrl);
+  level_resid<T>(L, e, r, (T*)L.t, c, ctrl, s);
   const MGLevel& C = lv[l + 1];
   launch_restrict<T>(L, C, (const T*)L.t, (T*)C.r, ctrl, s);
   *nl += 2;
