@@ -122,8 +122,11 @@ typedef struct o3d_params {
   double mg_omega;        /* relaxation of the red-black smoother; 0 -> 1 (Gauss-Seidel)
                              in FP64, 1.25 mixed */
   int mg_kernels;         /* mixed multigrid: 0 = fused level kernels on the levels large
-                             enough to fill the GPU (at least 152 blocks), 1 = one kernel
-                             per pass, 2 = fused on every level they can serve (same
+                             enough to fill the GPU (at least 152 blocks), except that a
+                             V-cycle from zero with one pre-sweep on a level of 2^22
+                             points or more runs its pre-smoothing, residual and
+                             restriction as one-pass 2.5D kernels; 1 = one kernel per
+                             pass; 2 = fused on every level they can serve (same
                              results in all three; 1 and 2 are for comparison and tests) */
 } o3d_params;
 

@@ -475,8 +475,10 @@ int build_mg(o3d_ctx* c) {
     errf("fused multigrid kernels: %s", cudaGetErrorString(cudaGetLastError()));
     return O3D_ERR_CUDA;
   }
-  for (size_t l = 0; l + 1 < c->mg.size(); ++l)
-    c->mg[l].fused = fuse && mg_fusable(c->mg[l], pre, post, c->P.mg_kernels == 2);
+  for (size_t l = 0; l < c->mg.size(); ++l) {
+    c->mg[l].fused = l + 1 < c->mg.size() && fuse && mg_fusable(c->mg[l], pre, post, c->P.mg_kernels == 2);
+    c->mg[l].fuse_all = c->P.mg_kernels == 2;
+  }
   const size_t tsz = c->mixed ? 4 : 8;
   for (auto& L : c->mg) {
     int st;

@@ -185,14 +185,17 @@ FUSED_CASES = [
     # shape, boundaries, multigrid options, the mg_kernels mode compared with
     # one kernel per pass (1): 2 fuses every level the kernels can serve (at
     # these sizes all but the coarsest, with partial tiles), 0 only the levels
-    # of at least 152 blocks.  The zero-start and from-correction kernels,
-    # V(2,1), V(1,1) and V(1,2), odd free-slip sizes, and fused levels below a
-    # non-nested one.
+    # of at least 152 blocks, and on a level of 2^22 points or more it runs
+    # the pre-smoothing of a V(1, *) cycle from zero, the residual and the
+    # restriction as 2.5D one-pass kernels before the fused k_mg_up.  The
+    # zero-start and from-correction kernels, V(2,1), V(1,1) and V(1,2), odd
+    # free-slip sizes, and fused levels below a non-nested one.
     ((64, 64, 64), (0, 0, 0), {"mg_pre": 2, "mg_post": 1}, 2),
     ((64, 65, 32), (0, 1, 0), {"mg_cycles": 2}, 2),
     ((33, 33, 33), (1, 1, 1), {"mg_pre": 1, "mg_post": 2}, 2),
     ((64, 64, 32), (0, 1, 0), {}, 2),
     ((256, 256, 64), (0, 0, 0), {}, 0),
+    ((256, 256, 64), (0, 0, 0), {}, 2),
 ]
 
 
