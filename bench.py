@@ -293,7 +293,12 @@ def link_rates(host) -> dict:
 KERNEL_BYTES = {
     "predict": (PRED_BYTES_PER_PT, "k_predict25v<float> (two x-adjacent points per thread)"),
     # read r, write e and the coarse rhs (1/8)
-    "mg_down": (4 + 4 + 0.5, "k_mg_down<2,zero> (pre-smoothing + residual + restriction, finest level)"),
+    "mg_down": (4 + 4 + 0.5, "k_mg_down<2,zero> (pre-smoothing + residual + restriction, finest level; "
+                             "the step runs mg_pre and mg_resid there instead)"),
+    # the finest level's first sweep from e = 0 (read r, write e) and its residual (read e, r; write t),
+    # the 2.5D one-pass kernels the step runs before the fused up kernel
+    "mg_pre": (4 + 4, "k_lvl25<1> (first red-black sweep from e = 0, finest level)"),
+    "mg_resid": (4 + 4 + 4, "k_lvl25<2> (level residual, finest level)"),
     # read e, r, p and the coarse correction (1/8), write e and p
     "mg_up": (4 + 4 + 8 + 0.5 + 4 + 8, "k_mg_up<2,update> (prolongation + post-smoothing + p += e, finest)"),
     # read u* (3 x FP32), write the FP32 rhs (its trapezoid-weighted sums ride along)

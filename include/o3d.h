@@ -316,7 +316,9 @@ O3D_API int o3d_sample_ready(const o3d_ctx *ctx);
  * the defect-correction loop, 5 fused pre-smoothing + residual + restriction
  * of the finest level (mixed method, from a zero correction), 6 fused
  * prolongation + post-smoothing + p += e of the finest level (mixed method;
- * the update goes to a scratch copy of p).  The launches only rewrite
+ * the update goes to a scratch copy of p), 7 the finest level's first sweep
+ * from a zero correction and 8 its residual, in the form a large level runs
+ * them before the fused up kernel.  The launches only rewrite
  * scratch outputs (u*, the free flux slot, rhs, the multigrid levels'
  * corrections and residuals) or recompute the velocity identically from u*
  * and p.  No counterpart in the reference (measurement hook). */

@@ -1669,6 +1669,10 @@ void launch_level_kernel(int which, double* p, const R* rhs, const MGLevel& L, S
   PoiCoef<T> c = make_poi<T>(L.h[0], L.h[1], L.h[2]);
   if (which == 0) {
     launch_pdl(k_smooth<T>, g3rb(L.g), dim3(32, 8), 0, s, (T*)L.e, (const T*)L.r, L.g, c, 0, (T)1, ctrl);
+  } else if (which == 2) {  // the first sweep from e = 0 into t, as a large level runs it
+    smooth_first<T>(L, (T*)L.t, (const T*)L.r, c, (T)1.25, ctrl, s);
+  } else if (which == 3) {  // the level residual from t into e
+    level_resid<T>(L, (const T*)L.t, (const T*)L.r, (T*)L.e, c, ctrl, s);
   } else {
     PoiCoef<double> c64 = make_poi<double>(L.h[0], L.h[1], L.h[2]);
     const PPair pp = ppair(p, L.g.n);

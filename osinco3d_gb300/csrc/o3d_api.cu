@@ -476,8 +476,9 @@ int build_mg(o3d_ctx* c) {
     return O3D_ERR_CUDA;
   }
   for (size_t l = 0; l < c->mg.size(); ++l) {
-    c->mg[l].fused = l + 1 < c->mg.size() && fuse && mg_fusable(c->mg[l], pre, post, c->P.mg_kernels == 2);
-    c->mg[l].fuse_all = c->P.mg_kernels == 2;
+    MGLevel& L = c->mg[l];
+    L.fused = l + 1 < c->mg.size() && fuse && mg_fusable(L, pre, post, c->P.mg_kernels == 2);
+    L.fuse_all = c->P.mg_kernels == 2;
   }
   const size_t tsz = c->mixed ? 4 : 8;
   for (auto& L : c->mg) {
@@ -1561,7 +1562,7 @@ int o3d_set_sample_buffers(o3d_ctx* c, float* d_feat, float* d_tgt) {
 int o3d_sample_ready(const o3d_ctx* c) { return c ? c->sample_ready : 0; }
 
 int o3d_time_kernel(o3d_ctx* c, int kernel, int reps, double* ms_per_launch) {
-  if (!c || reps < 1 || !ms_per_launch || kernel < 0 || kernel > 6) {
+  if (!c || reps < 1 || !ms_per_launch || kernel < 0 || kernel > 8) {
     errf("bad o3d_time_kernel request");
     return O3D_ERR_BADARG;
   }
@@ -1605,6 +1606,13 @@ int o3d_time_kernel(o3d_ctx* c, int kernel, int reps, double* ms_per_launch) {
         CKL();
         return O3D_OK;
       }
+      case 7:
+      case 8:
+        if (c->mixed) launch_level_kernel<float, float>(kernel - 5, c->pp, c->rhs32, c->mg[0], c->ctrl, c->s, c->pdf);
+        else launch_level_kernel<double, double>(kernel - 5, c->pp, (const double*)c->rhs, c->mg[0], c->ctrl, c->s, false);
+        c->launches++;
+        CKL();
+        return O3D_OK;
       default:
         if (c->mixed && c->rhs_f32)
           launch_level_kernel<float, float>(kernel - 3, c->pp, c->rhs32, c->mg[0], c->ctrl, c->s, c->pdf);

@@ -461,7 +461,8 @@ class Context:
     def sample_ready(self) -> bool:
         return bool(self.L.o3d_sample_ready(self.h))
 
-    KERNELS = {"predict": 0, "rhs": 1, "correct": 2, "mg_smooth": 3, "resid64": 4, "mg_down": 5, "mg_up": 6}
+    KERNELS = {"predict": 0, "rhs": 1, "correct": 2, "mg_smooth": 3, "resid64": 4, "mg_down": 5, "mg_up": 6,
+               "mg_pre": 7, "mg_resid": 8}
 
     def time_kernel(self, name: str, reps: int = 20) -> float:
         """Milliseconds per launch of one hot kernel on the live state."""
