@@ -125,8 +125,9 @@ typedef struct o3d_params {
                              enough to fill the GPU (at least 152 blocks), except that a
                              V-cycle from zero with one pre-sweep on a level of 2^22
                              points or more runs its pre-smoothing, residual and
-                             restriction as one-pass 2.5D kernels; 1 = one kernel per
-                             pass; 2 = fused on every level they can serve (same
+                             restriction as one-pass 2.5D kernels; 1 = one plain kernel
+                             per pass (no fused, 2.5D or staged forms); 2 = fused on
+                             every level they can serve (same
                              results in all three; 1 and 2 are for comparison and tests) */
 } o3d_params;
 

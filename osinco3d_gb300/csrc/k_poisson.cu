@@ -623,7 +623,7 @@ template <class T>
 static void smooth_first(const MGLevel& L, T* e, const T* r, const PoiCoef<T>& c, T om, const SolveCtrl* ctrl,
                          cudaStream_t s) {
   if constexpr (sizeof(T) == 4) {
-    if (lv_big(L.g)) {
+    if (lv_big(L.g) && !L.plain) {
       launch_pdl(k_lvl25<1>, lv_grid(L.g), dim3(LV_TX, LV_TY), 0, s, (float*)e, (const float*)r, (float*)nullptr, L.g,
                  c, (float)om, 0, ctrl);
       return;
@@ -651,7 +651,7 @@ template <class T>
 static void level_resid(const MGLevel& L, const T* e, const T* r, T* t, const PoiCoef<T>& c, const SolveCtrl* ctrl,
                         cudaStream_t s) {
   if constexpr (sizeof(T) == 4) {
-    if (lv_big(L.g)) {
+    if (lv_big(L.g) && !L.plain) {
       launch_pdl(k_lvl25<2>, lv_grid(L.g), dim3(LV_TX, LV_TY), 0, s, (float*)e, (const float*)r, (float*)t, L.g, c,
                  1.f, 0, ctrl);
       return;

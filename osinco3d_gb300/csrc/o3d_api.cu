@@ -479,6 +479,7 @@ int build_mg(o3d_ctx* c) {
     MGLevel& L = c->mg[l];
     L.fused = l + 1 < c->mg.size() && fuse && mg_fusable(L, pre, post, c->P.mg_kernels == 2);
     L.fuse_all = c->P.mg_kernels == 2;
+    L.plain = c->P.mg_kernels == 1;
   }
   const size_t tsz = c->mixed ? 4 : 8;
   for (auto& L : c->mg) {

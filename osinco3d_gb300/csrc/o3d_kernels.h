@@ -148,6 +148,7 @@ struct MGLevel {
   void* t;          // residual scratch (T); the smoothed e between the fused kernels
   int fused;        // pre/post-smoothing, residual and transfers by k_mg_down / k_mg_up
   int fuse_all;     // k_mg_down even where the 2.5D one-pass kernels would serve (o3d_params.mg_kernels = 2)
+  int plain;        // the plain one-pass kernels only (o3d_params.mg_kernels = 1): the reference path of the tests
 };
 
 // fused FP32 level kernels (k_mgfused.cu)

@@ -30,6 +30,7 @@ CASES = [
     ((44, 25, 21), (2, 1, 1), {}),           # open x axis
     ((64, 24, 16), (0, 0, 0), {"sim2d": 1}),  # 2D mode: no z derivatives
     ((33, 20, 24), (0, 1, 0), {}),           # nx not a multiple of 4: one-point kernel
+    ((132, 24, 16), (0, 1, 0), {}),          # a tile with no ghost-mapped halo
 ]
 
 
