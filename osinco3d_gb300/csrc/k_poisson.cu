@@ -488,9 +488,13 @@ __global__ void __launch_bounds__(256) k_smooth_first(T* __restrict__ e, const T
   }
 }
 
+// with eout, the colour's updated values and the other colour's old ones go
+// to eout (e is left as it was): the first colour pass of a sweep from a
+// correction that must end up in another array
 template <class T>
 __global__ void __launch_bounds__(256) k_smooth(T* __restrict__ e, const T* __restrict__ r, Grid g,
-                                                PoiCoef<T> c, int color, T om, const SolveCtrl* ctrl) {
+                                                PoiCoef<T> c, int color, T om, const SolveCtrl* ctrl,
+                                                T* __restrict__ eout) {
   pdl_enter();
   if (ctrl->done) return;
   const int ih = blockIdx.x * blockDim.x + threadIdx.x;
@@ -498,12 +502,19 @@ __global__ void __launch_bounds__(256) k_smooth(T* __restrict__ e, const T* __re
   const int k = blockIdx.z;
   if (j >= g.ny) return;
   const int i = 2 * ih + ((j + k + color) & 1);
+  if (eout) {  // the other colour's cell of the pair 2 ih, 2 ih + 1
+    const int io = 2 * ih + 1 - ((j + k + color) & 1);
+    if (io < g.nx) {
+      const int qo = idx3(g, io, j, k);
+      eout[qo] = e[qo];
+    }
+  }
   if (i >= g.nx) return;
   const int q = idx3(g, i, j, k);
   const T s = lap6<T>(e, q, nb6(g, i, j, k), c);
   const T ec = e[q];
   const T en = (r[q] - s) * c.invA;
-  e[q] = ec + om * (en - ec);
+  (eout ? eout : e)[q] = ec + om * (en - ec);
 }
 
 int launch_sor_sweep_ctrl(double* p, const double* rhs, const Grid& g, const PoiCoef<double>& c,
@@ -615,7 +626,7 @@ static void smooth_sweeps(const MGLevel& L, T* e, const T* r, const PoiCoef<T>& 
   for (int q = 0; q < n; ++q)
     for (int color = 0; color < 2; ++color)
       launch_pdl(k_smooth<T>, dim3((unsigned)(((L.g.nx + 1) / 2 + 31) / 32), (L.g.ny + 7) / 8, L.g.nz), dim3(32, 8),
-                 0, s, e, r, L.g, c, color, om, ctrl);
+                 0, s, e, r, L.g, c, color, om, ctrl, (T*)nullptr);
   *nl += 2 * n;
 }
 // the first sweep from e = 0 and the residual t = r - A e of a level
@@ -1255,7 +1266,20 @@ static bool vcycle(MGLevel* lv, int l, int nlev, int pre, int post, int coarse_s
   const MGLevel& L = lv[l];
   if constexpr (sizeof(T) == 4) {
     if (L.fused && l + 1 < nlev) {
-      if (zero_init && pre == 1 && lv_big(L.g) && !L.fuse_all) {
+      if (!zero_init && pre == 1 && lv_big(L.g) && !L.fuse_all) {
+        // from the correction in e: its red pass copied into t (red updated,
+        // black kept), the black pass in place on t, then the residual
+        // through e and the restriction, as from zero below
+        const PoiCoef<float> c = make_poi<float>(L.h[0], L.h[1], L.h[2]);
+        const dim3 grb((unsigned)(((L.g.nx + 1) / 2 + 31) / 32), (L.g.ny + 7) / 8, L.g.nz);
+        launch_pdl(k_smooth<float>, grb, dim3(32, 8), 0, s, (float*)L.e, (const float*)L.r, L.g, c, 0, (float)om, ctrl,
+                   (float*)L.t);
+        launch_pdl(k_smooth<float>, grb, dim3(32, 8), 0, s, (float*)L.t, (const float*)L.r, L.g, c, 1, (float)om, ctrl,
+                   (float*)nullptr);
+        level_resid<float>(L, (const float*)L.t, (const float*)L.r, (float*)L.e, c, ctrl, s);
+        launch_restrict<float>(L, lv[l + 1], (const float*)L.e, (float*)lv[l + 1].r, ctrl, s);
+        *nl += 4;
+      } else if (zero_init && pre == 1 && lv_big(L.g) && !L.fuse_all) {
         // one sweep from e = 0, the residual and the restriction as 2.5D
         // one-pass kernels: on a large level they move 24.5 B per point at
         // about 70 % of HBM, faster than k_mg_down's issue-bound march over
@@ -1668,7 +1692,7 @@ void launch_level_kernel(int which, double* p, const R* rhs, const MGLevel& L, S
                          cudaStream_t s, bool pair) {
   PoiCoef<T> c = make_poi<T>(L.h[0], L.h[1], L.h[2]);
   if (which == 0) {
-    launch_pdl(k_smooth<T>, g3rb(L.g), dim3(32, 8), 0, s, (T*)L.e, (const T*)L.r, L.g, c, 0, (T)1, ctrl);
+    launch_pdl(k_smooth<T>, g3rb(L.g), dim3(32, 8), 0, s, (T*)L.e, (const T*)L.r, L.g, c, 0, (T)1, ctrl, (T*)nullptr);
   } else if (which == 2) {  // the first sweep from e = 0 into t, as a large level runs it
     smooth_first<T>(L, (T*)L.t, (const T*)L.r, c, (T)1.25, ctrl, s);
   } else if (which == 3) {  // the level residual from t into e

@@ -518,6 +518,7 @@ __global__ void __launch_bounds__(NT, 3) k_div25v(const float* __restrict__ fx, 
   // TwoSum-compensated FP32 pairs (the weights are powers of two, so each
   // weighted term is exact)
   float sum_hi = 0.f, sum_lo = 0.f, wsum_hi = 0.f, wsum_lo = 0.f;
+  const float rdt = 1.f / dt;
   const float wyy = ((wmask & 2) && (j == 0 || j == g.ny - 1)) ? 0.5f : 1.f;
   const float wxa = (((wmask & 1) && (ia == 0 || ia == g.nx - 1)) ? 0.5f : 1.f) * wyy;
   const float wxb = (((wmask & 1) && (ia + 1 == 0 || ia + 1 == g.nx - 1)) ? 0.5f : 1.f) * wyy;
@@ -560,7 +561,10 @@ __global__ void __launch_bounds__(NT, 3) k_div25v(const float* __restrict__ fx, 
     const float da = ddxa + ddya + ddza, db = ddxb + ddyb + ddzb;
     if (valid) {
       const long long p = out0 + sz * (k0 + lp);
-      const float oa = divide ? da / dt : da, ob = divide ? db / dt : db;
+      // div / dt as a product with 1 / dt, formed once: an IEEE division per
+      // point costs more than the rest of the pair's arithmetic together
+      // (the FP32 rhs then differs from the quotient by at most an ulp)
+      const float oa = divide ? da * rdt : da, ob = divide ? db * rdt : db;
       if (out) {
         if constexpr (sizeof(O) == 8)
           __stcs(reinterpret_cast<double2*>(out + p), make_double2(to_t<double>(oa), to_t<double>(ob)));
@@ -849,6 +853,7 @@ __global__ void __launch_bounds__(NT, 3) k_transeq25v(ScalArgs<float> A, int kc)
   };
 
   const int own = (ty + 3) * VW + 4 + 2 * tx;
+  const float rsc = 1.f / A.sc;
   float2 q[ZQ];
 #pragma unroll
   for (int m = 0; m < ZQ; ++m) q[m] = make_float2(0.f, 0.f);
@@ -937,7 +942,7 @@ __global__ void __launch_bounds__(NT, 3) k_transeq25v(ScalArgs<float> A, int kc)
         const float* d2v = e ? d2b : d2a;
         const float uu = e ? in[0].y : in[0].x, vv = e ? in[1].y : in[1].x, ww = e ? in[2].y : in[2].x;
         float alpha = A.alpha0;
-        if (LES) alpha = alpha + (e ? in[3].y : in[3].x) / A.sc;
+        if (LES) alpha = alpha + (e ? in[3].y : in[3].x) * rsc;  // nu_t / sc as a product (one division per thread)
         const float F = alpha * (d2v[0] + d2v[1] + d2v[2]) - (uu * d1v[0] + vv * d1v[1] + ww * d1v[2]) +
                         (e ? in[4].y : in[4].x);
         float ph = pc[e] + A.adu * F;

@@ -195,6 +195,7 @@ FUSED_CASES = [
     ((33, 33, 33), (1, 1, 1), {"mg_pre": 1, "mg_post": 2}, 2),
     ((64, 64, 32), (0, 1, 0), {}, 2),
     ((256, 256, 64), (0, 0, 0), {}, 0),
+    ((256, 256, 64), (0, 0, 0), {"mg_cycles": 2}, 0),  # the second cycle starts from its correction
     ((256, 256, 64), (0, 0, 0), {}, 2),
     # a large level with a non-nested y axis: its 2.5D one-pass smoothing
     # and residual against the plain kernels
