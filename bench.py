@@ -45,7 +45,9 @@ TRAFFIC_PER_LAUNCH: dict = {
     "mg_up": (288.510464 + 152.460032) * 1e6,     # k_mg_up_tgv256.md
     "predict": (424.591104 + 348.993024) * 1e6,   # k_predict25v_tgv256.md
     "rhs": (208.823552 + 43.305472) * 1e6,        # k_div25v_tgv256.md (the rhs-writing launch)
-    "correct": (352.484864 + 149.464832) * 1e6,   # k_correct25v_tgv256.md
+    "correct": (271.854336 + 144.600320) * 1e6,   # k_correct25vf_tgv256.md
+    "mg_pre": (67.647488 + 24.289280) * 1e6,      # k_lvl25_tgv256.md
+    "mg_resid": (134.770176 + 42.197504) * 1e6,   # k_lvl25_tgv256.md
     "resid64": (204.008448 + 48.967936) * 1e6,    # k_resid25_tgv256.md
 }
 
