@@ -308,7 +308,7 @@ KERNEL_BYTES = {
     # read u* (3 x FP32) and the pressure's FP32 high plane, write u (3 x FP32)
     "correct": (4 * 6 + 4, "k_correct25vf (FP32 high plane of the pressure pair, FP32 velocity)"),
     # read the pressure pair (2 x FP32) and the FP32 rhs, write r (FP32)
-    "resid64": (8 + 4 + 4, "k_resid25<float,float,pair> (double-float residual, finest level)"),
+    "resid64": (8 + 4 + 4, "k_resid25p (double-float residual from the pressure pair, two points per thread)"),
 }
 # the kernel the roofline entry describes: the finest level's fused
 # post-smoothing kernel, the largest single share of the step

@@ -424,6 +424,109 @@ __global__ void __launch_bounds__(RZ_TX * RZ_TY) k_resid25(const double* __restr
   }
 }
 
+// The residual of the mixed method's defect correction with two x-adjacent
+// points per thread (nx a multiple of 64): a block owns a 64 x 8 column, the pair's
+// high and low parts and its FP32 rhs come as float2 loads, the x-y plane
+// of the pressure pair lands in a double-buffered shared tile (high and low
+// planes, 66 x 10 cells with the 1-cell halo), the z-neighbours stay in
+// registers.  Each point's value is df_resid7 of the same operands as in
+// k_resid25<float, float, MAX, pair>, so the two give the same bits.
+// tile rows: column 1 the left halo, columns 2 .. 2 TX + 1 the pairs (even
+// columns, so that a pair is an aligned float2), column 2 TX + 2 the right
+// halo; R2_SW even
+constexpr int R2_TX = 32, R2_TY = 8, R2_KC = 32, R2_SW = 2 * R2_TX + 4;
+static inline dim3 r2_grid(const Grid& g) {
+  return dim3((g.nx + 2 * R2_TX - 1) / (2 * R2_TX), (g.ny + R2_TY - 1) / R2_TY, (g.nz + R2_KC - 1) / R2_KC);
+}
+template <bool MAX>
+__global__ void __launch_bounds__(R2_TX * R2_TY) k_resid25p(PPair pp, const float* __restrict__ rhs,
+                                                            float* __restrict__ r0, Grid g, PoiDF cdf,
+                                                            SolveCtrl* ctrl) {
+  pdl_enter();
+  if (ctrl->done) return;
+  constexpr int TX = R2_TX, TY = R2_TY, SW = R2_SW, PLN = (TY + 2) * SW;
+  __shared__ float th[2][PLN], tl[2][PLN];
+  const int tx = threadIdx.x, ty = threadIdx.y, t = ty * TX + tx;
+  const int i0 = blockIdx.x * 2 * TX, j0 = blockIdx.y * TY;
+  const int ia = i0 + 2 * tx, j = j0 + ty;
+  const bool valid = j < g.ny;  // nx a multiple of 64: every pair is in the grid
+  const int k0 = blockIdx.z * R2_KC, k1 = min(k0 + R2_KC, g.nz);
+  const long long sz = g.sz();
+  bool f;
+  const int jj = ghost(j, g.ny, g.bc[1], &f);
+  const int cxy = ia + g.nx * jj;
+  // halo cell of this thread (t < 2 (TY + 2 TX)): left and right columns, rows below and above
+  const bool hon = t < 2 * (TY + 2 * TX);
+  int hi, hj, hidx;
+  if (t < TY) { hi = i0 - 1; hj = j0 + t; hidx = (t + 1) * SW + 1; }
+  else if (t < 2 * TY) { hi = i0 + 2 * TX; hj = j0 + t - TY; hidx = (t - TY + 1) * SW + 2 * TX + 2; }
+  else if (t < 2 * TY + 2 * TX) { hi = i0 + t - 2 * TY; hj = j0 - 1; hidx = t - 2 * TY + 2; }
+  else { const int u = min(t - 2 * TY - 2 * TX, 2 * TX - 1); hi = i0 + u; hj = j0 + TY; hidx = (TY + 1) * SW + u + 2; }
+  const int hxy = ghost(hi, g.nx, g.bc[0], &f) + g.nx * ghost(hj, g.ny, g.bc[1], &f);
+  const int sc = (ty + 1) * SW + 2 * tx + 2;  // the pair's first cell in the tile (even)
+  auto zoff = [&](int k) { return sz * ghost(k, g.nz, g.bc[2], &f); };
+  const long long out0 = valid ? (long long)ia + (long long)g.nx * j : 0;
+  const DF mean = {ctrl->rhs_mean_h, ctrl->rhs_mean_l};
+  auto ld2f = [&](const float* b, long long q) { return __ldg(reinterpret_cast<const float2*>(b + q)); };
+
+  float2 bh = ld2f(pp.hi, zoff(k0 - 1) + cxy), bl = ld2f(pp.lo, zoff(k0 - 1) + cxy);
+  float2 ch = ld2f(pp.hi, zoff(k0) + cxy), cl = ld2f(pp.lo, zoff(k0) + cxy);
+  float2 nh = ld2f(pp.hi, zoff(k0 + 1) + cxy), nl = ld2f(pp.lo, zoff(k0 + 1) + cxy);
+  float hvh = hon ? __ldg(pp.hi + zoff(k0) + hxy) : 0.f, hvl = hon ? __ldg(pp.lo + zoff(k0) + hxy) : 0.f;
+  float2 rr = valid ? ld2f(rhs, out0 + sz * k0) : make_float2(0.f, 0.f);
+  float m = 0.f;
+  int buf = 0;
+  for (int k = k0; k < k1; ++k) {
+    const float2 th_ = nh, tl_ = nl;  // plane k + 1
+    *reinterpret_cast<float2*>(&th[buf][sc]) = ch;
+    *reinterpret_cast<float2*>(&tl[buf][sc]) = cl;
+    if (hon) {
+      th[buf][hidx] = hvh;
+      tl[buf][hidx] = hvl;
+    }
+    const float2 rcur = rr;
+    if (k + 1 < k1) {
+      nh = ld2f(pp.hi, zoff(k + 2) + cxy);
+      nl = ld2f(pp.lo, zoff(k + 2) + cxy);
+      if (hon) {
+        hvh = __ldg(pp.hi + zoff(k + 1) + hxy);
+        hvl = __ldg(pp.lo + zoff(k + 1) + hxy);
+      }
+      if (valid) rr = ld2f(rhs, out0 + sz * (k + 1));
+    }
+    __syncthreads();
+    if (valid) {
+      const float* H = th[buf];
+      const float* L = tl[buf];
+      float rv[2];
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const int q = sc + e;
+        const DF pc = e ? DF{ch.y, cl.y} : DF{ch.x, cl.x};
+        const DF pw = DF{H[q - 1], L[q - 1]}, pe = DF{H[q + 1], L[q + 1]};
+        const DF ps = DF{H[q - SW], L[q - SW]}, pn = DF{H[q + SW], L[q + SW]};
+        const DF pb = e ? DF{bh.y, bl.y} : DF{bh.x, bl.x}, pt = e ? DF{th_.y, tl_.y} : DF{th_.x, tl_.x};
+        DF rh = DF{e ? rcur.y : rcur.x, 0.f}, rs;  // rhs - mean: exact TwoSum of the high parts, low parts added
+        two_sum(rh.h, -mean.h, rs.h, rs.l);
+        rs.l += rh.l - mean.l;
+        rv[e] = df_resid7(rs, pc, pw, pe, ps, pn, pb, pt, cdf.A, cdf.ox, cdf.oy, cdf.oz);
+      }
+      *reinterpret_cast<float2*>(r0 + out0 + sz * k) = make_float2(rv[0], rv[1]);
+      if (MAX) m = fmaxf(m, fmaxf(fabsf(rv[0]), fabsf(rv[1])));
+    }
+    bh = ch;
+    bl = cl;
+    ch = th_;
+    cl = tl_;
+    buf ^= 1;
+  }
+  if (MAX) {
+    const float bm = block_max_f(m);
+    if (threadIdx.x == 0 && threadIdx.y == 0 && bm > 0.f)
+      atomicMax(&ctrl->res_key, (unsigned long long)__double_as_longlong((double)bm));
+  }
+}
+
 // max |rhs - A p| after a solve (less the rhs mean when shift: the mixed
 // multigrid solve leaves the rhs unshifted)
 template <class R, bool PP>
@@ -616,6 +719,83 @@ __global__ void __launch_bounds__(LV_TX * LV_TY) k_lvl25(float* __restrict__ e, 
   }
 }
 
+// OP 1 and 2 of k_lvl25 with two x-adjacent points per thread, for a level
+// whose nx is a multiple of 64: a block owns a 64 x 8 column, the pair's
+// values come and go as float2, the field's plane lands in a shared tile of
+// 68 x 10 cells (column 1 the left halo, the pairs at even columns 2 ..
+// 65, column 66 the right halo; the tile of k_resid25p).  The same
+// expressions in the same order as k_lvl25: the same bits.
+constexpr int LP_TX = 32, LP_TY = 8, LP_KC = 16, LP_SW = 2 * LP_TX + 4;
+static inline dim3 lp_grid(const Grid& g) {
+  return dim3(g.nx / (2 * LP_TX), (g.ny + LP_TY - 1) / LP_TY, (g.nz + LP_KC - 1) / LP_KC);
+}
+template <int OP>
+__global__ void __launch_bounds__(LP_TX * LP_TY) k_lvl25p(float* __restrict__ e, const float* __restrict__ r,
+                                                          float* __restrict__ t, Grid g, PoiCoef<float> c, float om,
+                                                          const SolveCtrl* ctrl) {
+  pdl_enter();
+  if (ctrl->done) return;
+  constexpr int TX = LP_TX, TY = LP_TY, SW = LP_SW, PLN = (TY + 2) * SW;
+  __shared__ float tile[2][PLN];
+  const float* F = OP == 1 ? r : e;
+  const int tx = threadIdx.x, ty = threadIdx.y, th = ty * TX + tx;
+  const int i0 = blockIdx.x * 2 * TX, j0 = blockIdx.y * TY;
+  const int ia = i0 + 2 * tx, j = j0 + ty;
+  const bool valid = j < g.ny;  // nx a multiple of 64: every pair is in the grid
+  const int k0 = blockIdx.z * LP_KC, k1 = min(k0 + LP_KC, g.nz);
+  const long long sz = g.sz();
+  bool f;
+  const int cxy = ia + g.nx * ghost(j, g.ny, g.bc[1], &f);
+  const bool hon = th < 2 * (TY + 2 * TX);
+  int hi, hj, hidx;
+  if (th < TY) { hi = i0 - 1; hj = j0 + th; hidx = (th + 1) * SW + 1; }
+  else if (th < 2 * TY) { hi = i0 + 2 * TX; hj = j0 + th - TY; hidx = (th - TY + 1) * SW + 2 * TX + 2; }
+  else if (th < 2 * TY + 2 * TX) { hi = i0 + th - 2 * TY; hj = j0 - 1; hidx = th - 2 * TY + 2; }
+  else { const int u = min(th - 2 * TY - 2 * TX, 2 * TX - 1); hi = i0 + u; hj = j0 + TY; hidx = (TY + 1) * SW + u + 2; }
+  const int hxy = ghost(hi, g.nx, g.bc[0], &f) + g.nx * ghost(hj, g.ny, g.bc[1], &f);
+  const int sc = (ty + 1) * SW + 2 * tx + 2;
+  auto zoff = [&](int k) { return sz * ghost(k, g.nz, g.bc[2], &f); };
+  const long long out0 = valid ? (long long)ia + (long long)g.nx * j : 0;
+  auto ld2f = [&](const float* b, long long q) { return __ldg(reinterpret_cast<const float2*>(b + q)); };
+
+  float2 pb = ld2f(F, zoff(k0 - 1) + cxy), pc = ld2f(F, zoff(k0) + cxy), ptn = ld2f(F, zoff(k0 + 1) + cxy);
+  float hv = hon ? __ldg(F + zoff(k0) + hxy) : 0.f;
+  float2 rr = (OP == 2 && valid) ? ld2f(r, out0 + sz * k0) : make_float2(0.f, 0.f);
+  int buf = 0;
+  for (int k = k0; k < k1; ++k) {
+    const float2 pt = ptn;
+    *reinterpret_cast<float2*>(&tile[buf][sc]) = pc;
+    if (hon) tile[buf][hidx] = hv;
+    const float2 rcur = rr;
+    if (k + 1 < k1) {
+      ptn = ld2f(F, zoff(k + 2) + cxy);
+      if (hon) hv = __ldg(F + zoff(k + 1) + hxy);
+      if (OP == 2 && valid) rr = ld2f(r, out0 + sz * (k + 1));
+    }
+    __syncthreads();
+    if (valid) {
+      const float* T0 = tile[buf];
+      float o[2];
+#pragma unroll
+      for (int q2 = 0; q2 < 2; ++q2) {
+        const int q = sc + q2;
+        const float vc = q2 ? pc.y : pc.x, vb = q2 ? pb.y : pb.x, vt = q2 ? pt.y : pt.x;
+        const float s = c.ox * (T0[q - 1] + T0[q + 1]) + c.oy * (T0[q - SW] + T0[q + SW]) + c.oz * (vb + vt);
+        if (OP == 1) {
+          if (((ia + q2 + j + k) & 1) == 0) o[q2] = om * (vc * c.invA);
+          else o[q2] = om * ((vc - om * (s * c.invA)) * c.invA);
+        } else {
+          o[q2] = (q2 ? rcur.y : rcur.x) - (s + c.A * vc);
+        }
+      }
+      *reinterpret_cast<float2*>((OP == 1 ? e : t) + out0 + sz * k) = make_float2(o[0], o[1]);
+    }
+    pb = pc;
+    pc = pt;
+    buf ^= 1;
+  }
+}
+
 // `n` red-black sweeps of A e = r with relaxation om, in place on e
 template <class T>
 static void smooth_sweeps(const MGLevel& L, T* e, const T* r, const PoiCoef<T>& c, T om, int n,
@@ -635,8 +815,12 @@ static void smooth_first(const MGLevel& L, T* e, const T* r, const PoiCoef<T>& c
                          cudaStream_t s) {
   if constexpr (sizeof(T) == 4) {
     if (lv_big(L.g) && !L.plain) {
-      launch_pdl(k_lvl25<1>, lv_grid(L.g), dim3(LV_TX, LV_TY), 0, s, (float*)e, (const float*)r, (float*)nullptr, L.g,
-                 c, (float)om, 0, ctrl);
+      if (L.g.nx % (2 * LP_TX) == 0)
+        launch_pdl(k_lvl25p<1>, lp_grid(L.g), dim3(LP_TX, LP_TY), 0, s, (float*)e, (const float*)r, (float*)nullptr,
+                   L.g, c, (float)om, ctrl);
+      else
+        launch_pdl(k_lvl25<1>, lv_grid(L.g), dim3(LV_TX, LV_TY), 0, s, (float*)e, (const float*)r, (float*)nullptr,
+                   L.g, c, (float)om, 0, ctrl);
       return;
     }
   }
@@ -663,8 +847,12 @@ static void level_resid(const MGLevel& L, const T* e, const T* r, T* t, const Po
                         cudaStream_t s) {
   if constexpr (sizeof(T) == 4) {
     if (lv_big(L.g) && !L.plain) {
-      launch_pdl(k_lvl25<2>, lv_grid(L.g), dim3(LV_TX, LV_TY), 0, s, (float*)e, (const float*)r, (float*)t, L.g, c,
-                 1.f, 0, ctrl);
+      if (L.g.nx % (2 * LP_TX) == 0)
+        launch_pdl(k_lvl25p<2>, lp_grid(L.g), dim3(LP_TX, LP_TY), 0, s, (float*)e, (const float*)r, (float*)t, L.g, c,
+                   1.f, ctrl);
+      else
+        launch_pdl(k_lvl25<2>, lv_grid(L.g), dim3(LV_TX, LV_TY), 0, s, (float*)e, (const float*)r, (float*)t, L.g, c,
+                   1.f, 0, ctrl);
       return;
     }
   }
@@ -1342,6 +1530,16 @@ void launch_mg_resid(double* p, const R* rhs, MGLevel* lv, SolveCtrl* ctrl, cuda
   PoiCoef<double> c64 = make_poi<double>(L0.h[0], L0.h[1], L0.h[2]);
   // the mixed method subtracts the rhs mean here; the FP64 method's rhs was shifted in place
   constexpr bool PP = sizeof(T) == 4;
+  if constexpr (sizeof(T) == 4 && sizeof(R) == 4) {
+    // two points per thread on whole 64-point x tiles: every thread's pair is
+    // in the grid and the x halo is the tile's two edge columns
+    if (L0.g.nx % (2 * R2_TX) == 0 && !L0.plain) {
+      launch_pdl(k_resid25p<true>, r2_grid(L0.g), dim3(R2_TX, R2_TY), 0, s, ppair(p, L0.g.n), (const float*)rhs,
+                 (float*)L0.r, L0.g, poi_df(c64), ctrl);
+      *nl += 1;
+      return;
+    }
+  }
   launch_pdl(k_resid25<T, R, true, PP>, rz_grid(L0.g), dim3(RZ_TX, RZ_TY), 0, s, p, ppair(p, L0.g.n), rhs,
              (T*)L0.r, L0.g, c64, poi_df(c64), ctrl, (int)(sizeof(T) == 4));
   *nl += 1;
@@ -1702,6 +1900,15 @@ void launch_level_kernel(int which, double* p, const R* rhs, const MGLevel& L, S
     const PPair pp = ppair(p, L.g.n);
     if constexpr (sizeof(T) == 4) {
       if (pair) {
+        // the kernel the step runs: two points per thread on whole x tiles
+        // with the FP32 rhs (its rhs less the mean, as in the loop)
+        if constexpr (sizeof(R) == 4) {
+          if (L.g.nx % (2 * R2_TX) == 0 && !L.plain) {
+            launch_pdl(k_resid25p<false>, r2_grid(L.g), dim3(R2_TX, R2_TY), 0, s, pp, (const float*)rhs, (float*)L.r,
+                       L.g, poi_df(c64), ctrl);
+            return;
+          }
+        }
         launch_pdl(k_resid25<T, R, false, true>, rz_grid(L.g), dim3(RZ_TX, RZ_TY), 0, s, p, pp, rhs, (T*)L.r, L.g,
                    c64, poi_df(c64), ctrl, 0);
         return;

@@ -289,3 +289,25 @@ def test_incompatible_rhs_stagnates_like_reference(oracle, o3d):
         st, it, dm, om = ctx.poisson_solve(got, rhs, 1.5, 1e-8, 20000, 0)
     assert st_ref == oracle.SOR_STAGNATED
     assert st == o3d.WARN_STAGNATION
+
+
+def test_two_point_residual_matches_one_point(oracle, o3d):
+    """Mixed multigrid steps with the FP32 rhs on a grid whose nx is a
+    multiple of 64 take the residual with two points per thread; with one
+    plain kernel per pass (mg_kernels = 1) they take the one-point residual.
+    The velocity and the pressure after three steps agree bit for bit."""
+    c = _case(oracle, (128, 32, 32), (0, 0, 0))
+    s = oracle.State.zeros(c)
+    oracle.init_tgv(c, s)
+    out = []
+    for mk in (0, 1):
+        prm = params_of(o3d, c, solver=o3d.SOLVER_MG, precision=o3d.PREC_MIXED, eps=1e-9, kmax=100,
+                        guess=o3d.GUESS_EXTRAPOLATED2, mg_kernels=mk)
+        with o3d.Context(prm) as ctx:
+            for nm, f in zip(("ux", "uy", "uz", "pp"), (s.u[0], s.u[1], s.u[2], s.pp)):
+                ctx.upload(nm, f)
+            for it in range(1, 4):
+                assert ctx.step(it).poisson_status == o3d.OK
+            out.append([ctx.download(nm) for nm in ("ux", "uy", "uz", "pp")])
+    for a, b in zip(*out):
+        np.testing.assert_array_equal(a, b)
