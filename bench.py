@@ -46,9 +46,9 @@ TRAFFIC_PER_LAUNCH: dict = {
     "predict": (424.591104 + 348.993024) * 1e6,   # k_predict25v_tgv256.md
     "rhs": (208.823552 + 43.305472) * 1e6,        # k_div25v_tgv256.md (the rhs-writing launch)
     "correct": (271.854336 + 144.600320) * 1e6,   # k_correct25vf_tgv256.md
-    "mg_pre": (67.647488 + 24.289280) * 1e6,      # k_lvl25_tgv256.md
-    "mg_resid": (134.770176 + 42.197504) * 1e6,   # k_lvl25_tgv256.md
-    "resid64": (204.008448 + 48.967936) * 1e6,    # k_resid25_tgv256.md
+    "mg_pre": (68.070656 + 25.961216) * 1e6,      # k_lvl25_tgv256.md
+    "mg_resid": (138.118144 + 39.967488) * 1e6,   # k_lvl25_tgv256.md
+    "resid64": (208.324352 + 48.478720) * 1e6,    # k_resid25_tgv256.md
 }
 
 
@@ -299,8 +299,8 @@ KERNEL_BYTES = {
                              "the step runs mg_pre and mg_resid there instead)"),
     # the finest level's first sweep from e = 0 (read r, write e) and its residual (read e, r; write t),
     # the 2.5D one-pass kernels the step runs before the fused up kernel
-    "mg_pre": (4 + 4, "k_lvl25<1> (first red-black sweep from e = 0, finest level)"),
-    "mg_resid": (4 + 4 + 4, "k_lvl25<2> (level residual, finest level)"),
+    "mg_pre": (4 + 4, "k_lvl25p<1> (first red-black sweep from e = 0, finest level)"),
+    "mg_resid": (4 + 4 + 4, "k_lvl25p<2> (level residual, finest level)"),
     # read e, r, p and the coarse correction (1/8), write e and p
     "mg_up": (4 + 4 + 8 + 0.5 + 4 + 8, "k_mg_up<2,update> (prolongation + post-smoothing + p += e, finest)"),
     # read u* (3 x FP32), write the FP32 rhs (its trapezoid-weighted sums ride along)
