@@ -302,7 +302,14 @@ KERNEL_BYTES = {
     "mg_pre": (4 + 4, "k_lvl25p<1> (first red-black sweep from e = 0, finest level)"),
     "mg_resid": (4 + 4 + 4, "k_lvl25p<2> (level residual, finest level)"),
     # read e, r, p and the coarse correction (1/8), write e and p
-    "mg_up": (4 + 4 + 8 + 0.5 + 4 + 8, "k_mg_up<2,update> (prolongation + post-smoothing + p += e, finest)"),
+    "mg_up": (4 + 4 + 8 + 0.5 + 4 + 8, "k_mg_up<2,update> (prolongation + post-smoothing + p += e, finest; "
+                                       "mg_kernels = 2 only, the step runs mg_prolong, mg_red and mg_post there)"),
+    # the post-smoothing of the step's finest level as one-pass kernels: the prolongation-add (read e and
+    # the coarse correction, write e), the red pass (read e, r; write e) and the black pass with the
+    # pressure pair's update (read e, r and the pair; write the pair)
+    "mg_prolong": (4 + 0.5 + 4, "k_prolong_cell (prolongation-add, finest level)"),
+    "mg_red": (4 + 4 + 4, "k_smooth<float> colour 0 (red pass, finest level)"),
+    "mg_post": (4 + 4 + 8 + 8, "k_smooth_upd (black pass + p += e on the pressure pair + max|e|, finest level)"),
     # read u* (3 x FP32), write the FP32 rhs (its trapezoid-weighted sums ride along)
     "rhs": (4 * 3 + 4, "k_div25v<float> (Poisson rhs, FP32, with its weighted sums)"),
     # read u* (3 x FP32) and the pressure's FP32 high plane, write u (3 x FP32)
@@ -310,9 +317,9 @@ KERNEL_BYTES = {
     # read the pressure pair (2 x FP32) and the FP32 rhs, write r (FP32)
     "resid64": (8 + 4 + 4, "k_resid25p (double-float residual from the pressure pair, two points per thread)"),
 }
-# the kernel the roofline entry describes: the finest level's fused
-# post-smoothing kernel, the largest single share of the step
-ROOF_KERNEL = "mg_up"
+# the kernel the roofline entry describes: the outer iteration's
+# double-float residual, three launches per step and the largest share of it
+ROOF_KERNEL = "resid64"
 
 
 def kernel_roofline(o3d, ctx, peaks: dict) -> dict:

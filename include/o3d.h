@@ -319,7 +319,10 @@ O3D_API int o3d_sample_ready(const o3d_ctx *ctx);
  * prolongation + post-smoothing + p += e of the finest level (mixed method;
  * the update goes to a scratch copy of p), 7 the finest level's first sweep
  * from a zero correction and 8 its residual, in the form a large level runs
- * them before the fused up kernel.  The launches only rewrite
+ * them before the fused up kernel; 9, 10 and 11 the post-smoothing passes of
+ * the finest level in the cycle that updates the pressure: the
+ * prolongation-add, the red pass and the black pass with p += e (on a
+ * scratch copy of p).  The launches only rewrite
  * scratch outputs (u*, the free flux slot, rhs, the multigrid levels'
  * corrections and residuals) or recompute the velocity identically from u*
  * and p.  No counterpart in the reference (measurement hook). */

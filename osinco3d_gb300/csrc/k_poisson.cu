@@ -594,7 +594,9 @@ __global__ void __launch_bounds__(256) k_smooth_first(T* __restrict__ e, const T
 // with eout, the colour's updated values and the other colour's old ones go
 // to eout (e is left as it was): the first colour pass of a sweep from a
 // correction that must end up in another array
-template <class T>
+// ZP planes per thread (a large level): the loads of all of a thread's
+// planes are issued before its updates, which only read the other colour
+template <class T, int ZP = 1>
 __global__ void __launch_bounds__(256) k_smooth(T* __restrict__ e, const T* __restrict__ r, Grid g,
                                                 PoiCoef<T> c, int color, T om, const SolveCtrl* ctrl,
                                                 T* __restrict__ eout) {
@@ -602,23 +604,43 @@ __global__ void __launch_bounds__(256) k_smooth(T* __restrict__ e, const T* __re
   if (ctrl->done) return;
   const int ih = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
+  const int kb = blockIdx.z * ZP;
   if (j >= g.ny) return;
-  const int i = 2 * ih + ((j + k + color) & 1);
-  if (eout) {  // the other colour's cell of the pair 2 ih, 2 ih + 1
-    const int io = 2 * ih + 1 - ((j + k + color) & 1);
-    if (io < g.nx) {
-      const int qo = idx3(g, io, j, k);
-      eout[qo] = e[qo];
+  T s[ZP], ec[ZP], rq[ZP], eo[ZP];
+#pragma unroll
+  for (int u = 0; u < ZP; ++u) {
+    const int k = kb + u;
+    if (k >= g.nz) break;
+    const int i = 2 * ih + ((j + k + color) & 1);
+    if (eout) {  // the other colour's cell of the pair 2 ih, 2 ih + 1
+      const int io = 2 * ih + 1 - ((j + k + color) & 1);
+      if (io < g.nx) eo[u] = e[idx3(g, io, j, k)];
+    }
+    if (i < g.nx) {
+      const int q = idx3(g, i, j, k);
+      s[u] = lap6<T>(e, q, nb6(g, i, j, k), c);
+      ec[u] = e[q];
+      rq[u] = r[q];
     }
   }
-  if (i >= g.nx) return;
-  const int q = idx3(g, i, j, k);
-  const T s = lap6<T>(e, q, nb6(g, i, j, k), c);
-  const T ec = e[q];
-  const T en = (r[q] - s) * c.invA;
-  (eout ? eout : e)[q] = ec + om * (en - ec);
+#pragma unroll
+  for (int u = 0; u < ZP; ++u) {
+    const int k = kb + u;
+    if (k >= g.nz) break;
+    const int i = 2 * ih + ((j + k + color) & 1);
+    if (eout) {
+      const int io = 2 * ih + 1 - ((j + k + color) & 1);
+      if (io < g.nx) eout[idx3(g, io, j, k)] = eo[u];
+    }
+    if (i < g.nx) {
+      const int q = idx3(g, i, j, k);
+      const T en = (rq[u] - s[u]) * c.invA;
+      (eout ? eout : e)[q] = ec[u] + om * (en - ec[u]);
+    }
+  }
 }
+// planes per thread of a colour pass on a large level
+constexpr int SM_ZP = 4;
 
 int launch_sor_sweep_ctrl(double* p, const double* rhs, const Grid& g, const PoiCoef<double>& c,
                           SolveCtrl* ctrl, cudaStream_t s) {
@@ -645,6 +667,19 @@ static inline dim3 lv_grid(const Grid& g) {
 }
 // the level kernels take the 2.5D form from this size on
 static inline bool lv_big(const Grid& g) { return g.n >= (1LL << 22) && g.nx >= 16 && g.ny >= 8 && g.nz >= 8; }
+
+// one colour pass of the relaxed Gauss-Seidel smoother (k_smooth), SM_ZP
+// planes per thread on a large level
+template <class T>
+static void launch_color(const Grid& g, T* e, const T* r, const PoiCoef<T>& c, int color, T om,
+                         const SolveCtrl* ctrl, T* eout, cudaStream_t s) {
+  const unsigned gx = (unsigned)(((g.nx + 1) / 2 + 31) / 32), gy = (unsigned)((g.ny + 7) / 8);
+  if (lv_big(g))
+    launch_pdl(k_smooth<T, SM_ZP>, dim3(gx, gy, (unsigned)((g.nz + SM_ZP - 1) / SM_ZP)), dim3(32, 8), 0, s, e, r, g,
+               c, color, om, ctrl, eout);
+  else
+    launch_pdl(k_smooth<T, 1>, dim3(gx, gy, (unsigned)g.nz), dim3(32, 8), 0, s, e, r, g, c, color, om, ctrl, eout);
+}
 
 template <int OP>
 __global__ void __launch_bounds__(LV_TX * LV_TY) k_lvl25(float* __restrict__ e, const float* __restrict__ r,
@@ -805,8 +840,7 @@ static void smooth_sweeps(const MGLevel& L, T* e, const T* r, const PoiCoef<T>& 
   // 512 x 256 x 256)
   for (int q = 0; q < n; ++q)
     for (int color = 0; color < 2; ++color)
-      launch_pdl(k_smooth<T>, dim3((unsigned)(((L.g.nx + 1) / 2 + 31) / 32), (L.g.ny + 7) / 8, L.g.nz), dim3(32, 8),
-                 0, s, e, r, L.g, c, color, om, ctrl, (T*)nullptr);
+      launch_color<T>(L.g, e, r, c, color, om, ctrl, (T*)nullptr, s);
   *nl += 2 * n;
 }
 // the first sweep from e = 0 and the residual t = r - A e of a level
@@ -1378,42 +1412,87 @@ __global__ void __launch_bounds__(256) k_update(double* __restrict__ p, PPair pp
 // k_update does, so the pair and the max are those of the two passes.  The
 // black values are not stored: the cycle that updates the pressure is the
 // outer iteration's last, and its correction is not read again.
+// planes per thread of k_smooth_upd: all loads of a thread's planes are in
+// flight together, and a block reduces and publishes its max once for them
+constexpr int SU_ZP = 4;
 __global__ void __launch_bounds__(256) k_smooth_upd(const float* __restrict__ e, const float* __restrict__ r, Grid g,
                                                     PoiCoef<float> c, float om, PPair pp, SolveCtrl* ctrl) {
   pdl_enter();
   if (ctrl->done) return;
   const int ih = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
+  const int kb = blockIdx.z * SU_ZP;
   float m = 0.f;
-  if (j < g.ny) {
-    const int par = (j + k + 1) & 1;
-    const int i = 2 * ih + par, io = 2 * ih + 1 - par;  // the black cell and its red partner
-    if (io < g.nx) {
-      const int qo = idx3(g, io, j, k);
-      const float ev = e[qo];
-      float h = pp.hi[qo], l = pp.lo[qo];
-      df_add_f(h, l, ev);
-      pp.hi[qo] = h;
-      pp.lo[qo] = l;
-      m = fmaxf(m, fabsf(ev));
+  if (j < g.ny && (g.nx & 1) == 0) {
+    // even nx: the pair starts at an even offset, and the correction and
+    // both planes of the pressure pair move as float2
+    if (2 * ih < g.nx) {
+      float2 e2[SU_ZP], h2[SU_ZP], l2[SU_ZP];
+      float sl[SU_ZP], rq[SU_ZP];
+#pragma unroll
+      for (int u = 0; u < SU_ZP; ++u) {
+        const int k = kb + u;
+        if (k < g.nz) {
+          const int par = (j + k + 1) & 1;
+          const int q0 = idx3(g, 2 * ih, j, k), q = q0 + par;
+          e2[u] = *reinterpret_cast<const float2*>(e + q0);
+          sl[u] = lap6<float>(e, q, nb6(g, 2 * ih + par, j, k), c);
+          rq[u] = r[q];
+          h2[u] = *reinterpret_cast<const float2*>(pp.hi + q0);
+          l2[u] = *reinterpret_cast<const float2*>(pp.lo + q0);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < SU_ZP; ++u) {
+        const int k = kb + u;
+        if (k < g.nz) {
+          const int par = (j + k + 1) & 1;
+          const int q0 = idx3(g, 2 * ih, j, k);
+          const float ec = par ? e2[u].y : e2[u].x;
+          const float en = (rq[u] - sl[u]) * c.invA;
+          const float ev = ec + om * (en - ec);
+          const float v0 = par ? e2[u].x : ev, v1 = par ? ev : e2[u].y;
+          df_add_f(h2[u].x, l2[u].x, v0);
+          df_add_f(h2[u].y, l2[u].y, v1);
+          *reinterpret_cast<float2*>(pp.hi + q0) = h2[u];
+          *reinterpret_cast<float2*>(pp.lo + q0) = l2[u];
+          m = fmaxf(m, fmaxf(fabsf(v0), fabsf(v1)));
+        }
+      }
     }
-    if (i < g.nx) {
-      const int q = idx3(g, i, j, k);
-      const float sl = lap6<float>(e, q, nb6(g, i, j, k), c);
-      const float ec = e[q];
-      const float en = (r[q] - sl) * c.invA;
-      const float ev = ec + om * (en - ec);
-      float h = pp.hi[q], l = pp.lo[q];
-      df_add_f(h, l, ev);
-      pp.hi[q] = h;
-      pp.lo[q] = l;
-      m = fmaxf(m, fabsf(ev));
+  } else if (j < g.ny) {
+    for (int k = kb; k < kb + SU_ZP && k < g.nz; ++k) {
+      const int par = (j + k + 1) & 1;
+      const int i = 2 * ih + par, io = 2 * ih + 1 - par;  // the black cell and its red partner
+      if (io < g.nx) {
+        const int qo = idx3(g, io, j, k);
+        const float ev = e[qo];
+        float h = pp.hi[qo], l = pp.lo[qo];
+        df_add_f(h, l, ev);
+        pp.hi[qo] = h;
+        pp.lo[qo] = l;
+        m = fmaxf(m, fabsf(ev));
+      }
+      if (i < g.nx) {
+        const int q = idx3(g, i, j, k);
+        const float sl = lap6<float>(e, q, nb6(g, i, j, k), c);
+        const float ec = e[q];
+        const float en = (r[q] - sl) * c.invA;
+        const float ev = ec + om * (en - ec);
+        float h = pp.hi[q], l = pp.lo[q];
+        df_add_f(h, l, ev);
+        pp.hi[q] = h;
+        pp.lo[q] = l;
+        m = fmaxf(m, fabsf(ev));
+      }
     }
   }
   const float bm = block_max_f(m);
   if (threadIdx.x == 0 && threadIdx.y == 0 && bm > 0.f)
     atomicMax(&ctrl->dmax_key, (unsigned long long)__double_as_longlong((double)bm));
+}
+static dim3 su_grid(const Grid& g) {
+  return dim3((unsigned)(((g.nx + 1) / 2 + 31) / 32), (g.ny + 7) / 8, (g.nz + SU_ZP - 1) / SU_ZP);
 }
 
 // the last post-smoothing sweep's two colour passes, the black one with the
@@ -1421,9 +1500,8 @@ __global__ void __launch_bounds__(256) k_smooth_upd(const float* __restrict__ e,
 // the sweep and k_update: 1.8 % of the 512 x 256 x 256 mixing-layer step)
 static void smooth_last_upd(const MGLevel& L, float* e, const float* r, const PoiCoef<float>& c, float om,
                             double* p, SolveCtrl* ctrl, cudaStream_t s, long long* nl) {
-  const dim3 grb((unsigned)(((L.g.nx + 1) / 2 + 31) / 32), (L.g.ny + 7) / 8, L.g.nz);
-  launch_pdl(k_smooth<float>, grb, dim3(32, 8), 0, s, e, r, L.g, c, 0, om, (const SolveCtrl*)ctrl, (float*)nullptr);
-  launch_pdl(k_smooth_upd, grb, dim3(32, 8), 0, s, (const float*)e, r, L.g, c, om, ppair(p, L.g.n), ctrl);
+  launch_color<float>(L.g, e, r, c, 0, om, ctrl, (float*)nullptr, s);
+  launch_pdl(k_smooth_upd, su_grid(L.g), dim3(32, 8), 0, s, (const float*)e, r, L.g, c, om, ppair(p, L.g.n), ctrl);
   *nl += 2;
 }
 
@@ -1445,7 +1523,6 @@ __global__ void k_mg_control(SolveCtrl* c) {
 }
 
 static inline dim3 g3(const Grid& g) { return dim3((g.nx + 31) / 32, (g.ny + 7) / 8, g.nz); }
-static inline dim3 g3rb(const Grid& g) { return dim3((unsigned)(((g.nx + 1) / 2 + 31) / 32), (g.ny + 7) / 8, g.nz); }
 
 // the host constants of a level's non-nested transfer
 template <class T>
@@ -1499,6 +1576,20 @@ static void launch_prolong_add(const MGLevel& L, const MGLevel& C, T* ef, const 
     launch_pdl(k_prolong<T>, g3(L.g), b, 0, s, ef, ec, L.g, C.g, cz, ctrl);
 }
 
+void launch_post_pass(int which, const MGLevel& L, const MGLevel& C, float om, double* p, SolveCtrl* ctrl,
+                      cudaStream_t s) {
+  const PoiCoef<float> c = make_poi<float>(L.h[0], L.h[1], L.h[2]);
+  float* t = (float*)L.t;
+  const float* r = (const float*)L.r;
+  if (which == 0)
+    launch_prolong_add<float>(L, C, t, (const float*)C.e, ctrl, s);
+  else if (which == 1)
+    launch_color<float>(L.g, t, r, c, 0, om, ctrl, (float*)nullptr, s);
+  else
+    launch_pdl(k_smooth_upd, su_grid(L.g), dim3(32, 8), 0, s, (const float*)t, r, L.g, c, om, ppair(p, L.g.n),
+               ctrl);
+}
+
 // One V-cycle on level l for A e = r, from e = 0 (zero_init: the first
 // sweep in one pass from r) or from the current e.
 // On a fused level (FP32 only) k_mg_down and k_mg_up do the level's work;
@@ -1516,11 +1607,8 @@ static bool vcycle(MGLevel* lv, int l, int nlev, int pre, int post, int coarse_s
         // black kept), the black pass in place on t, then the residual
         // through e and the restriction, as from zero below
         const PoiCoef<float> c = make_poi<float>(L.h[0], L.h[1], L.h[2]);
-        const dim3 grb((unsigned)(((L.g.nx + 1) / 2 + 31) / 32), (L.g.ny + 7) / 8, L.g.nz);
-        launch_pdl(k_smooth<float>, grb, dim3(32, 8), 0, s, (float*)L.e, (const float*)L.r, L.g, c, 0, (float)om, ctrl,
-                   (float*)L.t);
-        launch_pdl(k_smooth<float>, grb, dim3(32, 8), 0, s, (float*)L.t, (const float*)L.r, L.g, c, 1, (float)om, ctrl,
-                   (float*)nullptr);
+        launch_color<float>(L.g, (float*)L.e, (const float*)L.r, c, 0, (float)om, ctrl, (float*)L.t, s);
+        launch_color<float>(L.g, (float*)L.t, (const float*)L.r, c, 1, (float)om, ctrl, (float*)nullptr, s);
         level_resid<float>(L, (const float*)L.t, (const float*)L.r, (float*)L.e, c, ctrl, s);
         launch_restrict<float>(L, lv[l + 1], (const float*)L.e, (float*)lv[l + 1].r, ctrl, s);
         *nl += 4;
@@ -1540,6 +1628,16 @@ static bool vcycle(MGLevel* lv, int l, int nlev, int pre, int post, int coarse_s
         *nl += 1;
       }
       vcycle<T>(lv, l + 1, nlev, pre, post, coarse_sweeps, om, ctrl, s, nl, true);
+      if (p_upd && post == 1 && lv_big(L.g) && !L.fuse_all) {
+        // the cycle that updates the pressure: the prolongation-add into the
+        // smoothed e (in t), its red pass and the black pass with the pair's
+        // update as one-pass kernels (44.5 B per point near the HBM roofline,
+        // 2.7 % of the 256^3 step faster than k_mg_up's 28.5 B per point
+        // issue-bound march)
+        for (int w = 0; w < 3; ++w) launch_post_pass(w, L, lv[l + 1], (float)om, p_upd, ctrl, s);
+        *nl += 3;
+        return true;
+      }
       launch_mg_up(L, lv[l + 1], (float)om, post, p_upd, ctrl, s);
       *nl += 1;
       return p_upd != nullptr;
@@ -1954,7 +2052,7 @@ void launch_level_kernel(int which, double* p, const R* rhs, const MGLevel& L, S
                          cudaStream_t s, bool pair) {
   PoiCoef<T> c = make_poi<T>(L.h[0], L.h[1], L.h[2]);
   if (which == 0) {
-    launch_pdl(k_smooth<T>, g3rb(L.g), dim3(32, 8), 0, s, (T*)L.e, (const T*)L.r, L.g, c, 0, (T)1, ctrl, (T*)nullptr);
+    launch_color<T>(L.g, (T*)L.e, (const T*)L.r, c, 0, (T)1, ctrl, (T*)nullptr, s);
   } else if (which == 2) {  // the first sweep from e = 0 into t, as a large level runs it
     smooth_first<T>(L, (T*)L.t, (const T*)L.r, c, (T)1.25, ctrl, s);
   } else if (which == 3) {  // the level residual from t into e

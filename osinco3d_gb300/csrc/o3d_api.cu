@@ -1563,7 +1563,7 @@ int o3d_set_sample_buffers(o3d_ctx* c, float* d_feat, float* d_tgt) {
 int o3d_sample_ready(const o3d_ctx* c) { return c ? c->sample_ready : 0; }
 
 int o3d_time_kernel(o3d_ctx* c, int kernel, int reps, double* ms_per_launch) {
-  if (!c || reps < 1 || !ms_per_launch || kernel < 0 || kernel > 8) {
+  if (!c || reps < 1 || !ms_per_launch || kernel < 0 || kernel > 11) {
     errf("bad o3d_time_kernel request");
     return O3D_ERR_BADARG;
   }
@@ -1573,11 +1573,11 @@ int o3d_time_kernel(o3d_ctx* c, int kernel, int reps, double* ms_per_launch) {
       int st = build_mg(c);
       if (st) return st;
     }
-    if (kernel >= 5 && !(c->mg.size() > 1 && c->mg[0].fused)) {
+    if (kernel >= 5 && kernel != 7 && kernel != 8 && !(c->mg.size() > 1 && c->mg[0].fused)) {
       errf("o3d_time_kernel: the finest level does not run the fused multigrid kernels");
       return O3D_ERR_BADARG;
     }
-    if (kernel == 6) {
+    if (kernel == 6 || kernel == 11) {
       CK(cudaMalloc(&p_scratch, (size_t)c->g.n * 8));
       CK(cudaMemcpyAsync(p_scratch, c->pp, (size_t)c->g.n * 8, cudaMemcpyDeviceToDevice, c->s));
     }
@@ -1607,6 +1607,13 @@ int o3d_time_kernel(o3d_ctx* c, int kernel, int reps, double* ms_per_launch) {
         CKL();
         return O3D_OK;
       }
+      case 9:
+      case 10:
+      case 11:
+        launch_post_pass(kernel - 9, c->mg[0], c->mg[1], (float)mg_omega_of(c), p_scratch, c->ctrl, c->s);
+        c->launches++;
+        CKL();
+        return O3D_OK;
       case 7:
       case 8:
         if (c->mixed) launch_level_kernel<float, float>(kernel - 5, c->pp, c->rhs32, c->mg[0], c->ctrl, c->s, c->pdf);

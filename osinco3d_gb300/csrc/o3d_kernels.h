@@ -224,6 +224,12 @@ void launch_learn_target(const double* p, const double* pprev, MGLevel* lv, int 
 template <class T, class R>
 void launch_level_kernel(int which, double* p, const R* rhs, const MGLevel& L, SolveCtrl* ctrl,
                          cudaStream_t s, bool pair);
+// one pass of the post-smoothing of a large fused level as the step runs it
+// on the finest level of the cycle that updates the pressure, for timing:
+// 0 the prolongation-add into t (k_prolong_cell), 1 the red pass in place on
+// t (k_smooth), 2 the black pass with the pair update p += e (k_smooth_upd)
+void launch_post_pass(int which, const MGLevel& L, const MGLevel& C, float om, double* p, SolveCtrl* ctrl,
+                      cudaStream_t s);
 template <class R>
 void launch_rhs_wmean(const R* rhs, const Grid& g, double* part, SolveCtrl* ctrl, cudaStream_t s,
                       long long* nl);

@@ -462,7 +462,7 @@ class Context:
         return bool(self.L.o3d_sample_ready(self.h))
 
     KERNELS = {"predict": 0, "rhs": 1, "correct": 2, "mg_smooth": 3, "resid64": 4, "mg_down": 5, "mg_up": 6,
-               "mg_pre": 7, "mg_resid": 8}
+               "mg_pre": 7, "mg_resid": 8, "mg_prolong": 9, "mg_red": 10, "mg_post": 11}
 
     def time_kernel(self, name: str, reps: int = 20) -> float:
         """Milliseconds per launch of one hot kernel on the live state."""
