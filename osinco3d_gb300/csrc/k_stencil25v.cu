@@ -1042,62 +1042,69 @@ __global__ void __launch_bounds__(NT, 3) k_correct25vf(CorrArgs<float, float> A,
 #pragma unroll
   for (int a = 0; a < 3; ++a) { mn[a] = INFINITY; mx[a] = -INFINITY; am[a] = 0.f; }
   bool nan = false;
+  // the plane loop unrolled by the ring's length: every ring stage and
+  // z-queue slot index is a constant (plane lp - 3 + m in slot (u + m) % ZQ;
+  // 108 -> 102 us at 256^3.  The larger predictor, divergence and scalar
+  // bodies ran slower unrolled and keep the rotating queue.)
 #pragma unroll 1
-  for (int lp = 0; lp < np; ++lp) {
-    cp_async_wait<PD - 1>();
-    __syncthreads();
-    issue(lp + 3 + PD, (lp + 3 + PD) % ZQ);
-    const float* s = sm.s[lp % ZQ];
-    if constexpr (zon) q[6] = lds2(&sm.s[(lp + 3) % ZQ][own]);
-    float w[10];
+  for (int lb = 0; lb < np; lb += ZQ) {
 #pragma unroll
-    for (int m = 0; m < 5; ++m) {
-      const float2 p2 = lds2(&s[own - 4 + 2 * m]);
-      w[2 * m] = p2.x;
-      w[2 * m + 1] = p2.y;
-    }
-    float ga[3], gb[3];
-    ga[0] = d1x<XO>(w + 1, A.cf.ax[0], pca);
-    gb[0] = d1x<XO>(w + 2, A.cf.ax[0], pcb);
-    float va[7], vb[7];
+    for (int u = 0; u < ZQ; ++u) {
+      const int lp = lb + u;
+      if (lp >= np) break;
+      cp_async_wait<PD - 1>();
+      __syncthreads();
+      issue(lp + 3 + PD, (u + 3 + PD) % ZQ);
+      const float* s = sm.s[u];
+      if constexpr (zon) q[(u + 6) % ZQ] = lds2(&sm.s[(u + 3) % ZQ][own]);
+      float w[10];
 #pragma unroll
-    for (int m = 0; m < 7; ++m) {
-      const float2 p2 = lds2(&s[own + (m - 3) * VW]);
-      va[m] = p2.x;
-      vb[m] = p2.y;
-    }
-    ga[1] = d1(va, A.cf.ax[1]);
-    gb[1] = d1(vb, A.cf.ax[1]);
-    ga[2] = gb[2] = 0.f;
-    if constexpr (zon) {
+      for (int m = 0; m < 5; ++m) {
+        const float2 p2 = lds2(&s[own - 4 + 2 * m]);
+        w[2 * m] = p2.x;
+        w[2 * m + 1] = p2.y;
+      }
+      float ga[3], gb[3];
+      ga[0] = d1x<XO>(w + 1, A.cf.ax[0], pca);
+      gb[0] = d1x<XO>(w + 2, A.cf.ax[0], pcb);
+      float va[7], vb[7];
 #pragma unroll
       for (int m = 0; m < 7; ++m) {
-        va[m] = q[m].x;
-        vb[m] = q[m].y;
+        const float2 p2 = lds2(&s[own + (m - 3) * VW]);
+        va[m] = p2.x;
+        vb[m] = p2.y;
       }
-      ga[2] = d1(va, A.cf.ax[2]);
-      gb[2] = d1(vb, A.cf.ax[2]);
+      ga[1] = d1(va, A.cf.ax[1]);
+      gb[1] = d1(vb, A.cf.ax[1]);
+      ga[2] = gb[2] = 0.f;
+      if constexpr (zon) {
 #pragma unroll
-      for (int m = 0; m < ZQ - 1; ++m) q[m] = q[m + 1];
-    }
-    if (valid) {
-      const long long p = out0 + sz * (k0 + lp);
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        float na = us[a].x - A.dt * ga[a], nb = us[a].y - A.dt * gb[a];
-        if (XO) {  // inflow nodes keep their value
-          if (pca == 1) na = us[a].x;
-          if (pcb == 1) nb = us[a].y;
+        for (int m = 0; m < 7; ++m) {
+          va[m] = q[(u + m) % ZQ].x;
+          vb[m] = q[(u + m) % ZQ].y;
         }
-        __stcs(reinterpret_cast<float2*>(A.u[a] + p), make_float2(na, nb));
-        if (na != na || nb != nb) nan = true;
-        mn[a] = fminf(mn[a], fminf(na, nb));
-        mx[a] = fmaxf(mx[a], fmaxf(na, nb));
-        am[a] = fmaxf(am[a], fmaxf(fabsf(na), fabsf(nb)));
+        ga[2] = d1(va, A.cf.ax[2]);
+        gb[2] = d1(vb, A.cf.ax[2]);
       }
-      if (lp + 1 < np) {
+      if (valid) {
+        const long long p = out0 + sz * (k0 + lp);
 #pragma unroll
-        for (int a = 0; a < 3; ++a) us[a] = ld_stream2(A.up[a] + p + sz);
+        for (int a = 0; a < 3; ++a) {
+          float na = us[a].x - A.dt * ga[a], nb = us[a].y - A.dt * gb[a];
+          if (XO) {  // inflow nodes keep their value
+            if (pca == 1) na = us[a].x;
+            if (pcb == 1) nb = us[a].y;
+          }
+          __stcs(reinterpret_cast<float2*>(A.u[a] + p), make_float2(na, nb));
+          if (na != na || nb != nb) nan = true;
+          mn[a] = fminf(mn[a], fminf(na, nb));
+          mx[a] = fmaxf(mx[a], fmaxf(na, nb));
+          am[a] = fmaxf(am[a], fmaxf(fabsf(na), fabsf(nb)));
+        }
+        if (lp + 1 < np) {
+#pragma unroll
+          for (int a = 0; a < 3; ++a) us[a] = ld_stream2(A.up[a] + p + sz);
+        }
       }
     }
   }
