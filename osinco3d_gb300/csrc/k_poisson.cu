@@ -476,6 +476,9 @@ __global__ void __launch_bounds__(R2_TX * R2_TY) k_resid25p(PPair pp, const floa
   float2 rr = valid ? ld2f(rhs, out0 + sz * k0) : make_float2(0.f, 0.f);
   float m = 0.f;
   int buf = 0;
+  // (unrolled by two: the tile buffer and the plane queue's registers are
+  // fixed in each half)
+#pragma unroll 2
   for (int k = k0; k < k1; ++k) {
     const float2 th_ = nh, tl_ = nl;  // plane k + 1
     *reinterpret_cast<float2*>(&th[buf][sc]) = ch;
@@ -503,7 +506,9 @@ __global__ void __launch_bounds__(R2_TX * R2_TY) k_resid25p(PPair pp, const floa
       for (int e = 0; e < 2; ++e) {
         const int q = sc + e;
         const DF pc = e ? DF{ch.y, cl.y} : DF{ch.x, cl.x};
-        const DF pw = DF{H[q - 1], L[q - 1]}, pe = DF{H[q + 1], L[q + 1]};
+        // the x-neighbour inside the pair from registers, the other from the tile
+        const DF pw = e ? DF{ch.x, cl.x} : DF{H[q - 1], L[q - 1]};
+        const DF pe = e ? DF{H[q + 1], L[q + 1]} : DF{ch.y, cl.y};
         const DF ps = DF{H[q - SW], L[q - SW]}, pn = DF{H[q + SW], L[q + SW]};
         const DF pb = e ? DF{bh.y, bl.y} : DF{bh.x, bl.x}, pt = e ? DF{th_.y, tl_.y} : DF{th_.x, tl_.x};
         DF rh = DF{e ? rcur.y : rcur.x, 0.f}, rs;  // rhs - mean: exact TwoSum of the high parts, low parts added
@@ -936,6 +941,11 @@ __global__ void __launch_bounds__(256) k_restrict(const T* __restrict__ tf, T* _
 
 // full weighting when every axis is coarsened: the 3 x 3 x 3 fine block of
 // each coarse point, offsets resolved once per axis, separable weights
+// A thread marches RF_KZ coarse planes along z: the fine plane 2K + 1, the
+// last of coarse plane K's three, is the first of K + 1's, so its nine
+// values stay in registers (18 loads per coarse point instead of 27).  The
+// sum of every coarse point still runs over its 27 terms in the same order.
+constexpr int RF_KZ = 4;
 template <class T>
 __global__ void __launch_bounds__(256) k_restrict_full(const T* __restrict__ tf, T* __restrict__ rc, Grid gf,
                                                        Grid gc, const SolveCtrl* ctrl) {
@@ -943,26 +953,43 @@ __global__ void __launch_bounds__(256) k_restrict_full(const T* __restrict__ tf,
   if (ctrl->done) return;
   const int I = blockIdx.x * blockDim.x + threadIdx.x;
   const int J = blockIdx.y * blockDim.y + threadIdx.y;
-  const int K = blockIdx.z;
+  const int K0 = blockIdx.z * RF_KZ;
   if (I >= gc.nx || J >= gc.ny) return;
-  int xo[3], yo[3], zo[3];
+  int xo[3], yo[3];
 #pragma unroll
   for (int o = 0; o < 3; ++o) {
     xo[o] = fine_of(I, o - 1, gf.nx, gf.bc[0], 1);
     yo[o] = gf.nx * fine_of(J, o - 1, gf.ny, gf.bc[1], 1);
-    zo[o] = gf.nx * gf.ny * fine_of(K, o - 1, gf.nz, gf.bc[2], 1);
   }
   const T w[3] = {(T)0.25, (T)0.5, (T)0.25};
-  T acc = (T)0;
+  const long long sz = (long long)gf.nx * gf.ny;
+  auto plane = [&](int kf, T v[3][3]) {
+    const T* base = tf + sz * kf;
 #pragma unroll
-  for (int oz = 0; oz < 3; ++oz)
+    for (int oy = 0; oy < 3; ++oy)
 #pragma unroll
-    for (int oy = 0; oy < 3; ++oy) {
-      const T* row = tf + zo[oz] + yo[oy];
+      for (int ox = 0; ox < 3; ++ox) v[oy][ox] = __ldg(base + yo[oy] + xo[ox]);
+  };
+  T pl[3][3][3];  // the fine planes 2K - 1, 2K, 2K + 1
+  plane(fine_of(K0, -1, gf.nz, gf.bc[2], 1), pl[0]);
+  for (int K = K0; K < K0 + RF_KZ && K < gc.nz; ++K) {
+    if (K > K0) {
 #pragma unroll
-      for (int ox = 0; ox < 3; ++ox) acc += w[oz] * w[oy] * w[ox] * __ldg(row + xo[ox]);
+      for (int oy = 0; oy < 3; ++oy)
+#pragma unroll
+        for (int ox = 0; ox < 3; ++ox) pl[0][oy][ox] = pl[2][oy][ox];
     }
-  rc[idx3(gc, I, J, K)] = acc;
+    plane(fine_of(K, 0, gf.nz, gf.bc[2], 1), pl[1]);
+    plane(fine_of(K, 1, gf.nz, gf.bc[2], 1), pl[2]);
+    T acc = (T)0;
+#pragma unroll
+    for (int oz = 0; oz < 3; ++oz)
+#pragma unroll
+      for (int oy = 0; oy < 3; ++oy)
+#pragma unroll
+        for (int ox = 0; ox < 3; ++ox) acc += w[oz] * w[oy] * w[ox] * pl[oz][oy][ox];
+    rc[idx3(gc, I, J, K)] = acc;
+  }
 }
 
 // coarse indices and weights of fine index i along one axis
@@ -1554,7 +1581,8 @@ static void launch_restrict(const MGLevel& L, const MGLevel& C, const T* tf, T* 
   else if (cz.c[0] == 2 || cz.c[1] == 2 || cz.c[2] == 2)
     launch_pdl(k_restrict_nn<T>, g3(C.g), b, 0, s, tf, rc, L.g, C.g, nn_xfer<T>(L, C), ctrl);
   else if (cz.c[0] && cz.c[1] && cz.c[2])
-    launch_pdl(k_restrict_full<T>, g3(C.g), b, 0, s, tf, rc, L.g, C.g, ctrl);
+    launch_pdl(k_restrict_full<T>, dim3((C.g.nx + 31) / 32, (C.g.ny + 7) / 8, (C.g.nz + RF_KZ - 1) / RF_KZ), b, 0, s,
+               tf, rc, L.g, C.g, ctrl);
   else
     launch_pdl(k_restrict<T>, g3(C.g), b, 0, s, tf, rc, L.g, C.g, cz, ctrl);
 }
