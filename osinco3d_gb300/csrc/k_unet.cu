@@ -458,7 +458,11 @@ __global__ void k_pack_input(const float* __restrict__ in, int nch, long long nv
 // of clock); a wait that runs out sets g_tc_timeout and the CTA finishes
 // without further waits.
 // ---------------------------------------------------------------------------
-constexpr int TC_M = 128, TC_THREADS = 128, TC_STAGES = 4;
+// TC_STAGES stages, copies started TC_LA steps ahead: a stage is refilled
+// TC_STAGES - TC_LA steps after the MMA that read it was issued, so the
+// wait for that MMA rarely stalls (with 4 stages and 3 ahead every step
+// waited for the previous step's MMA)
+constexpr int TC_M = 128, TC_THREADS = 128, TC_STAGES = 8, TC_LA = 4;
 constexpr int TC_A_BYTES = TC_M * 32;  // 128 rows x 16 BF16
 
 __device__ int g_tc_timeout;
@@ -581,14 +585,14 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv3_tc(ConvArgs A, int ncols) 
 
   bool ok_all = true;
 #pragma unroll 1
-  for (int i = 0; i < TC_STAGES - 1; ++i) {
+  for (int i = 0; i < TC_LA; ++i) {
     if (i < nsteps) load(q0 + i, i);
     cp_async_commit();
   }
 #pragma unroll 1
   for (int i = 0; i < nsteps; ++i) {
     const int st = i % TC_STAGES;
-    const int nx = i + TC_STAGES - 1;  // the step whose copies start now
+    const int nx = i + TC_LA;  // the step whose copies start now
     if (nx < nsteps) {
       const int sn = nx % TC_STAGES;
       // its stage was last read by the MMA of step nx - TC_STAGES
@@ -596,7 +600,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv3_tc(ConvArgs A, int ncols) 
       load(q0 + nx, sn);
     }
     cp_async_commit();
-    cp_async_wait<TC_STAGES - 1>();  // step i's copies landed
+    cp_async_wait<TC_LA>();  // step i's copies landed
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     ok_all = __syncthreads_and(ok_all) != 0;  // one verdict for the CTA: after a timeout nobody waits again
     if (t == 0 && ok_all) {
