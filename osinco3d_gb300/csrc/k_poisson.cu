@@ -434,7 +434,7 @@ __global__ void __launch_bounds__(RZ_TX * RZ_TY) k_resid25(const double* __restr
 // tile rows: column 1 the left halo, columns 2 .. 2 TX + 1 the pairs (even
 // columns, so that a pair is an aligned float2), column 2 TX + 2 the right
 // halo; R2_SW even
-constexpr int R2_TX = 32, R2_TY = 8, R2_KC = 32, R2_SW = 2 * R2_TX + 4;
+constexpr int R2_TX = 32, R2_TY = 8, R2_KC = 16, R2_SW = 2 * R2_TX + 4;
 static inline dim3 r2_grid(const Grid& g) {
   return dim3((g.nx + 2 * R2_TX - 1) / (2 * R2_TX), (g.ny + R2_TY - 1) / R2_TY, (g.nz + R2_KC - 1) / R2_KC);
 }
