@@ -941,19 +941,21 @@ __global__ void __launch_bounds__(256) k_restrict(const T* __restrict__ tf, T* _
 
 // full weighting when every axis is coarsened: the 3 x 3 x 3 fine block of
 // each coarse point, offsets resolved once per axis, separable weights
-// A thread marches RF_KZ coarse planes along z: the fine plane 2K + 1, the
+// A thread marches KZ coarse planes along z: the fine plane 2K + 1, the
 // last of coarse plane K's three, is the first of K + 1's, so its nine
 // values stay in registers (18 loads per coarse point instead of 27).  The
 // sum of every coarse point still runs over its 27 terms in the same order.
+// Large coarse grids take RF_KZ planes per thread; small ones, whose
+// restriction is latency-bound, one.
 constexpr int RF_KZ = 4;
-template <class T>
+template <class T, int KZ>
 __global__ void __launch_bounds__(256) k_restrict_full(const T* __restrict__ tf, T* __restrict__ rc, Grid gf,
                                                        Grid gc, const SolveCtrl* ctrl) {
   pdl_enter();
   if (ctrl->done) return;
   const int I = blockIdx.x * blockDim.x + threadIdx.x;
   const int J = blockIdx.y * blockDim.y + threadIdx.y;
-  const int K0 = blockIdx.z * RF_KZ;
+  const int K0 = blockIdx.z * KZ;
   if (I >= gc.nx || J >= gc.ny) return;
   int xo[3], yo[3];
 #pragma unroll
@@ -972,7 +974,7 @@ __global__ void __launch_bounds__(256) k_restrict_full(const T* __restrict__ tf,
   };
   T pl[3][3][3];  // the fine planes 2K - 1, 2K, 2K + 1
   plane(fine_of(K0, -1, gf.nz, gf.bc[2], 1), pl[0]);
-  for (int K = K0; K < K0 + RF_KZ && K < gc.nz; ++K) {
+  for (int K = K0; K < K0 + KZ && K < gc.nz; ++K) {
     if (K > K0) {
 #pragma unroll
       for (int oy = 0; oy < 3; ++oy)
@@ -1580,9 +1582,11 @@ static void launch_restrict(const MGLevel& L, const MGLevel& C, const T* tf, T* 
                s, tf, rc, L.g, C.g, nn_xfer<T>(L, C), ctrl);
   else if (cz.c[0] == 2 || cz.c[1] == 2 || cz.c[2] == 2)
     launch_pdl(k_restrict_nn<T>, g3(C.g), b, 0, s, tf, rc, L.g, C.g, nn_xfer<T>(L, C), ctrl);
+  else if (cz.c[0] && cz.c[1] && cz.c[2] && C.g.n >= (1LL << 20))
+    launch_pdl(k_restrict_full<T, RF_KZ>, dim3((C.g.nx + 31) / 32, (C.g.ny + 7) / 8, (C.g.nz + RF_KZ - 1) / RF_KZ), b,
+               0, s, tf, rc, L.g, C.g, ctrl);
   else if (cz.c[0] && cz.c[1] && cz.c[2])
-    launch_pdl(k_restrict_full<T>, dim3((C.g.nx + 31) / 32, (C.g.ny + 7) / 8, (C.g.nz + RF_KZ - 1) / RF_KZ), b, 0, s,
-               tf, rc, L.g, C.g, ctrl);
+    launch_pdl(k_restrict_full<T, 1>, g3(C.g), b, 0, s, tf, rc, L.g, C.g, ctrl);
   else
     launch_pdl(k_restrict<T>, g3(C.g), b, 0, s, tf, rc, L.g, C.g, cz, ctrl);
 }
