@@ -48,7 +48,9 @@ TRAFFIC_PER_LAUNCH: dict = {
     "correct": (271.854336 + 144.600320) * 1e6,   # k_correct25vf_tgv256.md
     "mg_pre": (68.070656 + 25.961216) * 1e6,      # k_lvl25_tgv256.md
     "mg_resid": (138.118144 + 39.967488) * 1e6,   # k_lvl25_tgv256.md
-    "resid64": (208.324352 + 48.478720) * 1e6,    # k_resid25_tgv256.md
+    "resid64": (202.877952 + 45.707520) * 1e6,    # k_resid25_tgv256.md
+    "mg_post": (268.986368 + 87.478272) * 1e6,    # k_smooth_upd_tgv256.md
+    "mg_prolong": (75.505920 + 11.468032) * 1e6,  # k_smooth_upd_tgv256.md (the finest k_prolong_cell)
 }
 
 
