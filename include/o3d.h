@@ -125,7 +125,10 @@ typedef struct o3d_params {
                              enough to fill the GPU (at least 152 blocks), except that a
                              V-cycle from zero with one pre-sweep on a level of 2^22
                              points or more runs its pre-smoothing, residual and
-                             restriction as one-pass 2.5D kernels; 1 = one plain kernel
+                             restriction as one-pass 2.5D kernels, and the cycle that
+                             updates the pressure its post-smoothing as one-pass
+                             kernels with the update in the last black pass (so does
+                             an unfused finest level); 1 = one plain kernel
                              per pass (no fused, 2.5D or staged forms); 2 = fused on
                              every level they can serve (same
                              results in all three; 1 and 2 are for comparison and tests) */

@@ -74,3 +74,20 @@ def test_clock_record_summary(tmp_path):
     s = c.summary()
     assert s["sm_mhz"] == 1980 and s["sm_max_mhz"] == 2070
     assert s["reasons"] == ["sw_power_cap"] and s["samples"] == 3
+
+
+def test_roofline_tables_name_timed_kernels():
+    """Every kernel bench.py reports a roofline for has a timing id in the
+    library's o3d_time_kernel, the roofline kernel is one of them, and every
+    DRAM traffic figure belongs to a reported kernel."""
+    sys.path.insert(0, ROOT)
+    import bench
+    from osinco3d_gb300 import o3d
+
+    ids = o3d.Context.KERNELS
+    assert set(bench.KERNEL_BYTES) <= set(ids)
+    assert bench.ROOF_KERNEL in bench.KERNEL_BYTES
+    assert set(bench.TRAFFIC_PER_LAUNCH) <= set(bench.KERNEL_BYTES)
+    assert sorted(ids.values()) == list(range(len(ids)))  # 0 .. 11, the ids o3d_time_kernel accepts
+    src = open(os.path.join(ROOT, "osinco3d_gb300", "csrc", "o3d_api.cu")).read()
+    assert f"kernel > {len(ids) - 1})" in src
