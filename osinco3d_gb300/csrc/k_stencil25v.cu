@@ -977,11 +977,19 @@ __global__ void __launch_bounds__(NT, 3) k_transeq25v(ScalArgs<float> A, int kc)
 // ring of 7 single-field stages of 14 rows x 72 columns, as the scalar's in
 // k_transeq25v, with no conversion pass.
 // ---------------------------------------------------------------------------
+// u* lands beside the pressure ring: plane L in slot L % ZQ, copied with
+// the pressure's plane L + 3 (three planes ahead of its use, in flight
+// without registers; one plane ahead through registers left the kernel
+// waiting on those loads)
+struct TURing {
+  float s[ZQ][TS];
+  float u[ZQ][3][VY * VX];
+};
 template <bool ZON, bool XO>
 __global__ void __launch_bounds__(NT, 3) k_correct25vf(CorrArgs<float, float> A, int kc) {
   pdl_enter();
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  TRing& sm = *reinterpret_cast<TRing*>(smem_raw);
+  TURing& sm = *reinterpret_cast<TURing*>(smem_raw);
   const Grid& g = A.g;
   const int tx = threadIdx.x, ty = threadIdx.y, t = ty * VTX + tx;
   const int i0 = blockIdx.x * VX, j0 = blockIdx.y * VY;
@@ -1002,6 +1010,7 @@ __global__ void __launch_bounds__(NT, 3) k_correct25vf(CorrArgs<float, float> A,
   const bool has_x = t < VY * 6;
   const XCell xc = xcell_of(g, i0, j0, has_x ? t / 6 : 0, t % 6, (3 + (has_x ? t / 6 : 0)) * VW);
 
+  const int ucol = ty * VX + 2 * tx;  // the pair in a u* plane of the ring
   auto issue = [&](int lp, int st) {
     if (lp <= last_centre) {
       const ZPlane z = z_plane(g, k0 + lp);
@@ -1009,6 +1018,12 @@ __global__ void __launch_bounds__(NT, 3) k_correct25vf(CorrArgs<float, float> A,
       const bool full = lp < np;
       if ((un.flags & 1) && (full || (un.flags & 4))) issue_unit(un, A.p, z, g, sbase);
       if (full && has_x) cp4(sbase + (unsigned)xc.dst * 4u, A.p + z.off + xc.xy);
+    }
+    const int L = lp - 3;  // st = lp % ZQ, so u* plane L goes to slot (st + ZQ - 3) % ZQ = L % ZQ
+    if (valid && L >= 0 && L < np) {
+      const long long src = out0 + sz * (k0 + L);
+#pragma unroll
+      for (int a = 0; a < 3; ++a) cp_async<8>(&sm.u[(st + ZQ - 3) % ZQ][a][ucol], A.up[a] + src);
     }
     cp_async_commit();
   };
@@ -1029,9 +1044,6 @@ __global__ void __launch_bounds__(NT, 3) k_correct25vf(CorrArgs<float, float> A,
       q[m] = make_float2(__ldg(f + iia), __ldg(f + iib));
     }
   }
-  float2 us[3];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) us[a] = (valid && np > 0) ? ld_stream2(A.up[a] + out0 + sz * k0) : make_float2(0.f, 0.f);
   cp_async_wait<PD>();
   __syncthreads();
   if constexpr (zon) {
@@ -1088,6 +1100,9 @@ __global__ void __launch_bounds__(NT, 3) k_correct25vf(CorrArgs<float, float> A,
       }
       if (valid) {
         const long long p = out0 + sz * (k0 + lp);
+        float2 us[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) us[a] = lds2(&sm.u[u][a][ucol]);
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
           float na = us[a].x - A.dt * ga[a], nb = us[a].y - A.dt * gb[a];
@@ -1100,10 +1115,6 @@ __global__ void __launch_bounds__(NT, 3) k_correct25vf(CorrArgs<float, float> A,
           mn[a] = fminf(mn[a], fminf(na, nb));
           mx[a] = fmaxf(mx[a], fmaxf(na, nb));
           am[a] = fmaxf(am[a], fmaxf(fabsf(na), fabsf(nb)));
-        }
-        if (lp + 1 < np) {
-#pragma unroll
-          for (int a = 0; a < 3; ++a) us[a] = ld_stream2(A.up[a] + p + sz);
         }
       }
     }
@@ -1156,7 +1167,7 @@ void correct_v_launch(const CorrArgs<float, double>& a, cudaStream_t s) {
 
 template <bool ZON, bool XO>
 void correct_vf_launch(const CorrArgs<float, float>& a, cudaStream_t s) {
-  constexpr size_t bytes = sizeof(TRing);
+  constexpr size_t bytes = sizeof(TURing);
   static std::atomic<bool> attr[64];
   allow_smem_v(k_correct25vf<ZON, XO>, bytes, attr);
   const int kc = v_chunk(a.g, 3);  // the tiling of the FP64-pressure kernel (one record table)
