@@ -45,7 +45,7 @@ TRAFFIC_PER_LAUNCH: dict = {
     "mg_up": (288.510464 + 152.460032) * 1e6,     # k_mg_up_tgv256.md
     "predict": (424.591104 + 348.993024) * 1e6,   # k_predict25v_tgv256.md
     "rhs": (208.823552 + 43.305472) * 1e6,        # k_div25v_tgv256.md (the rhs-writing launch)
-    "correct": (271.854336 + 144.600320) * 1e6,   # k_correct25vf_tgv256.md
+    "correct": (278.680320 + 155.391744) * 1e6,   # k_correct25vf_tgv256.md
     "mg_pre": (68.070656 + 25.961216) * 1e6,      # k_lvl25_tgv256.md
     "mg_resid": (138.118144 + 39.967488) * 1e6,   # k_lvl25_tgv256.md
     "resid64": (202.877952 + 45.707520) * 1e6,    # k_resid25_tgv256.md
