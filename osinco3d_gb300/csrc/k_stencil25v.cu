@@ -290,16 +290,18 @@ __global__ void __launch_bounds__(NT, 2) k_predict25v(PredArgs<float> A, int kc)
 #pragma unroll
     for (int c = 0; c < 3; ++c) q[c][3 + m] = lds2(&sm.s[m][own + c * VW]);
 
+  // ring slots of planes lp, lp + 3 and lp + 3 + PD, advanced each plane
+  int s0 = 0, s3 = 3, s6 = (3 + PD) % ZQ;
 #pragma unroll 1
   for (int lp = 0; lp < np; ++lp) {
     cp_async_wait<PD - 1>();  // group(lp + 3) landed
-    fix(lp + 3, (lp + 3) % ZQ);
+    fix(lp + 3, s3);
     __syncthreads();
-    issue(lp + 3 + PD, (lp + 3 + PD) % ZQ);
-    const float* s = sm.s[lp % ZQ];
+    issue(lp + 3 + PD, s6);
+    const float* s = sm.s[s0];
     if constexpr (zon) {
 #pragma unroll
-      for (int c = 0; c < 3; ++c) q[c][6] = lds2(&sm.s[(lp + 3) % ZQ][own + c * VW]);
+      for (int c = 0; c < 3; ++c) q[c][6] = lds2(&sm.s[s3][own + c * VW]);
     }
     float2 uc[3];
 #pragma unroll
@@ -393,6 +395,9 @@ __global__ void __launch_bounds__(NT, 2) k_predict25v(PredArgs<float> A, int kc)
 #pragma unroll
         for (int m = 0; m < ZQ - 1; ++m) q[c][m] = q[c][m + 1];
     }
+    s0 = s0 == ZQ - 1 ? 0 : s0 + 1;
+    s3 = s3 == ZQ - 1 ? 0 : s3 + 1;
+    s6 = s6 == ZQ - 1 ? 0 : s6 + 1;
   }
   cp_async_wait<0>();
 }
@@ -522,14 +527,16 @@ __global__ void __launch_bounds__(NT, 3) k_div25v(const float* __restrict__ fx, 
   const float wyy = ((wmask & 2) && (j == 0 || j == g.ny - 1)) ? 0.5f : 1.f;
   const float wxa = (((wmask & 1) && (ia == 0 || ia == g.nx - 1)) ? 0.5f : 1.f) * wyy;
   const float wxb = (((wmask & 1) && (ia + 1 == 0 || ia + 1 == g.nx - 1)) ? 0.5f : 1.f) * wyy;
+  // ring slots of planes lp, lp + 3 and lp + 3 + PD, advanced each plane
+  int s0 = 0, s3 = 3, s6 = (3 + PD) % ZQ;
 #pragma unroll 1
   for (int lp = 0; lp < np; ++lp) {
     cp_async_wait<PD - 1>();
-    fix(lp + 3, (lp + 3) % ZQ);
+    fix(lp + 3, s3);
     __syncthreads();
-    issue(lp + 3 + PD, (lp + 3 + PD) % ZQ);
-    const float* s = sm.s[lp % ZQ];
-    if constexpr (zon) q[6] = lds2(&sm.s[(lp + 3) % ZQ][ownz]);
+    issue(lp + 3 + PD, s6);
+    const float* s = sm.s[s0];
+    if constexpr (zon) q[6] = lds2(&sm.s[s3][ownz]);
     float w[10];
 #pragma unroll
     for (int m = 0; m < 5; ++m) {
@@ -583,6 +590,9 @@ __global__ void __launch_bounds__(NT, 3) k_div25v(const float* __restrict__ fx, 
       if (da > mx) { mx = da; imx = p; }  // k ascends, a before b: the first max is kept
       if (db > mx) { mx = db; imx = p + 1; }
     }
+    s0 = s0 == ZQ - 1 ? 0 : s0 + 1;
+    s3 = s3 == ZQ - 1 ? 0 : s3 + 1;
+    s6 = s6 == ZQ - 1 ? 0 : s6 + 1;
   }
   cp_async_wait<0>();
   if (part) {
@@ -887,13 +897,15 @@ __global__ void __launch_bounds__(NT, 3) k_transeq25v(ScalArgs<float> A, int kc)
     for (int m = 0; m < 3; ++m) q[3 + m] = lds2(&sm.s[m][own]);
   }
   float s_hi[3] = {0.f, 0.f, 0.f}, s_lo[3] = {0.f, 0.f, 0.f};
+  // ring slots of planes lp, lp + 3 and lp + 3 + PD, advanced each plane
+  int s0 = 0, s3 = 3, s6 = (3 + PD) % ZQ;
 #pragma unroll 1
   for (int lp = 0; lp < np; ++lp) {
     cp_async_wait<PD - 1>();
     __syncthreads();
-    issue(lp + 3 + PD, (lp + 3 + PD) % ZQ);
-    const float* s = sm.s[lp % ZQ];
-    if constexpr (zon) q[6] = lds2(&sm.s[(lp + 3) % ZQ][own]);
+    issue(lp + 3 + PD, s6);
+    const float* s = sm.s[s0];
+    if constexpr (zon) q[6] = lds2(&sm.s[s3][own]);
     float w[10];
 #pragma unroll
     for (int m = 0; m < 5; ++m) {
@@ -961,6 +973,9 @@ __global__ void __launch_bounds__(NT, 3) k_transeq25v(ScalArgs<float> A, int kc)
       __stcs(reinterpret_cast<float2*>(A.phi_out + p), make_float2(co[0], co[1]));
       if (lp + 1 < np) load_in(p + sz);
     }
+    s0 = s0 == ZQ - 1 ? 0 : s0 + 1;
+    s3 = s3 == ZQ - 1 ? 0 : s3 + 1;
+    s6 = s6 == ZQ - 1 ? 0 : s6 + 1;
   }
   cp_async_wait<0>();
   double r[3];
